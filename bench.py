@@ -1,0 +1,363 @@
+#!/usr/bin/env python
+"""Coupled PSM lattice-step benchmark (MLUPS and HBM roofline fraction).
+
+Workload: periodic 256^3 lattice, tau = 0.55, 2000 spheres of radius 8 at
+seeded non-overlapping uniform random centres (solid fraction 0.256),
+velocities N(0, 0.01), angular velocities N(0, 1e-3), prescribed kinematics
+(x += v per step, periodic wrap, ghost images appended as LIGGGHTS would).
+A step is one coupling cycle: voxelize the spheres, collide-stream the whole
+lattice with the PSM dynamics, sum per-particle force and torque.
+
+MLUPS = lattice cells x steps / seconds / 1e6 (all cells, solid included).
+
+Headline `value`: FP32-deviation form, particle tables already in HBM, timed
+with CUDA events on the launching stream.  `fp64` carries the FP64 drop-in
+form on the same inputs, and `force_rel_err_fp32_vs_fp64` the per-particle
+force error between the two after the run.  `e2e` is the FP32 form through
+the C ABI (lbdem_cycle) with host buffers: the particle table copy in, the
+forces copy out and the per-step synchronisation are inside the timed region.
+
+`--impl reference` times the CPU oracle (a restatement of the reference's
+path; the reference itself needs Palabos, LIGGGHTS and MPI) on the host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG = ROOT / "lbdemcoupling-public_gb300"
+for _p in (str(ROOT), str(PKG)):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "coupled PSM MLUPS & %HBM roofline, FP32 vs FP64 form at force err ≤1e-4"
+SHAPE = (256, 256, 256)
+TAU = 0.55
+SEED = 2024
+WORKLOAD = "monodisperse suspension, periodic 256^3, 2000 spheres r=8, tau=0.55, prescribed kinematics"
+BYTES_PER_CELL = {"fp32": 2 * 19 * 4 + 4, "fp64": 2 * 19 * 8 + 4}  # 19 loads + 19 stores + voxel word
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def profiled_traffic():
+    """DRAM bytes per collide-stream launch from the committed ncu summary."""
+    p = ROOT / "profiles" / "collide_stream_traffic.txt"
+    out = {}
+    if p.exists():
+        for line in p.read_text().splitlines():
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] in ("fp32", "fp64"):
+                try:
+                    out[parts[0]] = float(parts[1])
+                except ValueError:
+                    pass
+    return out
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms while running."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc is not None:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [l for l in out.splitlines() if l.strip()]
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for l in getattr(self, "lines", []):
+            f = [x.strip() for x in l.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, val in zip(names, f[5:9]):
+                if val.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_tables(n_steps: int):
+    """Per-step particle tables (ghost images included) for prescribed kinematics."""
+    import workloads as W
+    import lbdem
+    _, p = W.monodisperse_256(SEED)
+    recs, host = [], []
+    for _ in range(n_steps):
+        g = W.with_ghosts(p, SHAPE)
+        recs.append(lbdem.pack_records(g.x, g.v, g.w, g.r, g.tag))
+        host.append(g)
+        p = W.advance(p, SHAPE)
+    offs = np.cumsum([0] + [r.shape[0] for r in recs])
+    return np.concatenate(recs), offs, host, p.n
+
+
+def run_device(prec_name: str, table, offs, steps: int, warmup: int, max_n: int, max_tag: int, device: int):
+    import torch
+    import lbdem
+    prec = lbdem.PREC_FP32_DEV if prec_name == "fp32" else lbdem.PREC_FP64
+    lat = lbdem.Lattice(*SHAPE, 1.0 / TAU, precision=prec, max_particles=max_n, max_tag=max_tag,
+                        max_radius=8.0, device=device)
+    stream = torch.cuda.Stream(device=device)
+    lat.set_stream(stream.cuda_stream)
+    d_tab = torch.from_numpy(table).to(f"cuda:{device}")
+    d_out = torch.zeros(6 * max_n, dtype=torch.float64, device=f"cuda:{device}")
+    base = d_tab.data_ptr()
+    torch.cuda.synchronize(device)
+
+    def step(s):
+        n = int(offs[s + 1] - offs[s])
+        lat.set_particles_device(n, base + int(offs[s]) * 12 * 8)
+        lat.collide_and_stream()
+        lat.get_forces_device(d_out.data_ptr())
+
+    with torch.cuda.stream(stream):
+        for s in range(warmup):
+            step(s)
+        torch.cuda.synchronize(device)
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True),
+               torch.cuda.Event(enable_timing=True)) for _ in range(steps)]
+        t0 = torch.cuda.Event(enable_timing=True)
+        t1 = torch.cuda.Event(enable_timing=True)
+        l0 = lat.launch_count()
+        with ClockSampler(device) as clk:
+            torch.cuda.synchronize(device)
+            t0.record(stream)
+            for k in range(steps):
+                s = warmup + k
+                n = int(offs[s + 1] - offs[s])
+                e_a, e_b, e_c = ev[k]
+                e_a.record(stream)
+                lat.set_particles_device(n, base + int(offs[s]) * 12 * 8)
+                e_b.record(stream)
+                lat.collide_and_stream()
+                e_c.record(stream)
+                lat.get_forces_device(d_out.data_ptr())
+            t1.record(stream)
+            torch.cuda.synchronize(device)
+        launches = lat.launch_count() - l0
+    total_ms = t0.elapsed_time(t1)
+    k2 = [a.elapsed_time(b) for a, b, _ in ev]
+    k1 = [b.elapsed_time(c) for _, b, c in ev]
+    n_last = int(offs[warmup + steps] - offs[warmup + steps - 1])
+    F = d_out[: 3 * n_last].cpu().numpy().reshape(n_last, 3)
+    errs = lat.device_errors()
+    lat.close()
+    return {"total_ms": total_ms, "k1_ms": float(np.mean(k1)), "k2_ms": float(np.mean(k2)),
+            "k1_ms_min": float(np.min(k1)), "launches": launches, "F": F, "clocks": clk.summary(),
+            "device_errors": errs}
+
+
+def run_e2e(host_tables, steps: int, warmup: int, max_n: int, max_tag: int, device: int):
+    """FP32 form through lbdem_cycle with host buffers (copies and sync in the timed region)."""
+    import lbdem
+    lat = lbdem.Lattice(*SHAPE, 1.0 / TAU, precision=lbdem.PREC_FP32_DEV, max_particles=max_n,
+                        max_tag=max_tag, max_radius=8.0, device=device)
+    F = np.zeros((max_n, 3))
+    T = np.zeros((max_n, 3))
+    for s in range(warmup):
+        g = host_tables[s]
+        lat.cycle(g.x, g.v, g.w, g.r, g.tag, F=F[: g.n], T=T[: g.n])
+    h2d = d2h = 0
+    t0 = time.perf_counter()
+    for k in range(steps):
+        g = host_tables[warmup + k]
+        lat.cycle(g.x, g.v, g.w, g.r, g.tag, F=F[: g.n], T=T[: g.n])
+        h2d += g.n * 12 * 8
+        d2h += g.n * 6 * 8 + 4
+    dt = time.perf_counter() - t0
+    lat.close()
+    return dt, h2d / steps, d2h / steps
+
+
+def cpu_oracle_mlups(host_tables, budget_s: float, max_cycles: int, threads: int):
+    """Bounded sample of the same workload on the CPU oracle (full 256^3 cycles)."""
+    from oracle import psm_oracle
+    ol = psm_oracle.OracleLattice(*SHAPE, 1.0 / TAU, threads=threads)
+    done = 0
+    t0 = time.perf_counter()
+    while done < max_cycles:
+        g = host_tables[done % len(host_tables)]
+        ol.set_particles(g.x, g.v, g.w, g.r, g.tag)
+        ol.collide_and_stream()
+        ol.get_forces()
+        done += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    N = int(np.prod(SHAPE))
+    return N * done / dt / 1e6, done, dt
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=1000)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-oracle work")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        ap.error("--warmup must be >= 3")
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    threads = os.cpu_count() or 1
+    N = int(np.prod(SHAPE))
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        import workloads as W
+        _, p = W.monodisperse_256(SEED)
+        tables = []
+        q = p
+        for _ in range(min(args.warmup + args.steps, 64)):
+            tables.append(W.with_ghosts(q, SHAPE))
+            q = W.advance(q, SHAPE)
+        from oracle import psm_oracle
+        ol = psm_oracle.OracleLattice(*SHAPE, 1.0 / TAU, threads=threads)
+        for s in range(min(args.warmup, 1)):
+            g = tables[s]
+            ol.set_particles(g.x, g.v, g.w, g.r, g.tag); ol.collide_and_stream(); ol.get_forces()
+        budget = 120.0
+        done = 0
+        t0 = time.perf_counter()
+        while done < args.steps and time.perf_counter() - t0 < budget:
+            g = tables[(done + 1) % len(tables)]
+            ol.set_particles(g.x, g.v, g.w, g.r, g.tag); ol.collide_and_stream(); ol.get_forces()
+            done += 1
+        dt = time.perf_counter() - t0
+        mlups = N * done / dt / 1e6
+        sample = f"{done} of {args.steps} coupling cycles on the full 256^3 workload (time-bounded)"
+        print(json.dumps({
+            "impl": "reference", "metric": METRIC, "value": mlups, "unit": "MLUPS", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * dt / max(done, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": {"workload": WORKLOAD, "form": "fp64 CPU oracle"},
+            "cpu_baseline": {"value": mlups, "unit": "MLUPS", "cores": threads, "kind": "port", "sample": sample},
+            "e2e": {"value": mlups, "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        }))
+        return
+
+    import torch
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    device = local if world > 1 else 0
+    table, offs, host, n_local = build_tables(args.warmup + args.steps)
+    max_n = int(np.max(np.diff(offs)))
+    max_tag = n_local + 1
+
+    if dist:
+        dist.barrier()
+    r32 = run_device("fp32", table, offs, args.steps, args.warmup, max_n, max_tag, device)
+    r64 = run_device("fp64", table, offs, args.steps, args.warmup, max_n, max_tag, device)
+    e2e_s, h2d, d2h = run_e2e(host, args.steps, args.warmup, max_n, max_tag, device)
+
+    t32 = r32["total_ms"]
+    if dist:
+        t = torch.tensor([t32, r64["total_ms"], e2e_s], dtype=torch.float64, device=f"cuda:{device}")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        t32, t64, e2e_s = (float(v) for v in t.tolist())
+    else:
+        t64 = r64["total_ms"]
+    if rank != 0:
+        dist.destroy_process_group()
+        return
+
+    peak, peak_kind = peaks()
+    traffic = profiled_traffic()
+    value = world * N * args.steps / (t32 * 1e-3) / 1e6
+    v64 = world * N * args.steps / (t64 * 1e-3) / 1e6
+    ach32 = BYTES_PER_CELL["fp32"] * N / (r32["k1_ms"] * 1e-3) / 1e9
+    ach64 = BYTES_PER_CELL["fp64"] * N / (r64["k1_ms"] * 1e-3) / 1e9
+    F32, F64 = r32["F"], r64["F"]
+    ferr = float(np.max(np.abs(F32 - F64)) / np.max(np.abs(F64)))
+
+    cpu = None
+    if not args.no_cpu_baseline:
+        mlups, cycles, secs = cpu_oracle_mlups(host, args.cpu_budget, 1000, threads)
+        cpu = {"value": mlups, "unit": "MLUPS", "cores": threads, "kind": "port",
+               "sample": f"{cycles} coupling cycles of the same 256^3 workload in {secs:.1f} s (FP64 oracle)"}
+
+    out = {
+        "metric": METRIC, "value": value, "unit": "MLUPS", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": t32 / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "form": "fp32 deviation populations, fp64 force/torque sums",
+                   "cells": N, "particles_local": n_local, "particles_with_ghosts_max": max_n,
+                   "l2": "inputs larger than L2 (populations 1.27 GB fp32 / 2.55 GB fp64)",
+                   "parallelism": "replicas" if world > 1 else "single GPU"},
+        "roofline": {"bound": "hbm", "achieved": ach32, "peak": peak, "unit": "GB/s", "frac": ach32 / peak,
+                     "traffic": traffic.get("fp32"), "kernel": "k_collide_stream<float>",
+                     "bytes_per_cell": BYTES_PER_CELL["fp32"], "peak_source": peak_kind,
+                     "k1_ms": r32["k1_ms"], "k2_voxelize_ms": r32["k2_ms"]},
+        "fp64": {"value": v64, "unit": "MLUPS", "ms_per_step": t64 / args.steps,
+                 "roofline": {"bound": "hbm", "achieved": ach64, "peak": peak, "unit": "GB/s",
+                              "frac": ach64 / peak, "traffic": traffic.get("fp64"),
+                              "kernel": "k_collide_stream<double>", "bytes_per_cell": BYTES_PER_CELL["fp64"],
+                              "k1_ms": r64["k1_ms"], "k2_voxelize_ms": r64["k2_ms"]}},
+        "force_rel_err_fp32_vs_fp64": ferr,
+        "e2e": {"value": world * N * args.steps / e2e_s / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h},
+        "cpu_baseline": cpu,
+        "clocks": r32["clocks"],
+        "gpu_launches": r32["launches"],
+        "device_errors": r32["device_errors"] | r64["device_errors"],
+    }
+    print(json.dumps(out))
+    if dist:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,186 @@
+/*
+ * lbdem_gpu.h -- C ABI of the GB300 partially-saturated-cells (PSM) lattice step.
+ *
+ * One handle owns one D3Q19 lattice resident in GPU memory together with its
+ * per-cell coupling state (solid fraction, owner particle tag, particle surface
+ * velocity) and the per-particle force/torque accumulators.  A coupling cycle
+ * of the LBDEMcoupling reference maps onto three calls:
+ *
+ *   reference (LBDEMcoupling)                         this ABI
+ *   setSpheresOnLattice(...)                          lbdem_set_particles
+ *     src/ibDataExchangeWrappers3D.hh:33-146            (voxelization kernel)
+ *   lattice.collideAndStream() with IBcompositeDynamics lbdem_collide_and_stream
+ *     src/ibCompositeDynamics3D.hh:130-203              (fused collide-stream kernel,
+ *                                                       force/torque reduction fused)
+ *   getForcesFromLattice(...)                         lbdem_get_forces
+ *     src/ibDataExchangeWrappers3D.hh:160-246           (reads back F and T)
+ *
+ * Conventions
+ *  - Every call returns lbdem_status; LBDEM_OK is 0.  lbdem_last_error() gives
+ *    a human-readable message for the last failing call on a handle.
+ *  - Lattice units throughout (the caller converts with PhysUnits3D, exactly as
+ *    the reference's wrappers do before calling SetSingleSphere3D).
+ *  - Fields are laid out [component][x][y][z] with z fastest (Palabos order).
+ *  - Populations are stored as f̄_i = f_i - t_i (Palabos' storage convention),
+ *    in double (LBDEM_PREC_FP64, the drop-in form) or float
+ *    (LBDEM_PREC_FP32_DEV, deviation form; force/torque still accumulate in
+ *    double).
+ *  - A handle is not thread-safe: one host thread per handle.  All GPU work of
+ *    a handle is ordered on one CUDA stream (its own, or one set with
+ *    lbdem_set_stream).  Host buffers belong to the caller; device memory
+ *    belongs to the handle.
+ *  - Functions ending in _device take device pointers and do not synchronize.
+ */
+#ifndef LBDEM_GPU_H
+#define LBDEM_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+    LBDEM_OK = 0,
+    LBDEM_ERR_INVALID_ARG = 1,  /* null handle/pointer, bad size, bad enum        */
+    LBDEM_ERR_CUDA = 2,         /* a CUDA runtime call failed                      */
+    LBDEM_ERR_OUT_OF_MEMORY = 3,/* device or pinned allocation failed              */
+    LBDEM_ERR_CAPACITY = 4,     /* more particles / tags / overlaps than reserved  */
+    LBDEM_ERR_DEVICE = 5,       /* the device error word is non-zero (see below)   */
+    LBDEM_ERR_NO_DEVICE = 6     /* no CUDA device, or not a GB300-class device     */
+} lbdem_status;
+
+/* Bits of the device error word (lbdem_get_device_errors). */
+#define LBDEM_DEVERR_TILE_LIST     0x1u  /* a tile is overlapped by more spheres than fit   */
+#define LBDEM_DEVERR_PAIR_CAPACITY 0x2u  /* sphere/tile overlap list capacity exceeded      */
+#define LBDEM_DEVERR_TAG_RANGE     0x4u  /* a particle tag is < 1 or > max_tag              */
+#define LBDEM_DEVERR_UNMAPPED_TAG  0x8u  /* a solid cell names a tag with no particle       */
+#define LBDEM_DEVERR_RADIUS        0x10u /* a radius is not finite, <= 0 or > max_radius    */
+
+typedef enum {
+    LBDEM_PREC_FP64 = 0,     /* populations in double: the drop-in form            */
+    LBDEM_PREC_FP32_DEV = 1  /* populations f̄ = f - t_i in float, F/T in double   */
+} lbdem_precision;
+
+typedef enum {
+    LBDEM_FIELD_POPULATIONS = 0,      /* f̄_i, [19][N], lattice element type           */
+    LBDEM_FIELD_SOLID_FRACTION = 1,   /* double[N]  (IBscalarQuantity SolidFraction)   */
+    LBDEM_FIELD_PARTICLE_ID = 2,      /* int32[N]   (IBscalarQuantity ParticleId)      */
+    LBDEM_FIELD_PARTICLE_VELOCITY = 3,/* [3][N] lattice type (IBvectorQuantity ParticleVelocity) */
+    LBDEM_FIELD_HYDRO_FORCE = 4,      /* [3][N] lattice type (IBvectorQuantity HydrodynamicForce);
+                                         needs LBDEM_FLAG_CELL_FORCE                       */
+    LBDEM_FIELD_DENSITY = 5,          /* double[N]  rho = 1 + sum f̄_i                    */
+    LBDEM_FIELD_VELOCITY = 6,         /* double[3][N]  u = j / rho                        */
+    LBDEM_FIELD_SUBCELL_COUNT = 7     /* uint8[N]   solid sub-cell count n, sf = n/125    */
+} lbdem_field;
+
+/* Keep the per-cell hydrodynamic force field (for export).  Off by default: the
+ * force/torque sum is fused into the collide-stream kernel and needs no field. */
+#define LBDEM_FLAG_CELL_FORCE 0x1
+
+typedef struct {
+    int32_t nx, ny, nz;       /* lattice extent in cells                              */
+    int32_t periodic[3];      /* 1 = periodic axis, 0 = half-way bounce-back walls    */
+    double omega;             /* BGK relaxation frequency 1/tau, 0 < omega < 2        */
+    double body_force[3];     /* Guo body-force acceleration; zero = reference form   */
+    int32_t precision;        /* lbdem_precision                                      */
+    int32_t device;           /* CUDA device ordinal                                  */
+    int32_t max_particles;    /* capacity of one particle list, ghosts included       */
+    int32_t max_tag;          /* largest particle tag that may appear (< 2^25)        */
+    double max_radius;        /* largest sphere radius in lattice units               */
+    int32_t flags;            /* LBDEM_FLAG_*                                         */
+    int32_t reserved;
+} lbdem_config;
+
+typedef struct lbdem_handle lbdem_handle;
+
+/* Fills cfg with defaults: 32^3 periodic, omega 1, FP64, device 0,
+ * 1024 particles, max_tag 1<<20, max_radius 16. */
+void lbdem_config_default(lbdem_config* cfg);
+
+/* Creates a lattice at rest (f̄ = 0, i.e. rho = 1, u = 0; Palabos
+ * lattice.initialize()) with every cell free of particles. */
+lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out);
+lbdem_status lbdem_destroy(lbdem_handle* h);
+const char* lbdem_last_error(const lbdem_handle* h);
+const char* lbdem_status_string(lbdem_status s);
+
+/* Orders the handle's GPU work on the given cudaStream_t (NULL: back to the
+ * handle's own stream). */
+lbdem_status lbdem_set_stream(lbdem_handle* h, void* cuda_stream);
+lbdem_status lbdem_synchronize(lbdem_handle* h);
+
+/* Uniform equilibrium: f̄_i = feq_i(rhoBar, j = (1 + rhoBar) u) in every cell
+ * (Palabos initializeAtEquilibrium). */
+lbdem_status lbdem_init_equilibrium(lbdem_handle* h, double rho_bar, const double u[3]);
+
+/* Whole population field, [19][N] of the lattice element type, natural order
+ * (f̄_i at cell x), independent of the in-place streaming phase. */
+lbdem_status lbdem_set_populations(lbdem_handle* h, const void* host_f);
+lbdem_status lbdem_get_populations(lbdem_handle* h, void* host_f);
+
+/* setSpheresOnLattice / SetSingleSphere3D::process for n spheres applied in
+ * index order (LIGGGHTS local atoms first, then ghost images, which repeat the
+ * owner's tag).  x, v, omega: [n][3] doubles; r: [n]; tag: [n] int32 >= 1.
+ * init_vel != 0 sets the populations of fully covered cells to the equilibrium
+ * at the particle surface velocity (initVelFlag, src/ibProcessors3D.hh:107-108).
+ * Host buffers; returns after the data has been staged (work is queued).
+ * Replaces src/ibDataExchangeWrappers3D.hh:33-146 and src/ibProcessors3D.hh:53-184. */
+lbdem_status lbdem_set_particles(lbdem_handle* h, int32_t n, const double* x, const double* v,
+                                 const double* omega, const double* r, const int32_t* tag,
+                                 int32_t init_vel);
+
+/* Same, with the particle table already in device memory: rec is [n][12]
+ * doubles {x0,x1,x2, v0,v1,v2, w0,w1,w2, r, tag, 0} (tag stored as a double). */
+lbdem_status lbdem_set_particles_device(lbdem_handle* h, int32_t n, const double* rec,
+                                        int32_t init_vel);
+
+/* One lattice time step: PSM collision in every cell
+ * (IBcompositeDynamics::collide, src/ibCompositeDynamics3D.hh:130-203)
+ * followed by streaming, with the per-particle force and torque of
+ * SumForceTorque3D (src/ibProcessors3D.hh:203-263) accumulated in double in
+ * the same pass.  The sums refer to the particle list of the last
+ * lbdem_set_particles call. */
+lbdem_status lbdem_collide_and_stream(lbdem_handle* h);
+
+/* Forces and torques of the last lbdem_collide_and_stream, lattice units,
+ * [n][3] doubles indexed like the particle list: the entry of the first list
+ * index carrying a tag holds that tag's sum, ghost-image entries are zero
+ * (the reference's force/torque vectors, src/ibDataExchangeWrappers3D.hh:194-218).
+ * Synchronizes; returns LBDEM_ERR_DEVICE if the device error word is set. */
+lbdem_status lbdem_get_forces(lbdem_handle* h, int32_t n, double* force, double* torque);
+
+/* Device-pointer variant: copies 3n forces then 3n torques into dev_ft
+ * (6n doubles) on the handle's stream; does not synchronize. */
+lbdem_status lbdem_get_forces_device(lbdem_handle* h, int32_t n, double* dev_ft);
+
+/* One coupling cycle (set particles, step, read forces) with host buffers. */
+lbdem_status lbdem_cycle(lbdem_handle* h, int32_t n, const double* x, const double* v,
+                         const double* omega, const double* r, const int32_t* tag,
+                         int32_t init_vel, double* force, double* torque);
+
+/* Copies one field to host memory (see lbdem_field for types and sizes). */
+lbdem_status lbdem_get_field(lbdem_handle* h, int32_t which, void* host_buf);
+
+/* Total mass sum_x sum_i (f̄_i + t_i), accumulated in double on the GPU. */
+lbdem_status lbdem_mass(lbdem_handle* h, double* mass);
+
+/* Reads and clears the device error word (LBDEM_DEVERR_* bits). */
+lbdem_status lbdem_get_device_errors(lbdem_handle* h, uint32_t* bits);
+
+/* Number of completed lattice steps. */
+lbdem_status lbdem_get_step(lbdem_handle* h, int64_t* step);
+
+/* Bytes of device memory held by the handle. */
+lbdem_status lbdem_device_bytes(lbdem_handle* h, size_t* bytes);
+
+/* Kernel launches issued by this handle since creation (all kernels of this
+ * library; memset/memcpy not counted). */
+lbdem_status lbdem_get_launch_count(lbdem_handle* h, int64_t* count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* LBDEM_GPU_H */

@@ -1,0 +1,185 @@
+// Field export and initialisation kernels: population layout conversion for the
+// in-place AA storage, uniform equilibrium, density/velocity, total mass and the
+// voxel-word fields (the data of GetScalar/VectorQuantityFromDynamicsFunctional,
+// src/ibDataWritingFunctionals3D.hh:32-114).
+#include "lbdem_internal.h"
+
+namespace lbdem {
+namespace {
+
+// Index of the slot that holds population i of cell (x,y,z) in the AA layout.
+// phase 0 (even number of completed steps): slot (i, x).
+// phase 1: slot (opp i, x - c_i), or (i, x) when x - c_i is beyond a wall.
+__device__ __forceinline__ size_t slot_index(int i, int x, int y, int z, int phase, const Geom& g) {
+    if (phase == 0 || i == 0) return (size_t)i * g.N + ((size_t)x * g.ny + y) * g.nz + z;
+    int X = x - cx(i), Y = y - cy(i), Z = z - cz(i);
+    bool out = false;
+    if (X < 0 || X >= g.nx) { if (g.per[0]) X = X < 0 ? X + g.nx : X - g.nx; else out = true; }
+    if (Y < 0 || Y >= g.ny) { if (g.per[1]) Y = Y < 0 ? Y + g.ny : Y - g.ny; else out = true; }
+    if (Z < 0 || Z >= g.nz) { if (g.per[2]) Z = Z < 0 ? Z + g.nz : Z - g.nz; else out = true; }
+    if (out) return (size_t)i * g.N + ((size_t)x * g.ny + y) * g.nz + z;
+    return (size_t)opp(i) * g.N + ((size_t)X * g.ny + Y) * g.nz + Z;
+}
+
+__device__ __forceinline__ void decompose(size_t c, const Geom& g, int& x, int& y, int& z) {
+    z = (int)(c % g.nz);
+    const size_t r = c / g.nz;
+    y = (int)(r % g.ny);
+    x = (int)(r / g.ny);
+}
+
+template <typename T>
+__global__ void k_pop_gather(const T* __restrict__ f, T* __restrict__ out, int i, int phase, Geom g) {
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.N; c += (size_t)gridDim.x * blockDim.x) {
+        int x, y, z;
+        decompose(c, g, x, y, z);
+        size_t s;
+        switch (i) {
+#define CASE(k) case k: s = slot_index(k, x, y, z, phase, g); break;
+            CASE(0) CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8) CASE(9)
+            CASE(10) CASE(11) CASE(12) CASE(13) CASE(14) CASE(15) CASE(16) CASE(17) CASE(18)
+#undef CASE
+            default: s = c;
+        }
+        out[c] = f[s];
+    }
+}
+
+template <typename T>
+__global__ void k_pop_scatter(T* __restrict__ f, const T* __restrict__ in, int i, int phase, Geom g) {
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.N; c += (size_t)gridDim.x * blockDim.x) {
+        int x, y, z;
+        decompose(c, g, x, y, z);
+        size_t s;
+        switch (i) {
+#define CASE(k) case k: s = slot_index(k, x, y, z, phase, g); break;
+            CASE(0) CASE(1) CASE(2) CASE(3) CASE(4) CASE(5) CASE(6) CASE(7) CASE(8) CASE(9)
+            CASE(10) CASE(11) CASE(12) CASE(13) CASE(14) CASE(15) CASE(16) CASE(17) CASE(18)
+#undef CASE
+            default: s = c;
+        }
+        f[s] = in[c];
+    }
+}
+
+template <typename T>
+struct EqVals { T v[Q]; };
+
+template <typename T>
+__global__ void k_fill_equilibrium(T* __restrict__ f, EqVals<T> e, Geom g) {
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.N; c += (size_t)gridDim.x * blockDim.x) {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) f[(size_t)i * g.N + c] = e.v[i];
+    }
+}
+
+template <typename T>
+__global__ void k_macro(const T* __restrict__ f, int phase, double* __restrict__ rho, double* __restrict__ u,
+                        Geom g) {
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.N; c += (size_t)gridDim.x * blockDim.x) {
+        int x, y, z;
+        decompose(c, g, x, y, z);
+        double rb = 0, jx = 0, jy = 0, jz = 0;
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            const double v = (double)f[slot_index(i, x, y, z, phase, g)];
+            rb += v;
+            if (cx(i)) jx += cx(i) * v;
+            if (cy(i)) jy += cy(i) * v;
+            if (cz(i)) jz += cz(i) * v;
+        }
+        const double r = 1.0 + rb;
+        if (rho) rho[c] = r;
+        if (u) { u[c] = jx / r; u[g.N + c] = jy / r; u[2 * g.N + c] = jz / r; }
+    }
+}
+
+constexpr int MASS_THREADS = 256;
+template <typename T>
+__global__ void __launch_bounds__(MASS_THREADS) k_mass(const T* __restrict__ f, double* __restrict__ out, Geom g) {
+    __shared__ double s_part[MASS_THREADS / 32];
+    const size_t total = (size_t)Q * g.N;
+    double acc = 0;
+    for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < total; k += (size_t)gridDim.x * blockDim.x)
+        acc += (double)f[k];
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) s_part[threadIdx.x >> 5] = acc;
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        double v = threadIdx.x < MASS_THREADS / 32 ? s_part[threadIdx.x] : 0.0;
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+        if (threadIdx.x == 0) atomicAdd(out, v);
+    }
+}
+
+__global__ void k_vox_fields(const uint32_t* __restrict__ vox, double* __restrict__ sf, int32_t* __restrict__ id,
+                             uint8_t* __restrict__ nsub, Geom g) {
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.N; c += (size_t)gridDim.x * blockDim.x) {
+        const uint32_t w = vox[c];
+        const uint32_t n = w & VOX_NMASK;
+        if (sf) sf[c] = (1.0 / 125.0) * (double)n;   // fraction * n, src/ibProcessors3D.hh:157
+        if (id) id[c] = (int32_t)(w >> VOX_NBITS);
+        if (nsub) nsub[c] = (uint8_t)n;
+    }
+}
+
+inline unsigned grid_for(size_t n, int threads) {
+    size_t b = (n + threads - 1) / threads;
+    const size_t cap = 152 * 32;
+    return (unsigned)(b < cap ? (b > 0 ? b : 1) : cap);
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_pop_gather(const T* f, T* out, int i, int phase, Geom g, cudaStream_t s) {
+    k_pop_gather<T><<<grid_for(g.N, 256), 256, 0, s>>>(f, out, i, phase, g);
+    return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_pop_scatter(T* f, const T* in, int i, int phase, Geom g, cudaStream_t s) {
+    k_pop_scatter<T><<<grid_for(g.N, 256), 256, 0, s>>>(f, in, i, phase, g);
+    return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_fill_equilibrium(T* f, double rho_bar, const double* u, Geom g, cudaStream_t s) {
+    // Palabos iniCellAtEquilibrium: j = rho u; feq_i = t_i [rhoBar + 3 c.j + invRho (4.5 (c.j)^2 - 1.5 j.j)]
+    EqVals<T> e;
+    const T rb = T(rho_bar);
+    const T rho = T(1) + rb;
+    const T j[3] = {rho * T(u[0]), rho * T(u[1]), rho * T(u[2])};
+    const T jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
+    const T invRho = T(1) / rho;
+    for (int i = 0; i < Q; ++i) {
+        const T cj = T(cx(i)) * j[0] + T(cy(i)) * j[1] + T(cz(i)) * j[2];
+        e.v[i] = T(wt(i)) * (rb + T(3) * cj + invRho * (T(4.5) * cj * cj - T(1.5) * jSqr));
+    }
+    k_fill_equilibrium<T><<<grid_for(g.N, 256), 256, 0, s>>>(f, e, g);
+    return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_macro(const T* f, int phase, double* rho, double* u, Geom g, cudaStream_t s) {
+    k_macro<T><<<grid_for(g.N, 256), 256, 0, s>>>(f, phase, rho, u, g);
+    return cudaGetLastError();
+}
+template <typename T>
+cudaError_t launch_mass(const T* f, double* out, Geom g, cudaStream_t s) {
+    k_mass<T><<<grid_for((size_t)Q * g.N, MASS_THREADS), MASS_THREADS, 0, s>>>(f, out, g);
+    return cudaGetLastError();
+}
+cudaError_t launch_vox_fields(const uint32_t* vox, double* sf, int32_t* id, uint8_t* nsub, Geom g, cudaStream_t s) {
+    k_vox_fields<<<grid_for(g.N, 256), 256, 0, s>>>(vox, sf, id, nsub, g);
+    return cudaGetLastError();
+}
+
+#define INST(T)                                                                                      \
+    template cudaError_t launch_pop_gather<T>(const T*, T*, int, int, Geom, cudaStream_t);           \
+    template cudaError_t launch_pop_scatter<T>(T*, const T*, int, int, Geom, cudaStream_t);          \
+    template cudaError_t launch_fill_equilibrium<T>(T*, double, const double*, Geom, cudaStream_t);  \
+    template cudaError_t launch_macro<T>(const T*, int, double*, double*, Geom, cudaStream_t);       \
+    template cudaError_t launch_mass<T>(const T*, double*, Geom, cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
+
+}  // namespace lbdem

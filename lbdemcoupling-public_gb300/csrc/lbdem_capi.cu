@@ -1,0 +1,566 @@
+// C ABI of liblbdem_gb300: handle life cycle, device memory, staging buffers
+// and the launch sequence of one coupling cycle.  See include/lbdem_gpu.h.
+#include "lbdem_gpu.h"
+#include "lbdem_internal.h"
+
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+#include <string>
+
+using namespace lbdem;
+
+struct lbdem_handle {
+    lbdem_config cfg{};
+    Geom g{};
+    int prec = 0;
+    size_t esz = 8;
+    int device = 0;
+    cudaStream_t own_stream = nullptr;
+    cudaStream_t stream = nullptr;
+
+    void* f = nullptr;          // [19][N] populations
+    uint32_t* vox = nullptr;    // [N] n | tag << 7
+    void* up = nullptr;         // [3][N]
+    void* cf = nullptr;         // [3][N] optional
+    double* btab = nullptr;     // [126]
+
+    int cap = 0;
+    double* d_rec = nullptr;    // [cap][12]
+    SphereDev* d_sph = nullptr; // [cap]
+    int* d_tag2slot = nullptr;  // [max_tag + 1]
+    int ntiles = 0;
+    int* d_tile_off = nullptr;  // [ntiles + 1]
+    int* d_cursor = nullptr;    // [ntiles]
+    int pair_cap = 0;
+    int* d_list = nullptr;      // [pair_cap]
+    double* d_ft = nullptr;     // [6][cap]
+    unsigned* d_err = nullptr;
+    double* d_mass = nullptr;
+
+    double* h_rec = nullptr;    // pinned staging
+    double* h_ft = nullptr;
+    unsigned* h_err = nullptr;
+    cudaEvent_t ev_staged = nullptr;
+    bool staged_pending = false;
+
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
+    size_t dev_bytes = 0;
+
+    int n_cur = 0;
+    int64_t step = 0;
+    int64_t launches = 0;
+    std::string last_error;
+};
+
+namespace {
+
+// Restores the caller's current device on scope exit.
+struct DeviceGuard {
+    int prev = -1;
+    explicit DeviceGuard(int dev) {
+        if (cudaGetDevice(&prev) != cudaSuccess) prev = -1;
+        if (prev != dev) cudaSetDevice(dev);
+    }
+    ~DeviceGuard() {
+        int cur = -1;
+        if (prev >= 0 && cudaGetDevice(&cur) == cudaSuccess && cur != prev) cudaSetDevice(prev);
+    }
+};
+
+lbdem_status fail(lbdem_handle* h, lbdem_status s, const std::string& msg) {
+    if (h) h->last_error = msg;
+    return s;
+}
+
+lbdem_status fail_cuda(lbdem_handle* h, const char* what, cudaError_t e) {
+    std::string m = std::string(what) + ": " + cudaGetErrorName(e) + " (" + cudaGetErrorString(e) + ")";
+    return fail(h, e == cudaErrorMemoryAllocation ? LBDEM_ERR_OUT_OF_MEMORY : LBDEM_ERR_CUDA, m);
+}
+
+#define CK(h, call)                                              \
+    do {                                                         \
+        cudaError_t e_ = (call);                                 \
+        if (e_ != cudaSuccess) return fail_cuda((h), #call, e_); \
+    } while (0)
+
+template <typename P>
+cudaError_t dalloc(lbdem_handle* h, P** p, size_t bytes) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, bytes == 0 ? 16 : bytes);
+    if (e == cudaSuccess) {
+        *p = (P*)q;
+        h->dev_bytes += bytes;
+    }
+    return e;
+}
+
+void release(lbdem_handle* h) {
+    void* dev[] = {h->f, h->vox, h->up, h->cf, h->btab, h->d_rec, h->d_sph, h->d_tag2slot, h->d_tile_off,
+                   h->d_cursor, h->d_list, h->d_ft, h->d_err, h->d_mass, h->scratch};
+    for (void* p : dev)
+        if (p) cudaFree(p);
+    void* host[] = {h->h_rec, h->h_ft, h->h_err};
+    for (void* p : host)
+        if (p) cudaFreeHost(p);
+    if (h->ev_staged) cudaEventDestroy(h->ev_staged);
+    if (h->own_stream) cudaStreamDestroy(h->own_stream);
+}
+
+int tiles_per_axis_bound(double max_radius) {
+    // cells covered per axis <= 2 r + 7 (box [x - r - 2, x + r + 2] plus truncation)
+    const int cells = (int)std::ceil(2.0 * max_radius + 7.0);
+    return (cells - 1) / TILE + 2;
+}
+
+lbdem_status ensure_scratch(lbdem_handle* h, size_t bytes) {
+    if (h->scratch_bytes >= bytes) return LBDEM_OK;
+    if (h->scratch) {
+        cudaFree(h->scratch);
+        h->dev_bytes -= h->scratch_bytes;
+        h->scratch = nullptr;
+        h->scratch_bytes = 0;
+    }
+    CK(h, dalloc(h, &h->scratch, bytes));
+    h->scratch_bytes = bytes;
+    return LBDEM_OK;
+}
+
+lbdem_status wait_staging(lbdem_handle* h) {
+    if (h->staged_pending) {
+        CK(h, cudaEventSynchronize(h->ev_staged));
+        h->staged_pending = false;
+    }
+    return LBDEM_OK;
+}
+
+// Voxelization of the particle table already in h->d_rec (n records).
+lbdem_status voxelize(lbdem_handle* h, int n, int init_vel) {
+    cudaStream_t s = h->stream;
+    CK(h, cudaMemsetAsync(h->d_tile_off, 0, sizeof(int) * ((size_t)h->ntiles + 1), s));
+    CK(h, cudaMemsetAsync(h->d_tag2slot, 0x7F, sizeof(int) * ((size_t)h->cfg.max_tag + 1), s));
+    if (n > 0) {
+        CK(h, launch_prepare_spheres(h->d_rec, n, h->d_sph, h->d_tile_off, h->d_tag2slot, h->d_err, h->g,
+                                     h->cfg.max_tag, h->cfg.max_radius, s));
+        CK(h, launch_scan_tiles(h->d_tile_off, h->ntiles, h->pair_cap, h->d_cursor, h->d_err, s));
+        CK(h, launch_fill_pairs(h->d_sph, n, h->d_tile_off, h->d_cursor, h->d_list, h->pair_cap, h->g, s));
+        const int phase = (int)(h->step & 1);
+        if (h->prec == LBDEM_PREC_FP64)
+            CK(h, launch_voxelize<double>(h->d_sph, h->d_tile_off, h->d_list, h->ntiles, h->pair_cap, h->vox,
+                                          (double*)h->up, (double*)h->f, init_vel, phase, h->g, h->d_err, s));
+        else
+            CK(h, launch_voxelize<float>(h->d_sph, h->d_tile_off, h->d_list, h->ntiles, h->pair_cap, h->vox,
+                                         (float*)h->up, (float*)h->f, init_vel, phase, h->g, h->d_err, s));
+        h->launches += 4;
+    }
+    h->n_cur = n;
+    return LBDEM_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void lbdem_config_default(lbdem_config* c) {
+    if (!c) return;
+    std::memset(c, 0, sizeof(*c));
+    c->nx = c->ny = c->nz = 32;
+    c->periodic[0] = c->periodic[1] = c->periodic[2] = 1;
+    c->omega = 1.0;
+    c->precision = LBDEM_PREC_FP64;
+    c->device = 0;
+    c->max_particles = 1024;
+    c->max_tag = 1 << 20;
+    c->max_radius = 16.0;
+    c->flags = 0;
+}
+
+const char* lbdem_status_string(lbdem_status s) {
+    switch (s) {
+        case LBDEM_OK: return "ok";
+        case LBDEM_ERR_INVALID_ARG: return "invalid argument";
+        case LBDEM_ERR_CUDA: return "CUDA error";
+        case LBDEM_ERR_OUT_OF_MEMORY: return "out of memory";
+        case LBDEM_ERR_CAPACITY: return "capacity exceeded";
+        case LBDEM_ERR_DEVICE: return "device error word set";
+        case LBDEM_ERR_NO_DEVICE: return "no suitable CUDA device";
+    }
+    return "unknown status";
+}
+
+const char* lbdem_last_error(const lbdem_handle* h) { return h ? h->last_error.c_str() : "null handle"; }
+
+lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
+    if (!cfg || !out) return LBDEM_ERR_INVALID_ARG;
+    *out = nullptr;
+    const lbdem_config& c = *cfg;
+    if (c.nx <= 0 || c.ny <= 0 || c.nz <= 0) return LBDEM_ERR_INVALID_ARG;
+    if (!(c.omega > 0.0 && c.omega < 2.0)) return LBDEM_ERR_INVALID_ARG;
+    if (c.precision != LBDEM_PREC_FP64 && c.precision != LBDEM_PREC_FP32_DEV) return LBDEM_ERR_INVALID_ARG;
+    if (c.max_particles < 0 || c.max_tag < 1 || c.max_tag > MAX_TAG_LIMIT) return LBDEM_ERR_INVALID_ARG;
+    if (!(c.max_radius > 0.0 && c.max_radius <= 1024.0)) return LBDEM_ERR_INVALID_ARG;
+    for (int d = 0; d < 3; ++d)
+        if (c.periodic[d] != 0 && c.periodic[d] != 1) return LBDEM_ERR_INVALID_ARG;
+    if (!std::isfinite(c.body_force[0]) || !std::isfinite(c.body_force[1]) || !std::isfinite(c.body_force[2]))
+        return LBDEM_ERR_INVALID_ARG;
+    const size_t N = (size_t)c.nx * c.ny * c.nz;
+    if ((size_t)c.nx * c.ny > 0x7fffffffu || c.nz > 65535 * COLLIDE_BLOCK) return LBDEM_ERR_INVALID_ARG;
+
+    int ndev = 0;
+    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0 || c.device < 0 || c.device >= ndev) {
+        cudaGetLastError();
+        return LBDEM_ERR_NO_DEVICE;
+    }
+    cudaDeviceProp prop;
+    if (cudaGetDeviceProperties(&prop, c.device) != cudaSuccess) return LBDEM_ERR_NO_DEVICE;
+    // The library carries sm_103a code only.
+    if (!(prop.major == 10 && prop.minor == 3)) return LBDEM_ERR_NO_DEVICE;
+
+    lbdem_handle* h = new (std::nothrow) lbdem_handle();
+    if (!h) return LBDEM_ERR_OUT_OF_MEMORY;
+    h->cfg = c;
+    h->device = c.device;
+    h->prec = c.precision;
+    h->esz = c.precision == LBDEM_PREC_FP64 ? 8 : 4;
+    h->g.nx = c.nx; h->g.ny = c.ny; h->g.nz = c.nz;
+    for (int d = 0; d < 3; ++d) h->g.per[d] = c.periodic[d];
+    h->g.N = N;
+    h->cap = c.max_particles;
+    const int tnx = (c.nx + TILE - 1) / TILE, tny = (c.ny + TILE - 1) / TILE, tnz = (c.nz + TILE - 1) / TILE;
+    h->ntiles = tnx * tny * tnz;
+    const long long tpa = tiles_per_axis_bound(c.max_radius);
+    long long pc = (long long)h->cap * tpa * tpa * tpa;
+    if (pc > 0x3fffffffLL) pc = 0x3fffffffLL;
+    h->pair_cap = (int)(pc > 0 ? pc : 1);
+
+    DeviceGuard dg(h->device);
+    auto bail = [&](lbdem_status s) {
+        release(h);
+        delete h;
+        return s;
+    };
+    cudaError_t e;
+#define TRY(call)                                   \
+    if ((e = (call)) != cudaSuccess) {              \
+        cudaGetLastError();                         \
+        return bail(e == cudaErrorMemoryAllocation ? LBDEM_ERR_OUT_OF_MEMORY : LBDEM_ERR_CUDA); \
+    }
+    TRY(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
+    h->stream = h->own_stream;
+    TRY(cudaEventCreateWithFlags(&h->ev_staged, cudaEventDisableTiming));
+    TRY(dalloc(h, &h->f, (size_t)Q * N * h->esz));
+    TRY(dalloc(h, &h->vox, N * sizeof(uint32_t)));
+    TRY(dalloc(h, &h->up, 3 * N * h->esz));
+    if (c.flags & LBDEM_FLAG_CELL_FORCE) TRY(dalloc(h, &h->cf, 3 * N * h->esz));
+    TRY(dalloc(h, &h->btab, 126 * sizeof(double)));
+    const size_t capn = (size_t)(h->cap > 0 ? h->cap : 1);
+    TRY(dalloc(h, &h->d_rec, capn * REC_STRIDE * sizeof(double)));
+    TRY(dalloc(h, &h->d_sph, capn * sizeof(SphereDev)));
+    TRY(dalloc(h, &h->d_tag2slot, ((size_t)c.max_tag + 1) * sizeof(int)));
+    TRY(dalloc(h, &h->d_tile_off, ((size_t)h->ntiles + 1) * sizeof(int)));
+    TRY(dalloc(h, &h->d_cursor, (size_t)h->ntiles * sizeof(int)));
+    TRY(dalloc(h, &h->d_list, (size_t)h->pair_cap * sizeof(int)));
+    TRY(dalloc(h, &h->d_ft, 6 * capn * sizeof(double)));
+    TRY(dalloc(h, &h->d_err, sizeof(unsigned)));
+    TRY(dalloc(h, &h->d_mass, sizeof(double)));
+    TRY(cudaMallocHost((void**)&h->h_rec, capn * REC_STRIDE * sizeof(double)));
+    TRY(cudaMallocHost((void**)&h->h_ft, 6 * capn * sizeof(double)));
+    TRY(cudaMallocHost((void**)&h->h_err, sizeof(unsigned)));
+
+    // B(n) = sf ooo / ((1 - sf) + ooo), sf = n/125, ooo = 1/omega - 1/2
+    // (src/ibCompositeDynamics3D.hh:178-179); n = 125 is the full-solid branch, B = 1.
+    double bt[126];
+    const double ooo = 1. / c.omega - 0.5;
+    for (int n = 0; n < 126; ++n) {
+        const double sf = (1. / 125.) * (double)n;
+        bt[n] = sf * ooo / ((1. - sf) + ooo);
+    }
+    bt[0] = 0.0;
+    bt[125] = 1.0;
+    TRY(cudaMemcpy(h->btab, bt, sizeof(bt), cudaMemcpyHostToDevice));
+    TRY(cudaMemset(h->f, 0, (size_t)Q * N * h->esz));   // f̄ = 0: rho = 1, u = 0
+    TRY(cudaMemset(h->vox, 0, N * sizeof(uint32_t)));
+    TRY(cudaMemset(h->up, 0, 3 * N * h->esz));
+    if (h->cf) TRY(cudaMemset(h->cf, 0, 3 * N * h->esz));
+    TRY(cudaMemset(h->d_tag2slot, 0x7F, ((size_t)c.max_tag + 1) * sizeof(int)));
+    TRY(cudaMemset(h->d_ft, 0, 6 * capn * sizeof(double)));
+    TRY(cudaMemset(h->d_err, 0, sizeof(unsigned)));
+    TRY(cudaDeviceSynchronize());
+#undef TRY
+    *out = h;
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_destroy(lbdem_handle* h) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    {
+        DeviceGuard dg(h->device);
+        cudaStreamSynchronize(h->stream);
+        release(h);
+    }
+    delete h;
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_set_stream(lbdem_handle* h, void* stream) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    DeviceGuard dg(h->device);
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->stream = stream ? (cudaStream_t)stream : h->own_stream;
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_synchronize(lbdem_handle* h) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    DeviceGuard dg(h->device);
+    CK(h, cudaStreamSynchronize(h->stream));
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_init_equilibrium(lbdem_handle* h, double rho_bar, const double u[3]) {
+    if (!h || !u) return fail(h, LBDEM_ERR_INVALID_ARG, "init_equilibrium: null argument");
+    if (!(rho_bar > -1.0) || !std::isfinite(rho_bar)) return fail(h, LBDEM_ERR_INVALID_ARG, "rho_bar <= -1");
+    DeviceGuard dg(h->device);
+    if (h->prec == LBDEM_PREC_FP64) CK(h, launch_fill_equilibrium<double>((double*)h->f, rho_bar, u, h->g, h->stream));
+    else CK(h, launch_fill_equilibrium<float>((float*)h->f, rho_bar, u, h->g, h->stream));
+    h->launches += 1;
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_set_populations(lbdem_handle* h, const void* host_f) {
+    if (!h || !host_f) return fail(h, LBDEM_ERR_INVALID_ARG, "set_populations: null argument");
+    DeviceGuard dg(h->device);
+    lbdem_status st = ensure_scratch(h, h->g.N * h->esz);
+    if (st != LBDEM_OK) return st;
+    const int phase = (int)(h->step & 1);
+    for (int i = 0; i < Q; ++i) {
+        const char* src = (const char*)host_f + (size_t)i * h->g.N * h->esz;
+        CK(h, cudaMemcpyAsync(h->scratch, src, h->g.N * h->esz, cudaMemcpyHostToDevice, h->stream));
+        if (h->prec == LBDEM_PREC_FP64)
+            CK(h, launch_pop_scatter<double>((double*)h->f, (const double*)h->scratch, i, phase, h->g, h->stream));
+        else
+            CK(h, launch_pop_scatter<float>((float*)h->f, (const float*)h->scratch, i, phase, h->g, h->stream));
+        h->launches += 1;
+    }
+    CK(h, cudaStreamSynchronize(h->stream));
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_get_populations(lbdem_handle* h, void* host_f) {
+    return lbdem_get_field(h, LBDEM_FIELD_POPULATIONS, host_f);
+}
+
+lbdem_status lbdem_set_particles(lbdem_handle* h, int32_t n, const double* x, const double* v, const double* w,
+                                 const double* r, const int32_t* tag, int32_t init_vel) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    if (n < 0) return fail(h, LBDEM_ERR_INVALID_ARG, "set_particles: n < 0");
+    if (n > h->cap) return fail(h, LBDEM_ERR_CAPACITY, "set_particles: n exceeds max_particles");
+    if (n > 0 && (!x || !v || !w || !r || !tag)) return fail(h, LBDEM_ERR_INVALID_ARG, "set_particles: null array");
+    DeviceGuard dg(h->device);
+    lbdem_status st = wait_staging(h);
+    if (st != LBDEM_OK) return st;
+    for (int i = 0; i < n; ++i) {
+        double* p = h->h_rec + (size_t)i * REC_STRIDE;
+        p[0] = x[3 * i]; p[1] = x[3 * i + 1]; p[2] = x[3 * i + 2];
+        p[3] = v[3 * i]; p[4] = v[3 * i + 1]; p[5] = v[3 * i + 2];
+        p[6] = w[3 * i]; p[7] = w[3 * i + 1]; p[8] = w[3 * i + 2];
+        p[9] = r[i];
+        p[10] = (double)tag[i];
+        p[11] = 0.0;
+    }
+    if (n > 0) {
+        CK(h, cudaMemcpyAsync(h->d_rec, h->h_rec, (size_t)n * REC_STRIDE * sizeof(double), cudaMemcpyHostToDevice,
+                              h->stream));
+        CK(h, cudaEventRecord(h->ev_staged, h->stream));
+        h->staged_pending = true;
+    }
+    return voxelize(h, n, init_vel);
+}
+
+lbdem_status lbdem_set_particles_device(lbdem_handle* h, int32_t n, const double* rec, int32_t init_vel) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    if (n < 0) return fail(h, LBDEM_ERR_INVALID_ARG, "set_particles_device: n < 0");
+    if (n > h->cap) return fail(h, LBDEM_ERR_CAPACITY, "set_particles_device: n exceeds max_particles");
+    if (n > 0 && !rec) return fail(h, LBDEM_ERR_INVALID_ARG, "set_particles_device: null table");
+    DeviceGuard dg(h->device);
+    if (n > 0 && rec != h->d_rec)
+        CK(h, cudaMemcpyAsync(h->d_rec, rec, (size_t)n * REC_STRIDE * sizeof(double), cudaMemcpyDeviceToDevice,
+                              h->stream));
+    return voxelize(h, n, init_vel);
+}
+
+lbdem_status lbdem_collide_and_stream(lbdem_handle* h) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    DeviceGuard dg(h->device);
+    const int n = h->n_cur;
+    if (n > 0) CK(h, cudaMemsetAsync(h->d_ft, 0, 6 * (size_t)n * sizeof(double), h->stream));
+    const bool odd = (h->step & 1) != 0;
+    const bool force = h->cfg.body_force[0] != 0.0 || h->cfg.body_force[1] != 0.0 || h->cfg.body_force[2] != 0.0;
+    if (h->prec == LBDEM_PREC_FP64) {
+        CollideArgs<double> a;
+        a.g = h->g; a.f = (double*)h->f; a.vox = h->vox; a.up = (const double*)h->up; a.cf = (double*)h->cf;
+        a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.nslot = n; a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err;
+        a.btab = h->btab; a.omega = h->cfg.omega;
+        for (int d = 0; d < 3; ++d) a.g3[d] = h->cfg.body_force[d];
+        CK(h, launch_collide_stream<double>(a, odd, force, h->stream));
+    } else {
+        CollideArgs<float> a;
+        a.g = h->g; a.f = (float*)h->f; a.vox = h->vox; a.up = (const float*)h->up; a.cf = (float*)h->cf;
+        a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.nslot = n; a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err;
+        a.btab = h->btab; a.omega = h->cfg.omega;
+        for (int d = 0; d < 3; ++d) a.g3[d] = h->cfg.body_force[d];
+        CK(h, launch_collide_stream<float>(a, odd, force, h->stream));
+    }
+    h->launches += 1;
+    h->step += 1;
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_get_forces(lbdem_handle* h, int32_t n, double* force, double* torque) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    if (n != h->n_cur) return fail(h, LBDEM_ERR_INVALID_ARG, "get_forces: n differs from the particle list");
+    if (n > 0 && (!force || !torque)) return fail(h, LBDEM_ERR_INVALID_ARG, "get_forces: null output");
+    DeviceGuard dg(h->device);
+    if (n > 0)
+        CK(h, cudaMemcpyAsync(h->h_ft, h->d_ft, 6 * (size_t)n * sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemcpyAsync(h->h_err, h->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->staged_pending = false;
+    if (n > 0) {
+        std::memcpy(force, h->h_ft, 3 * (size_t)n * sizeof(double));
+        std::memcpy(torque, h->h_ft + 3 * (size_t)n, 3 * (size_t)n * sizeof(double));
+    }
+    if (*h->h_err) {
+        char buf[96];
+        std::snprintf(buf, sizeof(buf), "device error word 0x%x", *h->h_err);
+        return fail(h, LBDEM_ERR_DEVICE, buf);
+    }
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_get_forces_device(lbdem_handle* h, int32_t n, double* dev_ft) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    if (n != h->n_cur) return fail(h, LBDEM_ERR_INVALID_ARG, "get_forces_device: n differs from the particle list");
+    if (n > 0 && !dev_ft) return fail(h, LBDEM_ERR_INVALID_ARG, "get_forces_device: null output");
+    DeviceGuard dg(h->device);
+    if (n > 0)
+        CK(h, cudaMemcpyAsync(dev_ft, h->d_ft, 6 * (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, h->stream));
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_cycle(lbdem_handle* h, int32_t n, const double* x, const double* v, const double* w,
+                         const double* r, const int32_t* tag, int32_t init_vel, double* force, double* torque) {
+    lbdem_status s = lbdem_set_particles(h, n, x, v, w, r, tag, init_vel);
+    if (s != LBDEM_OK) return s;
+    s = lbdem_collide_and_stream(h);
+    if (s != LBDEM_OK) return s;
+    return lbdem_get_forces(h, n, force, torque);
+}
+
+lbdem_status lbdem_get_field(lbdem_handle* h, int32_t which, void* host_buf) {
+    if (!h || !host_buf) return fail(h, LBDEM_ERR_INVALID_ARG, "get_field: null argument");
+    DeviceGuard dg(h->device);
+    const size_t N = h->g.N;
+    const int phase = (int)(h->step & 1);
+    cudaStream_t s = h->stream;
+    lbdem_status st;
+    switch (which) {
+        case LBDEM_FIELD_POPULATIONS:
+            if ((st = ensure_scratch(h, N * h->esz)) != LBDEM_OK) return st;
+            for (int i = 0; i < Q; ++i) {
+                if (h->prec == LBDEM_PREC_FP64)
+                    CK(h, launch_pop_gather<double>((const double*)h->f, (double*)h->scratch, i, phase, h->g, s));
+                else
+                    CK(h, launch_pop_gather<float>((const float*)h->f, (float*)h->scratch, i, phase, h->g, s));
+                h->launches += 1;
+                CK(h, cudaMemcpyAsync((char*)host_buf + (size_t)i * N * h->esz, h->scratch, N * h->esz,
+                                      cudaMemcpyDeviceToHost, s));
+            }
+            break;
+        case LBDEM_FIELD_SOLID_FRACTION:
+        case LBDEM_FIELD_PARTICLE_ID:
+        case LBDEM_FIELD_SUBCELL_COUNT: {
+            if ((st = ensure_scratch(h, N * sizeof(double))) != LBDEM_OK) return st;
+            double* sf = which == LBDEM_FIELD_SOLID_FRACTION ? (double*)h->scratch : nullptr;
+            int32_t* id = which == LBDEM_FIELD_PARTICLE_ID ? (int32_t*)h->scratch : nullptr;
+            uint8_t* ns = which == LBDEM_FIELD_SUBCELL_COUNT ? (uint8_t*)h->scratch : nullptr;
+            CK(h, launch_vox_fields(h->vox, sf, id, ns, h->g, s));
+            h->launches += 1;
+            const size_t bytes = which == LBDEM_FIELD_SOLID_FRACTION ? N * 8 : which == LBDEM_FIELD_PARTICLE_ID ? N * 4 : N;
+            CK(h, cudaMemcpyAsync(host_buf, h->scratch, bytes, cudaMemcpyDeviceToHost, s));
+            break;
+        }
+        case LBDEM_FIELD_PARTICLE_VELOCITY:
+            CK(h, cudaMemcpyAsync(host_buf, h->up, 3 * N * h->esz, cudaMemcpyDeviceToHost, s));
+            break;
+        case LBDEM_FIELD_HYDRO_FORCE:
+            if (!h->cf) return fail(h, LBDEM_ERR_INVALID_ARG, "get_field: create with LBDEM_FLAG_CELL_FORCE");
+            CK(h, cudaMemcpyAsync(host_buf, h->cf, 3 * N * h->esz, cudaMemcpyDeviceToHost, s));
+            break;
+        case LBDEM_FIELD_DENSITY:
+        case LBDEM_FIELD_VELOCITY: {
+            const bool vel = which == LBDEM_FIELD_VELOCITY;
+            if ((st = ensure_scratch(h, (vel ? 3 : 1) * N * sizeof(double))) != LBDEM_OK) return st;
+            if (h->prec == LBDEM_PREC_FP64)
+                CK(h, launch_macro<double>((const double*)h->f, phase, vel ? nullptr : (double*)h->scratch,
+                                           vel ? (double*)h->scratch : nullptr, h->g, s));
+            else
+                CK(h, launch_macro<float>((const float*)h->f, phase, vel ? nullptr : (double*)h->scratch,
+                                          vel ? (double*)h->scratch : nullptr, h->g, s));
+            h->launches += 1;
+            CK(h, cudaMemcpyAsync(host_buf, h->scratch, (vel ? 3 : 1) * N * sizeof(double), cudaMemcpyDeviceToHost, s));
+            break;
+        }
+        default:
+            return fail(h, LBDEM_ERR_INVALID_ARG, "get_field: unknown field");
+    }
+    CK(h, cudaStreamSynchronize(s));
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_mass(lbdem_handle* h, double* mass) {
+    if (!h || !mass) return fail(h, LBDEM_ERR_INVALID_ARG, "mass: null argument");
+    DeviceGuard dg(h->device);
+    CK(h, cudaMemsetAsync(h->d_mass, 0, sizeof(double), h->stream));
+    if (h->prec == LBDEM_PREC_FP64) CK(h, launch_mass<double>((const double*)h->f, h->d_mass, h->g, h->stream));
+    else CK(h, launch_mass<float>((const float*)h->f, h->d_mass, h->g, h->stream));
+    h->launches += 1;
+    double m = 0;
+    CK(h, cudaMemcpyAsync(h->h_ft, h->d_mass, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    m = h->h_ft[0];
+    *mass = m + (double)h->g.N;   // sum_i t_i = 1 per cell
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_get_device_errors(lbdem_handle* h, uint32_t* bits) {
+    if (!h || !bits) return fail(h, LBDEM_ERR_INVALID_ARG, "get_device_errors: null argument");
+    DeviceGuard dg(h->device);
+    CK(h, cudaMemcpyAsync(h->h_err, h->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaMemsetAsync(h->d_err, 0, sizeof(unsigned), h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    *bits = *h->h_err;
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_get_step(lbdem_handle* h, int64_t* step) {
+    if (!h || !step) return LBDEM_ERR_INVALID_ARG;
+    *step = h->step;
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_device_bytes(lbdem_handle* h, size_t* bytes) {
+    if (!h || !bytes) return LBDEM_ERR_INVALID_ARG;
+    *bytes = h->dev_bytes;
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_get_launch_count(lbdem_handle* h, int64_t* count) {
+    if (!h || !count) return LBDEM_ERR_INVALID_ARG;
+    *count = h->launches;
+    return LBDEM_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,103 @@
+// Internal declarations shared by the CUDA translation units of liblbdem_gb300.
+//
+// D3Q19 in Palabos ordering (c[i+9] = -c[i], i = 1..9), populations stored as
+// f̄_i = f_i - t_i, fields laid out [component][x][y][z] with z fastest.
+#pragma once
+
+#include <cstddef>
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace lbdem {
+
+constexpr int Q = 19;
+constexpr int TILE = 8;                 // voxelization tile edge (cells)
+constexpr int TILE_CELLS = TILE * TILE * TILE;
+constexpr int TILE_LIST_MAX = 2048;     // spheres overlapping one tile, held in shared memory
+constexpr int REC_STRIDE = 12;          // doubles per particle record {x3, v3, w3, r, tag, 0}
+constexpr int VOX_NBITS = 7;            // voxel word: sub-cell count n (7 bits) | tag << 7
+constexpr uint32_t VOX_NMASK = (1u << VOX_NBITS) - 1u;
+constexpr int32_t MAX_TAG_LIMIT = (1 << 25) - 1;
+constexpr int COLLIDE_BLOCK = 128;      // threads per block along z in the collide-stream kernel
+
+// Lattice velocities, Palabos D3Q19 order.
+__host__ __device__ constexpr int cx(int i) {
+    return (i == 1 || i == 4 || i == 5 || i == 6 || i == 7) ? -1
+         : (i == 10 || i == 13 || i == 14 || i == 15 || i == 16) ? 1 : 0;
+}
+__host__ __device__ constexpr int cy(int i) {
+    return (i == 2 || i == 4 || i == 8 || i == 9 || i == 14) ? -1
+         : (i == 5 || i == 11 || i == 13 || i == 17 || i == 18) ? 1 : 0;
+}
+__host__ __device__ constexpr int cz(int i) {
+    return (i == 3 || i == 6 || i == 8 || i == 16 || i == 18) ? -1
+         : (i == 7 || i == 9 || i == 12 || i == 15 || i == 17) ? 1 : 0;
+}
+__host__ __device__ constexpr int opp(int i) { return i == 0 ? 0 : (i <= 9 ? i + 9 : i - 9); }
+__host__ __device__ constexpr double wt(int i) {
+    return i == 0 ? 1.0 / 3.0 : ((i == 1 || i == 2 || i == 3 || i == 10 || i == 11 || i == 12) ? 1.0 / 18.0 : 1.0 / 36.0);
+}
+
+struct Geom {
+    int nx, ny, nz;
+    int per[3];
+    size_t N;
+};
+
+// Arguments of one collide-stream launch.
+template <typename T>
+struct CollideArgs {
+    Geom g;
+    T* f;                    // [19][N] populations, AA in-place layout
+    const uint32_t* vox;     // [N] n | tag << 7
+    const T* up;             // [3][N] particle surface velocity
+    T* cf;                   // [3][N] per-cell force (nullptr: not kept)
+    const int* tag2slot;     // [max_tag + 1] lowest particle index per tag
+    const double* rec;       // [n][12] particle records (positions for the torque arm)
+    int nslot;               // particles in the current list
+    int max_tag;             // tag2slot has max_tag + 1 entries
+    double* ft;              // [6][n]: F (3n) then T (3n)
+    unsigned* err;
+    const double* btab;      // [126] B(n) = sf ooo / ((1 - sf) + ooo), double
+    double omega;
+    double g3[3];
+};
+
+struct SphereDev {
+    double x[3], v[3], w[3], r;
+    int tag;
+    int lo[3], hi[3];
+    int valid;
+};
+
+// Launchers (return cudaGetLastError() of the launch).
+template <typename T>
+cudaError_t launch_collide_stream(const CollideArgs<T>& a, bool odd, bool force, cudaStream_t s);
+
+cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, int* tile_count,
+                                   int* tag2slot, unsigned* err, Geom g, int max_tag,
+                                   double max_radius, cudaStream_t s);
+cudaError_t launch_scan_tiles(int* tile_count, int ntiles, int pair_capacity, int* cursor,
+                              unsigned* err, cudaStream_t s);
+cudaError_t launch_fill_pairs(const SphereDev* sph, int n, const int* tile_off, int* cursor,
+                              int* list, int pair_capacity, Geom g, cudaStream_t s);
+template <typename T>
+cudaError_t launch_voxelize(const SphereDev* sph, const int* tile_off, const int* list,
+                            int ntiles, int pair_capacity, uint32_t* vox, T* up, T* f,
+                            int init_vel, int odd_phase, Geom g, unsigned* err, cudaStream_t s);
+
+// Field helpers.  phase: number of completed steps mod 2 (storage layout).
+template <typename T>
+cudaError_t launch_pop_gather(const T* f, T* out, int i, int phase, Geom g, cudaStream_t s);
+template <typename T>
+cudaError_t launch_pop_scatter(T* f, const T* in, int i, int phase, Geom g, cudaStream_t s);
+template <typename T>
+cudaError_t launch_fill_equilibrium(T* f, double rho_bar, const double* u, Geom g, cudaStream_t s);
+template <typename T>
+cudaError_t launch_macro(const T* f, int phase, double* rho, double* u, Geom g, cudaStream_t s);
+template <typename T>
+cudaError_t launch_mass(const T* f, double* out, Geom g, cudaStream_t s);
+cudaError_t launch_vox_fields(const uint32_t* vox, double* sf, int32_t* id, uint8_t* nsub, Geom g,
+                              cudaStream_t s);
+
+}  // namespace lbdem

@@ -1,0 +1,295 @@
+"""ctypes binding of liblbdem_gb300 (the C ABI in include/lbdem_gpu.h).
+
+This is a thin host-side mirror of the reference's coupling surface for Python
+callers and tests:
+
+    reference (LBDEMcoupling, Palabos side)        here
+    setSpheresOnLattice(lattice, wrapper, ...)     Lattice.set_particles(...)
+    lattice.collideAndStream()                     Lattice.collide_and_stream()
+    getForcesFromLattice(lattice, wrapper, ...)    Lattice.get_forces(n)
+
+There is no CPU fallback: constructing a Lattice without the built library or
+without a GB300 raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+import numpy as np
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_build" / "liblbdem_gb300.so"
+
+PREC_FP64 = 0
+PREC_FP32_DEV = 1
+FLAG_CELL_FORCE = 0x1
+
+FIELD_POPULATIONS = 0
+FIELD_SOLID_FRACTION = 1
+FIELD_PARTICLE_ID = 2
+FIELD_PARTICLE_VELOCITY = 3
+FIELD_HYDRO_FORCE = 4
+FIELD_DENSITY = 5
+FIELD_VELOCITY = 6
+FIELD_SUBCELL_COUNT = 7
+
+DEVERR_TILE_LIST = 0x1
+DEVERR_PAIR_CAPACITY = 0x2
+DEVERR_TAG_RANGE = 0x4
+DEVERR_UNMAPPED_TAG = 0x8
+DEVERR_RADIUS = 0x10
+
+STATUS = {0: "LBDEM_OK", 1: "LBDEM_ERR_INVALID_ARG", 2: "LBDEM_ERR_CUDA", 3: "LBDEM_ERR_OUT_OF_MEMORY",
+          4: "LBDEM_ERR_CAPACITY", 5: "LBDEM_ERR_DEVICE", 6: "LBDEM_ERR_NO_DEVICE"}
+
+# Every function the C ABI exports, with (restype, argtypes).
+_P = C.c_void_p
+_D = C.POINTER(C.c_double)
+_I = C.c_int32
+
+
+class Config(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("periodic", C.c_int32 * 3), ("omega", C.c_double), ("body_force", C.c_double * 3),
+                ("precision", C.c_int32), ("device", C.c_int32), ("max_particles", C.c_int32),
+                ("max_tag", C.c_int32), ("max_radius", C.c_double), ("flags", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+SIGNATURES = {
+    "lbdem_config_default": (None, [C.POINTER(Config)]),
+    "lbdem_create": (C.c_int, [C.POINTER(Config), C.POINTER(_P)]),
+    "lbdem_destroy": (C.c_int, [_P]),
+    "lbdem_last_error": (C.c_char_p, [_P]),
+    "lbdem_status_string": (C.c_char_p, [C.c_int]),
+    "lbdem_set_stream": (C.c_int, [_P, _P]),
+    "lbdem_synchronize": (C.c_int, [_P]),
+    "lbdem_init_equilibrium": (C.c_int, [_P, C.c_double, _D]),
+    "lbdem_set_populations": (C.c_int, [_P, _P]),
+    "lbdem_get_populations": (C.c_int, [_P, _P]),
+    "lbdem_set_particles": (C.c_int, [_P, _I, _D, _D, _D, _D, C.POINTER(_I), _I]),
+    "lbdem_set_particles_device": (C.c_int, [_P, _I, _P, _I]),
+    "lbdem_collide_and_stream": (C.c_int, [_P]),
+    "lbdem_get_forces": (C.c_int, [_P, _I, _D, _D]),
+    "lbdem_get_forces_device": (C.c_int, [_P, _I, _P]),
+    "lbdem_cycle": (C.c_int, [_P, _I, _D, _D, _D, _D, C.POINTER(_I), _I, _D, _D]),
+    "lbdem_get_field": (C.c_int, [_P, _I, _P]),
+    "lbdem_mass": (C.c_int, [_P, _D]),
+    "lbdem_get_device_errors": (C.c_int, [_P, C.POINTER(C.c_uint32)]),
+    "lbdem_get_step": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "lbdem_device_bytes": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
+    "lbdem_get_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+}
+
+_lib = None
+
+
+def load(path: os.PathLike | None = None) -> C.CDLL:
+    """Loads the shared library (raises if it was not built)."""
+    global _lib
+    if _lib is not None and path is None:
+        return _lib
+    p = Path(path) if path else LIB_PATH
+    if not p.exists():
+        raise RuntimeError(f"liblbdem_gb300 not built: {p} missing (run build())")
+    lib = C.CDLL(str(p))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    if path is None:
+        _lib = lib
+    return lib
+
+
+class LbdemError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{STATUS.get(status, status)}: {msg}")
+        self.status = status
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(_D)
+
+
+def _c64(a, shape=None) -> np.ndarray:
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    if shape is not None:
+        a = a.reshape(shape)
+    return a
+
+
+class Lattice:
+    """A D3Q19 PSM lattice resident on the GPU (one handle of the C ABI)."""
+
+    def __init__(self, nx, ny, nz, omega, periodic=(1, 1, 1), precision=PREC_FP64, body_force=(0, 0, 0),
+                 max_particles=1024, max_tag=1 << 20, max_radius=16.0, flags=0, device=0):
+        self.lib = load()
+        cfg = Config()
+        self.lib.lbdem_config_default(C.byref(cfg))
+        cfg.nx, cfg.ny, cfg.nz = int(nx), int(ny), int(nz)
+        for d in range(3):
+            cfg.periodic[d] = int(periodic[d])
+            cfg.body_force[d] = float(body_force[d])
+        cfg.omega = float(omega)
+        cfg.precision = int(precision)
+        cfg.device = int(device)
+        cfg.max_particles = int(max_particles)
+        cfg.max_tag = int(max_tag)
+        cfg.max_radius = float(max_radius)
+        cfg.flags = int(flags)
+        self.cfg = cfg
+        self.shape = (int(nx), int(ny), int(nz))
+        self.N = int(nx) * int(ny) * int(nz)
+        self.dtype = np.float64 if precision == PREC_FP64 else np.float32
+        h = _P()
+        st = self.lib.lbdem_create(C.byref(cfg), C.byref(h))
+        if st != 0:
+            raise LbdemError(st, self.lib.lbdem_status_string(st).decode())
+        self.h = h
+        self.n = 0
+
+    # -- life cycle -------------------------------------------------------
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.lbdem_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st: int):
+        if st != 0:
+            raise LbdemError(st, self.lib.lbdem_last_error(self.h).decode())
+
+    # -- state ------------------------------------------------------------
+    def init_equilibrium(self, rho_bar=0.0, u=(0.0, 0.0, 0.0)):
+        uu = _c64(u)
+        self._check(self.lib.lbdem_init_equilibrium(self.h, float(rho_bar), _dptr(uu)))
+
+    def set_populations(self, f: np.ndarray):
+        f = np.ascontiguousarray(f, dtype=self.dtype).reshape(19, *self.shape)
+        self._check(self.lib.lbdem_set_populations(self.h, f.ctypes.data_as(_P)))
+
+    def get_populations(self) -> np.ndarray:
+        out = np.empty((19, *self.shape), dtype=self.dtype)
+        self._check(self.lib.lbdem_get_populations(self.h, out.ctypes.data_as(_P)))
+        return out
+
+    def get_field(self, which: int) -> np.ndarray:
+        shapes = {
+            FIELD_POPULATIONS: ((19, *self.shape), self.dtype),
+            FIELD_SOLID_FRACTION: (self.shape, np.float64),
+            FIELD_PARTICLE_ID: (self.shape, np.int32),
+            FIELD_PARTICLE_VELOCITY: ((3, *self.shape), self.dtype),
+            FIELD_HYDRO_FORCE: ((3, *self.shape), self.dtype),
+            FIELD_DENSITY: (self.shape, np.float64),
+            FIELD_VELOCITY: ((3, *self.shape), np.float64),
+            FIELD_SUBCELL_COUNT: (self.shape, np.uint8),
+        }
+        shp, dt = shapes[which]
+        out = np.empty(shp, dtype=dt)
+        self._check(self.lib.lbdem_get_field(self.h, int(which), out.ctypes.data_as(_P)))
+        return out
+
+    # -- coupling cycle ---------------------------------------------------
+    def set_particles(self, x, v, w, r, tag, init_vel=False):
+        x = _c64(x).reshape(-1, 3)
+        n = x.shape[0]
+        v = _c64(v).reshape(n, 3)
+        w = _c64(w).reshape(n, 3)
+        r = _c64(r).reshape(n)
+        tag = np.ascontiguousarray(tag, dtype=np.int32).reshape(n)
+        self._keep = (x, v, w, r, tag)
+        self._check(self.lib.lbdem_set_particles(self.h, n, _dptr(x), _dptr(v), _dptr(w), _dptr(r),
+                                                 tag.ctypes.data_as(C.POINTER(_I)), int(bool(init_vel))))
+        self.n = n
+
+    def set_particles_device(self, n: int, rec_ptr: int, init_vel=False):
+        self._check(self.lib.lbdem_set_particles_device(self.h, int(n), _P(rec_ptr), int(bool(init_vel))))
+        self.n = n
+
+    def collide_and_stream(self):
+        self._check(self.lib.lbdem_collide_and_stream(self.h))
+
+    def get_forces(self):
+        F = np.zeros((self.n, 3))
+        T = np.zeros((self.n, 3))
+        self._check(self.lib.lbdem_get_forces(self.h, self.n, _dptr(F), _dptr(T)))
+        return F, T
+
+    def get_forces_device(self, dev_ptr: int):
+        self._check(self.lib.lbdem_get_forces_device(self.h, self.n, _P(dev_ptr)))
+
+    def cycle(self, x, v, w, r, tag, init_vel=False, F=None, T=None):
+        x = _c64(x).reshape(-1, 3)
+        n = x.shape[0]
+        v = _c64(v).reshape(n, 3)
+        w = _c64(w).reshape(n, 3)
+        r = _c64(r).reshape(n)
+        tag = np.ascontiguousarray(tag, dtype=np.int32).reshape(n)
+        if F is None:
+            F = np.zeros((n, 3))
+        if T is None:
+            T = np.zeros((n, 3))
+        self._check(self.lib.lbdem_cycle(self.h, n, _dptr(x), _dptr(v), _dptr(w), _dptr(r),
+                                         tag.ctypes.data_as(C.POINTER(_I)), int(bool(init_vel)),
+                                         _dptr(F), _dptr(T)))
+        self.n = n
+        return F, T
+
+    # -- diagnostics ------------------------------------------------------
+    def mass(self) -> float:
+        m = C.c_double()
+        self._check(self.lib.lbdem_mass(self.h, C.byref(m)))
+        return m.value
+
+    def device_errors(self) -> int:
+        b = C.c_uint32()
+        self._check(self.lib.lbdem_get_device_errors(self.h, C.byref(b)))
+        return int(b.value)
+
+    def step_count(self) -> int:
+        s = C.c_int64()
+        self._check(self.lib.lbdem_get_step(self.h, C.byref(s)))
+        return int(s.value)
+
+    def launch_count(self) -> int:
+        s = C.c_int64()
+        self._check(self.lib.lbdem_get_launch_count(self.h, C.byref(s)))
+        return int(s.value)
+
+    def device_bytes(self) -> int:
+        s = C.c_size_t()
+        self._check(self.lib.lbdem_device_bytes(self.h, C.byref(s)))
+        return int(s.value)
+
+    def synchronize(self):
+        self._check(self.lib.lbdem_synchronize(self.h))
+
+    def set_stream(self, stream_ptr: int | None):
+        self._check(self.lib.lbdem_set_stream(self.h, _P(stream_ptr) if stream_ptr else None))
+
+
+def pack_records(x, v, w, r, tag) -> np.ndarray:
+    """Particle table in the device layout: [n][12] doubles {x3, v3, w3, r, tag, 0}."""
+    x = np.asarray(x, dtype=np.float64).reshape(-1, 3)
+    n = x.shape[0]
+    rec = np.zeros((n, 12))
+    rec[:, 0:3] = x
+    rec[:, 3:6] = np.asarray(v, dtype=np.float64).reshape(n, 3)
+    rec[:, 6:9] = np.asarray(w, dtype=np.float64).reshape(n, 3)
+    rec[:, 9] = np.asarray(r, dtype=np.float64).reshape(n)
+    rec[:, 10] = np.asarray(tag).reshape(n)
+    return rec

@@ -1,0 +1,90 @@
+"""The C ABI library builds, loads and exports every symbol include/lbdem_gpu.h
+declares; argument checks run before any device work, so they are testable
+without a GPU."""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parent.parent
+HEADER = ROOT / "include" / "lbdem_gpu.h"
+
+
+def declared_functions():
+    text = HEADER.read_text()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(lbdem_[a-z_]+)\s*\(", text)))
+
+
+def test_header_declares_the_abi():
+    names = declared_functions()
+    for must in ("lbdem_create", "lbdem_destroy", "lbdem_set_particles", "lbdem_collide_and_stream",
+                 "lbdem_get_forces", "lbdem_get_field", "lbdem_cycle", "lbdem_mass"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(lbdem_lib):
+    lib = lbdem_lib.load()
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(declared_functions()) == set(lbdem_lib.SIGNATURES), "ctypes signatures out of date"
+
+
+def test_config_struct_matches_header(lbdem_lib):
+    lib = lbdem_lib.load()
+    cfg = lbdem_lib.Config()
+    lib.lbdem_config_default(C.byref(cfg))
+    assert (cfg.nx, cfg.ny, cfg.nz) == (32, 32, 32)
+    assert list(cfg.periodic) == [1, 1, 1]
+    assert cfg.omega == 1.0 and cfg.max_particles == 1024 and cfg.max_tag == 1 << 20
+    assert cfg.max_radius == 16.0
+
+
+def test_config_layout_matches_c_compiler(lbdem_lib, tmp_path):
+    """ctypes field offsets equal the C compiler's offsetof for lbdem_config."""
+    import shutil
+    import subprocess
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    fields = [f[0] for f in lbdem_lib.Config._fields_]
+    src = tmp_path / "probe.c"
+    body = "".join(f'printf("%zu\\n", offsetof(lbdem_config, {f}));' for f in fields)
+    src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "lbdem_gpu.h"\n'
+                   f'int main(void){{{body} printf("%zu\\n", sizeof(lbdem_config)); return 0;}}\n')
+    exe = tmp_path / "probe"
+    subprocess.run([cc, "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    want = [getattr(lbdem_lib.Config, f).offset for f in fields] + [C.sizeof(lbdem_lib.Config)]
+    assert got == want
+
+
+@pytest.mark.parametrize("field,value", [("nx", 0), ("omega", 2.0), ("omega", 0.0), ("precision", 7),
+                                         ("max_tag", 1 << 25), ("max_radius", -1.0), ("max_particles", -1)])
+def test_create_rejects_bad_config(lbdem_lib, field, value):
+    lib = lbdem_lib.load()
+    cfg = lbdem_lib.Config()
+    lib.lbdem_config_default(C.byref(cfg))
+    setattr(cfg, field, value)
+    h = C.c_void_p()
+    assert lib.lbdem_create(C.byref(cfg), C.byref(h)) == 1
+    assert not h.value
+
+
+def test_null_handle_calls_fail_cleanly(lbdem_lib):
+    lib = lbdem_lib.load()
+    assert lib.lbdem_collide_and_stream(None) == 1
+    assert lib.lbdem_destroy(None) == 1
+    assert lib.lbdem_synchronize(None) == 1
+    assert lib.lbdem_status_string(5) == b"device error word set"
+    assert lib.lbdem_last_error(None) == b"null handle"
+
+
+def test_no_device_is_an_error_not_a_fallback(lbdem_lib):
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    with pytest.raises(lbdem_lib.LbdemError) as ei:
+        lbdem_lib.Lattice(8, 8, 8, 1.0)
+    assert ei.value.status == 6

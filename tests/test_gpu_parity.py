@@ -1,0 +1,180 @@
+"""GPU parity against the CPU oracle, through the C ABI.
+
+Bars (stated per assertion below):
+* voxelization: sub-cell count n, owner tag and particle surface velocity are
+  bit-identical to the oracle (IEEE double with no fused multiply-add);
+* FP64 populations: max |Δf̄| <= 1e-12 max |f̄|;
+* FP64 forces/torques: |ΔF_p| <= 1e-12 Σ_{cells of p} |f_cell| (summation order differs);
+* FP32 deviation form against the FP32 oracle: populations within 2e-5 of
+  max |f̄|; per-particle forces against the FP64 oracle within 1e-4 of max |F|.
+"""
+import numpy as np
+import pytest
+
+import workloads as W
+from helpers import rel_err, small_suspension
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    # shape, periodic, omega, n, rmin, rmax, overlap, body_force
+    "periodic_overlap": ((24, 20, 28), (1, 1, 1), 1 / 0.6, 7, 3.0, 5.5, True, (0.0, 0.0, 0.0)),
+    "channel_force": ((20, 24, 18), (1, 0, 1), 1 / 0.55, 4, 2.5, 4.5, False, (1e-5, 0.0, 2e-6)),
+    "closed_box": ((16, 18, 40), (0, 0, 0), 1 / 0.6, 2, 4.0, 5.0, False, (0.0, 0.0, 0.0)),
+    "tiny_radius": ((13, 11, 9), (1, 1, 1), 1.7, 5, 0.6, 1.6, True, (0.0, 0.0, 0.0)),
+}
+
+
+def _per_particle_scale(ostate, tag, n):
+    """Σ_{cells owned by tag} |f_cell| per list entry (zero for ghost entries)."""
+    ids = ostate["id"].ravel()
+    cf = np.abs(ostate["cf"].astype(np.float64)).reshape(3, -1).sum(axis=0)
+    sums = np.bincount(ids, weights=cf, minlength=int(tag.max()) + 1)
+    first = {}
+    for i, t in enumerate(tag):
+        first.setdefault(int(t), i)
+    s = np.zeros(n)
+    for t, i in first.items():
+        s[i] = sums[t]
+    return s
+
+
+def _run(lbdem, oracle, case, precision, steps, init_steps=(0, 3), seed=7):
+    shape, periodic, omega, n, rmin, rmax, overlap, bf = CASES[case]
+    rng = np.random.default_rng(seed)
+    dt = np.float64 if precision == lbdem.PREC_FP64 else np.float32
+    f0 = (rng.standard_normal((19, *shape)) * 1e-3).astype(dt)
+    gl = lbdem.Lattice(*shape, omega, periodic=periodic, precision=precision, body_force=bf,
+                       max_particles=256, max_tag=64, max_radius=8.0, flags=lbdem.FLAG_CELL_FORCE)
+    ol = oracle.OracleLattice(*shape, omega, periodic=periodic, precision=0 if dt == np.float64 else 1,
+                              body_force=bf)
+    gl.set_populations(f0)
+    ol.set_populations(f0)
+    assert np.array_equal(gl.get_populations(), f0)
+    p = small_suspension(shape, n, rmin, rmax, seed, periodic=periodic, overlap=overlap, v_std=0.3,
+                         w_std=0.05)
+    out = []
+    for s in range(steps):
+        g = W.with_ghosts(p, shape, periodic)
+        iv = s in init_steps
+        gl.set_particles(g.x, g.v, g.w, g.r, g.tag, init_vel=iv)
+        ol.set_particles(g.x, g.v, g.w, g.r, g.tag, init_vel=iv)
+        ost = ol.state()
+        assert np.array_equal(gl.get_field(lbdem.FIELD_SUBCELL_COUNT), ost["n"]), f"step {s}: counts differ"
+        assert np.array_equal(gl.get_field(lbdem.FIELD_PARTICLE_ID), ost["id"]), f"step {s}: owner tags differ"
+        assert np.array_equal(gl.get_field(lbdem.FIELD_SOLID_FRACTION), ost["sf"]), f"step {s}: sf differs"
+        assert np.array_equal(gl.get_field(lbdem.FIELD_PARTICLE_VELOCITY), ost["up"]), f"step {s}: uPart differs"
+        if iv:
+            assert np.array_equal(gl.get_populations(), ol.get_populations()) or \
+                rel_err(gl.get_populations(), ol.get_populations()) <= (1e-14 if dt == np.float64 else 1e-6)
+        gl.collide_and_stream()
+        ol.collide_and_stream()
+        Fg, Tg = gl.get_forces()
+        Fo, To = ol.get_forces()
+        ost = ol.state()
+        out.append((gl.get_populations(), ol.get_populations(), Fg, Fo, Tg, To, ost, g,
+                    gl.get_field(lbdem.FIELD_HYDRO_FORCE)))
+        p = W.advance(p, shape, periodic)
+    assert gl.device_errors() == 0
+    return out
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_fp64_parity(gpu, oracle, case):
+    res = _run(gpu, oracle, case, gpu.PREC_FP64, steps=6)
+    for s, (fg, fo, Fg, Fo, Tg, To, ost, g, cfg) in enumerate(res):
+        assert rel_err(fg, fo) <= 1e-12, f"step {s}: populations {rel_err(fg, fo):.3e}"
+        assert rel_err(cfg, ost["cf"]) <= 1e-12, f"step {s}: cell force field"
+        scale = _per_particle_scale(ost, g.tag, g.n)
+        span = max(fg.shape[1:])
+        assert np.all(np.abs(Fg - Fo) <= 1e-12 * scale[:, None] + 1e-300), f"step {s}: forces"
+        assert np.all(np.abs(Tg - To) <= 1e-12 * span * scale[:, None] + 1e-300), f"step {s}: torques"
+        ghost = np.ones(g.n, bool)
+        _, first = np.unique(g.tag, return_index=True)
+        ghost[first] = False
+        assert np.all(Fg[ghost] == 0) and np.all(Tg[ghost] == 0)
+    assert any(np.abs(r[2]).max() > 0 for r in res), "no force was exercised"
+
+
+@pytest.mark.parametrize("case", ["periodic_overlap", "channel_force"])
+def test_fp32_dev_parity(gpu, oracle, case):
+    res = _run(gpu, oracle, case, gpu.PREC_FP32_DEV, steps=6)
+    for s, (fg, fo, Fg, Fo, Tg, To, ost, g, cfg) in enumerate(res):
+        assert rel_err(fg, fo) <= 2e-5, f"step {s}: populations {rel_err(fg, fo):.3e}"
+    # FP32 form against the FP64 oracle on the same inputs: per-particle force
+    res64 = _run(gpu, oracle, case, gpu.PREC_FP64, steps=6)
+    for s in range(len(res)):
+        F32, F64 = res[s][2], res64[s][3]
+        assert rel_err(F32, F64) <= 1e-4, f"step {s}: FP32 force error {rel_err(F32, F64):.3e}"
+
+
+def test_mass_and_fields(gpu, oracle):
+    shape = (20, 16, 24)
+    rng = np.random.default_rng(3)
+    f0 = rng.standard_normal((19, *shape)) * 1e-3
+    gl = gpu.Lattice(*shape, 1.3, periodic=(1, 1, 1))
+    gl.set_populations(f0)
+    m0 = gl.mass()
+    assert abs(m0 - (f0.sum() + np.prod(shape))) <= 1e-9
+    for _ in range(5):
+        gl.collide_and_stream()
+    assert abs(gl.mass() - m0) <= 1e-10 * m0
+    f = gl.get_populations()
+    c = np.array([[0, 0, 0], [-1, 0, 0], [0, -1, 0], [0, 0, -1], [-1, -1, 0], [-1, 1, 0], [-1, 0, -1],
+                  [-1, 0, 1], [0, -1, -1], [0, -1, 1], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 0],
+                  [1, -1, 0], [1, 0, 1], [1, 0, -1], [0, 1, 1], [0, 1, -1]], dtype=np.float64)
+    rho = 1 + f.sum(axis=0)
+    j = np.einsum("qd,qxyz->dxyz", c, f)
+    assert rel_err(gl.get_field(gpu.FIELD_DENSITY), rho) <= 1e-14
+    assert rel_err(gl.get_field(gpu.FIELD_VELOCITY), j / rho) <= 1e-12
+
+
+def test_equilibrium_fixed_point(gpu):
+    gl = gpu.Lattice(12, 12, 12, 1.1)
+    gl.init_equilibrium(0.01, (0.02, -0.01, 0.005))
+    f0 = gl.get_populations()
+    for _ in range(3):
+        gl.collide_and_stream()
+    assert rel_err(gl.get_populations(), f0) <= 1e-13
+
+
+def test_unmapped_tag_is_reported(gpu, oracle):
+    """Cells keep a particle's state when it leaves the list (the reference
+    does too); the force sum then names a tag with no particle."""
+    shape = (16, 16, 16)
+    gl = gpu.Lattice(*shape, 1.2, max_particles=8, max_tag=8)
+    ol = oracle.OracleLattice(*shape, 1.2)
+    x = np.array([[8.0, 8.0, 8.0]]); v = np.zeros((1, 3)); w = np.zeros((1, 3)); r = np.array([3.0])
+    t = np.array([1], dtype=np.int32)
+    gl.set_particles(x, v, w, r, t)
+    ol.set_particles(x, v, w, r, t)
+    gl.collide_and_stream(); gl.get_forces()
+    e = np.zeros((0, 3))
+    gl.set_particles(e, e, e, np.zeros(0), np.zeros(0, np.int32))
+    ol.set_particles(e, e, e, np.zeros(0), np.zeros(0, np.int32))
+    gl.collide_and_stream()
+    ol.collide_and_stream()
+    ol.get_forces(e, np.zeros(0, np.int32))
+    with pytest.raises(gpu.LbdemError) as ei:
+        gl.get_forces()
+    assert ei.value.status == 5
+    assert gl.device_errors() & gpu.DEVERR_UNMAPPED_TAG
+    assert np.array_equal(gl.get_field(gpu.FIELD_PARTICLE_ID), ol.state()["id"])
+
+
+def test_bad_particles_rejected(gpu):
+    gl = gpu.Lattice(16, 16, 16, 1.2, max_particles=4, max_tag=10, max_radius=5.0)
+    x = np.full((1, 3), 8.0); z = np.zeros((1, 3))
+    with pytest.raises(gpu.LbdemError):
+        gl.set_particles(np.zeros((5, 3)), np.zeros((5, 3)), np.zeros((5, 3)), np.ones(5), np.arange(1, 6))
+    gl.set_particles(x, z, z, np.array([6.0]), np.array([1]))  # radius above max_radius
+    gl.collide_and_stream()
+    with pytest.raises(gpu.LbdemError):
+        gl.get_forces()
+    assert gl.device_errors() & gpu.DEVERR_RADIUS
+    gl.set_particles(x, z, z, np.array([3.0]), np.array([11]))  # tag above max_tag
+    gl.collide_and_stream()
+    with pytest.raises(gpu.LbdemError):
+        gl.get_forces()
+    assert gl.device_errors() & gpu.DEVERR_TAG_RANGE
+    assert gl.device_errors() == 0
