@@ -241,6 +241,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--cpu-budget", type=float, default=20.0, help="seconds of CPU-oracle work")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--forms", default="fp32,fp64", help="population forms to time (fp32 is the headline)")
+    ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI leg (profiling runs)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -299,17 +301,24 @@ def main():
 
     if dist:
         dist.barrier()
+    forms = [f.strip() for f in args.forms.split(",") if f.strip()]
+    if "fp32" not in forms:
+        ap.error("--forms must include fp32 (the headline form)")
     r32 = run_device("fp32", table, offs, args.steps, args.warmup, max_n, max_tag, device)
-    r64 = run_device("fp64", table, offs, args.steps, args.warmup, max_n, max_tag, device)
-    e2e_s, h2d, d2h = run_e2e(host, args.steps, args.warmup, max_n, max_tag, device)
+    r64 = run_device("fp64", table, offs, args.steps, args.warmup, max_n, max_tag, device) if "fp64" in forms else None
+    if args.no_e2e:
+        e2e_s, h2d, d2h = float("nan"), 0, 0
+    else:
+        e2e_s, h2d, d2h = run_e2e(host, args.steps, args.warmup, max_n, max_tag, device)
 
     t32 = r32["total_ms"]
     if dist:
-        t = torch.tensor([t32, r64["total_ms"], e2e_s], dtype=torch.float64, device=f"cuda:{device}")
+        t = torch.tensor([t32, r64["total_ms"] if r64 else 0.0, e2e_s], dtype=torch.float64,
+                         device=f"cuda:{device}")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         t32, t64, e2e_s = (float(v) for v in t.tolist())
     else:
-        t64 = r64["total_ms"]
+        t64 = r64["total_ms"] if r64 else float("nan")
     if rank != 0:
         dist.destroy_process_group()
         return
@@ -319,9 +328,11 @@ def main():
     value = world * N * args.steps / (t32 * 1e-3) / 1e6
     v64 = world * N * args.steps / (t64 * 1e-3) / 1e6
     ach32 = BYTES_PER_CELL["fp32"] * N / (r32["k1_ms"] * 1e-3) / 1e9
-    ach64 = BYTES_PER_CELL["fp64"] * N / (r64["k1_ms"] * 1e-3) / 1e9
-    F32, F64 = r32["F"], r64["F"]
-    ferr = float(np.max(np.abs(F32 - F64)) / np.max(np.abs(F64)))
+    ach64 = BYTES_PER_CELL["fp64"] * N / (r64["k1_ms"] * 1e-3) / 1e9 if r64 else None
+    ferr = None
+    if r64:
+        F32, F64 = r32["F"], r64["F"]
+        ferr = float(np.max(np.abs(F32 - F64)) / np.max(np.abs(F64)))
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -341,18 +352,19 @@ def main():
                      "traffic": traffic.get("fp32"), "kernel": "k_collide_stream<float>",
                      "bytes_per_cell": BYTES_PER_CELL["fp32"], "peak_source": peak_kind,
                      "k1_ms": r32["k1_ms"], "k2_voxelize_ms": r32["k2_ms"]},
-        "fp64": {"value": v64, "unit": "MLUPS", "ms_per_step": t64 / args.steps,
-                 "roofline": {"bound": "hbm", "achieved": ach64, "peak": peak, "unit": "GB/s",
-                              "frac": ach64 / peak, "traffic": traffic.get("fp64"),
-                              "kernel": "k_collide_stream<double>", "bytes_per_cell": BYTES_PER_CELL["fp64"],
-                              "k1_ms": r64["k1_ms"], "k2_voxelize_ms": r64["k2_ms"]}},
+        "fp64": None if r64 is None else {
+            "value": v64, "unit": "MLUPS", "ms_per_step": t64 / args.steps,
+            "roofline": {"bound": "hbm", "achieved": ach64, "peak": peak, "unit": "GB/s", "frac": ach64 / peak,
+                         "traffic": traffic.get("fp64"), "kernel": "k_collide_stream<double>",
+                         "bytes_per_cell": BYTES_PER_CELL["fp64"], "k1_ms": r64["k1_ms"],
+                         "k2_voxelize_ms": r64["k2_ms"]}},
         "force_rel_err_fp32_vs_fp64": ferr,
-        "e2e": {"value": world * N * args.steps / e2e_s / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": h2d,
-                "d2h_bytes_per_step": d2h},
+        "e2e": None if args.no_e2e else {"value": world * N * args.steps / e2e_s / 1e6, "unit": "MLUPS",
+                                         "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "cpu_baseline": cpu,
         "clocks": r32["clocks"],
         "gpu_launches": r32["launches"],
-        "device_errors": r32["device_errors"] | r64["device_errors"],
+        "device_errors": r32["device_errors"] | (r64["device_errors"] if r64 else 0),
     }
     print(json.dumps(out))
     if dist:

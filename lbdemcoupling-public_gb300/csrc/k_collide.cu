@@ -25,6 +25,10 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 
+// 1/x rounded to nearest (identical to the IEEE division 1/x).
+__device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
+__device__ __forceinline__ double recip(double x) { return 1.0 / x; }
+
 // c_i . (a, b, c) with the zero terms removed at compile time (0 * x is not
 // foldable under IEEE rules, so the sum is built from the non-zero components).
 template <typename T>
@@ -66,7 +70,7 @@ __device__ __forceinline__ void bgk(T (&f)[Q], T omega, T gx, T gy, T gz) {
     T rhoBar, jx, jy, jz;
     moments(f, rhoBar, jx, jy, jz);
     const T rho = T(1) + rhoBar;
-    const T invRho = T(1) / rho;
+    const T invRho = recip(rho);
     if (FORCE) {
         const T h = T(0.5) * rho;
         jx += h * gx; jy += h * gy; jz += h * gz;
@@ -115,7 +119,7 @@ __device__ __forceinline__ void psm(T (&f)[Q], int n, T up0, T up1, T up2, T B, 
     T rhoBar, jx, jy, jz;
     moments(f, rhoBar, jx, jy, jz);                  // post-collision moments, :146-148
     const T rho = T(1) + rhoBar;
-    const T invRho = T(1) / rho;
+    const T invRho = recip(rho);
     const T ux = up0 * rho, uy = up1 * rho, uz = up2 * rho;   // uPart (1 + rhoBar), :154
     const T q45 = T(4.5) * invRho;
     const T baseE = rhoBar - T(1.5) * invRho * (jx * jx + jy * jy + jz * jz);
@@ -161,8 +165,10 @@ k_collide_stream(const CollideArgs<T> a) {
     const size_t c = ((size_t)x * ny + y) * nz + (valid ? z : 0);
     T* __restrict__ F = a.f;
 
+    // Per-cell force and torque, summed over a warp in the population type
+    // (double for the FP64 form) and accumulated per particle in double.
     int key = -1;
-    double v[6] = {0, 0, 0, 0, 0, 0};
+    T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
 
     if (valid) {
         // neighbour coordinates along each axis (-1: beyond a wall)
@@ -229,19 +235,28 @@ k_collide_stream(const CollideArgs<T> a) {
             } else {
                 key = slot;
                 // torque arm with the minimum image of src/ibProcessors3D.hh:230-243
-                const double* p = a.rec + (size_t)slot * REC_STRIDE;
-                double dx = (double)x - __ldg(p + 0);
-                double dy = (double)y - __ldg(p + 1);
-                double dz = (double)z - __ldg(p + 2);
+                T dx, dy, dz;
+                if (sizeof(T) == 8) {
+                    const double* p = a.rec + (size_t)slot * REC_STRIDE;
+                    dx = T((double)x - __ldg(p + 0));
+                    dy = T((double)y - __ldg(p + 1));
+                    dz = T((double)z - __ldg(p + 2));
+                } else {
+                    // centre = hi + lo in float: (x - hi) - lo is the arm to ~1 ulp
+                    const float4* p = reinterpret_cast<const float4*>(a.xpf) + 2 * (size_t)slot;
+                    const float4 h = __ldg(p), l = __ldg(p + 1);
+                    dx = T(((float)x - h.x) - h.w);
+                    dy = T(((float)y - h.y) - l.x);
+                    dz = T(((float)z - h.z) - l.y);
+                }
                 const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
-                if (dx > hx) dx -= nx; else if (dx < -hx) dx += nx;
-                if (dy > hy) dy -= ny; else if (dy < -hy) dy += ny;
-                if (dz > hz) dz -= nz; else if (dz < -hz) dz += nz;
-                const double fX = (double)Fx, fY = (double)Fy, fZ = (double)Fz;
-                v[0] = fX; v[1] = fY; v[2] = fZ;
-                v[3] = dy * fZ - dz * fY;
-                v[4] = -dx * fZ + dz * fX;
-                v[5] = dx * fY - dy * fX;
+                if (dx > T(hx)) dx -= T(nx); else if (dx < T(-hx)) dx += T(nx);
+                if (dy > T(hy)) dy -= T(ny); else if (dy < T(-hy)) dy += T(ny);
+                if (dz > T(hz)) dz -= T(nz); else if (dz < T(-hz)) dz += T(nz);
+                v[0] = Fx; v[1] = Fy; v[2] = Fz;
+                v[3] = dy * Fz - dz * Fy;
+                v[4] = -dx * Fz + dz * Fx;
+                v[5] = dx * Fy - dy * Fx;
             }
         }
     }
@@ -258,7 +273,7 @@ k_collide_stream(const CollideArgs<T> a) {
     for (int d = 1; d < 32; d <<= 1) {
 #pragma unroll
         for (int k = 0; k < 6; ++k) {
-            const double o = __shfl_up_sync(FULL, v[k], d);
+            const T o = __shfl_up_sync(FULL, v[k], d);
             if (lane - d >= segStart) v[k] += o;
         }
     }
@@ -267,8 +282,8 @@ k_collide_stream(const CollideArgs<T> a) {
     if (tail && key >= 0) {
         double* Fp = a.ft + 3 * (size_t)key;
         double* Tp = a.ft + 3 * (size_t)a.nslot + 3 * (size_t)key;
-        atomicAdd(Fp + 0, v[0]); atomicAdd(Fp + 1, v[1]); atomicAdd(Fp + 2, v[2]);
-        atomicAdd(Tp + 0, v[3]); atomicAdd(Tp + 1, v[4]); atomicAdd(Tp + 2, v[5]);
+        atomicAdd(Fp + 0, (double)v[0]); atomicAdd(Fp + 1, (double)v[1]); atomicAdd(Fp + 2, (double)v[2]);
+        atomicAdd(Tp + 0, (double)v[3]); atomicAdd(Tp + 1, (double)v[4]); atomicAdd(Tp + 2, (double)v[5]);
     }
 }
 

@@ -11,10 +11,19 @@
 // list through the same state machine.  Cells are independent, so the result
 // equals the sequential sweep exactly.
 //
-// Arithmetic is IEEE double with every multiply and add rounded separately
-// (__dmul_rn / __dadd_rn: no fused multiply-add), in the reference's operation
-// order, so the sub-cell counts n, the owner tags and the surface velocities
-// are bit-identical to the CPU result.
+// Exactness of the sub-cell count.  The reference decides, in IEEE double,
+//   dist = (dx^2 + dy^2) + dz^2  against (r + sqrt(3.1)/2)^2 and (r - sqrt(3.1)/2)^2,
+//   (xs_i + ys_j) + zs_k < r^2   for the 125 sub-cell centres of shell cells.
+// GB300 runs double arithmetic at a small fraction of its float rate, so every
+// comparison is first evaluated in float together with a proven error bound
+// (margin M = 2^-15 (r + 5)^2, at least 8x the worst-case float error for cells
+// inside the box [x - r - 3, x + r + 3] with |x| < 2^24).  A float result
+// farther than M from the threshold decides the comparison exactly as the
+// double computation would; only cells with a comparison inside the band are
+// recomputed with the reference's double sequence (__dadd_rn/__dmul_rn, no
+// fused multiply-add).  The counts n and owner tags are therefore identical to
+// the sequential CPU result, and the FP64 form also reproduces the particle
+// surface velocity bit for bit.
 #include "lbdem_internal.h"
 
 namespace lbdem {
@@ -25,16 +34,14 @@ constexpr double SQRT3HALF = 0.8803408430829505;  // sqrt(3.1)/2, src/ibProcesso
 __device__ __forceinline__ double sub_delta(int i) {
     return i == 0 ? -0.4 : i == 1 ? -0.19999999999999996 : i == 2 ? 0.0 : i == 3 ? 0.20000000000000007 : 0.4;
 }
+__device__ __forceinline__ float sub_delta_f(int i) { return (float)sub_delta(i); }
 
-// calcSolidFraction as a sub-cell count n in [0,125]; sf = n / 125 exactly
-// (the early-outs return 0 and 1, i.e. n = 0 and n = 125).
-__device__ __forceinline__ int solid_count(double dx_, double dy_, double dz_, double r_) {
+// calcSolidFraction in the reference's double sequence, as a count n in [0,125]
+// (sf = n/125 exactly; the early-outs return 0 and 1, i.e. n = 0 and n = 125).
+__device__ __noinline__ int solid_count_exact(double dx_, double dy_, double dz_, const SphereDev& s) {
     const double dist = __dadd_rn(__dadd_rn(__dmul_rn(dx_, dx_), __dmul_rn(dy_, dy_)), __dmul_rn(dz_, dz_));
-    const double r_p = __dadd_rn(r_, SQRT3HALF);
-    if (dist > __dmul_rn(r_p, r_p)) return 0;
-    const double r_m = __dsub_rn(r_, SQRT3HALF);
-    if (dist < __dmul_rn(r_m, r_m)) return 125;
-    const double r_sq = __dmul_rn(r_, r_);
+    if (dist > s.rp2) return 0;
+    if (dist < s.rm2) return 125;
     double xs[5], ys[5], zs[5];
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
@@ -44,30 +51,60 @@ __device__ __forceinline__ int solid_count(double dx_, double dy_, double dz_, d
         const double az = __dadd_rn(dz_, d); zs[i] = __dmul_rn(az, az);
     }
     int n = 0;
+    for (int i = 0; i < 5; ++i)
+        for (int j = 0; j < 5; ++j) {
+            const double a = __dadd_rn(xs[i], ys[j]);
+#pragma unroll
+            for (int k = 0; k < 5; ++k) n += (__dadd_rn(a, zs[k]) < s.rsq) ? 1 : 0;
+        }
+    return n;
+}
+
+// Float evaluation of the sample count with the decision band; *unsure is set
+// when any of the 125 comparisons falls inside [rsq - M, rsq + M).
+__device__ __forceinline__ int solid_count_fast(float dxf, float dyf, float dzf, float rsq, float M, bool* unsure) {
+    float xs[5], ys[5], zs[5];
+#pragma unroll
+    for (int i = 0; i < 5; ++i) {
+        const float d = sub_delta_f(i);
+        const float ax = dxf + d; xs[i] = ax * ax;
+        const float ay = dyf + d; ys[i] = ay * ay;
+        const float az = dzf + d; zs[i] = az * az;
+    }
+    const float lo = rsq - M, hi = rsq + M;
+    int n_lo = 0, n_hi = 0;
 #pragma unroll
     for (int i = 0; i < 5; ++i)
 #pragma unroll
         for (int j = 0; j < 5; ++j) {
-            const double a = __dadd_rn(xs[i], ys[j]);
+            const float a = xs[i] + ys[j];
 #pragma unroll
-            for (int k = 0; k < 5; ++k) n += (__dadd_rn(a, zs[k]) < r_sq) ? 1 : 0;
+            for (int k = 0; k < 5; ++k) {
+                const float t = a + zs[k];
+                n_lo += t < lo ? 1 : 0;
+                n_hi += t < hi ? 1 : 0;
+            }
         }
-    return n;
+    *unsure = n_lo != n_hi;
+    return n_lo;
 }
 
 __device__ __forceinline__ int tiles_along(int n) { return (n + TILE - 1) / TILE; }
 
 // Per sphere: bounding box (double -> integer truncation toward zero,
 // src/ibProcessors3D.h:43-45) intersected with the lattice
-// (src/ibDataExchangeWrappers3D.hh:127-133), tile overlap counts, and the
-// tag -> lowest list index map (LAMMPS atom->map keeps the owned atom).
+// (src/ibDataExchangeWrappers3D.hh:127-133), thresholds, the float split of the
+// centre, the tag -> lowest list index map (LAMMPS atom->map keeps the owned
+// atom) and the number of tiles the box overlaps.
 __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereDev* __restrict__ sph,
-                                  int* __restrict__ tile_count, int* __restrict__ tag2slot,
-                                  unsigned* __restrict__ err, Geom g, int max_tag, double max_radius) {
+                                  SphereFast* __restrict__ fast, float* __restrict__ xpf,
+                                  int* __restrict__ tag2slot, unsigned* __restrict__ err, Geom g, int max_tag,
+                                  double max_radius) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     const double* p = rec + (size_t)i * REC_STRIDE;
     SphereDev s;
+    SphereFast q;
     for (int d = 0; d < 3; ++d) { s.x[d] = p[d]; s.v[d] = p[3 + d]; s.w[d] = p[6 + d]; }
     s.r = p[9];
     const double tagd = p[10];
@@ -86,9 +123,12 @@ __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereD
     const int dims[3] = {g.nx, g.ny, g.nz};
     for (int d = 0; d < 3; ++d) {
         const double xd = s.x[d];
-        // |x| bounded so that the integer conversions below are defined; such
-        // a sphere cannot reach the lattice anyway.
-        if (!(xd > -1.0e9 && xd < 1.0e9)) { s.valid = 0; s.lo[d] = 1; s.hi[d] = 0; continue; }
+        q.xh[d] = 0.f; q.xl[d] = 0.f;
+        // |x| < 2^24 keeps the integer conversions defined and the float split
+        // accurate; a sphere beyond cannot reach the lattice.
+        if (!(xd > -16777216.0 && xd < 16777216.0)) { s.valid = 0; s.lo[d] = 1; s.hi[d] = 0; continue; }
+        q.xh[d] = (float)xd;
+        q.xl[d] = (float)(xd - (double)q.xh[d]);
         long long lo = (long long)(__dsub_rn(__dsub_rn(xd, s.r), 2.0));
         long long hi = (long long)(__dadd_rn(__dadd_rn(xd, s.r), 2.0));
         if (lo < 0) lo = 0;
@@ -97,14 +137,55 @@ __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereD
         s.hi[d] = (int)(hi > -1 ? hi : -1);
         if (s.lo[d] > s.hi[d]) s.valid = 0;
     }
+    const double rp = __dadd_rn(s.r, SQRT3HALF), rm = __dsub_rn(s.r, SQRT3HALF);
+    s.rp2 = __dmul_rn(rp, rp);
+    s.rm2 = __dmul_rn(rm, rm);
+    s.rsq = __dmul_rn(s.r, s.r);
+    q.rp2 = (float)s.rp2;
+    q.rm2 = (float)s.rm2;
+    q.rsq = (float)s.rsq;
+    const float r5 = (float)s.r + 5.0f;
+    q.margin = ldexpf(r5 * r5, -15);
+    for (int d = 0; d < 3; ++d) {
+        q.lo[d] = s.valid ? s.lo[d] : 1;
+        q.hi[d] = s.valid ? s.hi[d] : 0;
+    }
+    q.tag = s.tag;
+    for (int d = 0; d < 3; ++d) { q.v[d] = (float)s.v[d]; q.w[d] = (float)s.w[d]; }
     sph[i] = s;
+    fast[i] = q;
+    float* xp = xpf + (size_t)i * 8;
+    xp[0] = q.xh[0]; xp[1] = q.xh[1]; xp[2] = q.xh[2]; xp[3] = q.xl[0];
+    xp[4] = q.xl[1]; xp[5] = q.xl[2]; xp[6] = 0.f; xp[7] = 0.f;
     if (s.tag >= 1) atomicMin(tag2slot + s.tag, i);
-    if (!s.valid) return;
+}
+
+// One warp per sphere, lanes stride over the tiles its box overlaps.
+// COUNT: tile_count[t] += 1.  FILL: list[off[t] + cursor[t]++] = sphere.
+template <bool FILL>
+__global__ void k_pairs(const SphereFast* __restrict__ fast, int n, int* __restrict__ tile_count,
+                        const int* __restrict__ off, int* __restrict__ cursor, int* __restrict__ list,
+                        int pair_capacity, Geom g) {
+    const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+    const int lane = threadIdx.x & 31;
+    if (i >= n) return;
+    const SphereFast& q = fast[i];
+    if (q.lo[0] > q.hi[0] || q.lo[1] > q.hi[1] || q.lo[2] > q.hi[2]) return;
+    const int tx0 = q.lo[0] / TILE, ty0 = q.lo[1] / TILE, tz0 = q.lo[2] / TILE;
+    const int ex = q.hi[0] / TILE - tx0 + 1, ey = q.hi[1] / TILE - ty0 + 1, ez = q.hi[2] / TILE - tz0 + 1;
     const int tny = tiles_along(g.ny), tnz = tiles_along(g.nz);
-    for (int tx = s.lo[0] / TILE; tx <= s.hi[0] / TILE; ++tx)
-        for (int ty = s.lo[1] / TILE; ty <= s.hi[1] / TILE; ++ty)
-            for (int tz = s.lo[2] / TILE; tz <= s.hi[2] / TILE; ++tz)
-                atomicAdd(tile_count + ((size_t)tx * tny + ty) * tnz + tz, 1);
+    const int total = ex * ey * ez;
+    for (int k = lane; k < total; k += 32) {
+        const int kz = k % ez, kr = k / ez;
+        const int ky = kr % ey, kx = kr / ey;
+        const size_t t = ((size_t)(tx0 + kx) * tny + (ty0 + ky)) * tnz + (tz0 + kz);
+        if (!FILL) {
+            atomicAdd(tile_count + t, 1);
+        } else {
+            const int pos = off[t] + atomicAdd(cursor + t, 1);
+            if (pos < pair_capacity) list[pos] = i;
+        }
+    }
 }
 
 // Exclusive scan of the tile counts (one block): tile_count[t] becomes the
@@ -143,22 +224,6 @@ k_scan_tiles(int* __restrict__ cnt, int ntiles, int pair_capacity, int* __restri
     }
 }
 
-__global__ void k_fill_pairs(const SphereDev* __restrict__ sph, int n, const int* __restrict__ off,
-                             int* __restrict__ cursor, int* __restrict__ list, int pair_capacity, Geom g) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    const SphereDev& s = sph[i];
-    if (!s.valid) return;
-    const int tny = tiles_along(g.ny), tnz = tiles_along(g.nz);
-    for (int tx = s.lo[0] / TILE; tx <= s.hi[0] / TILE; ++tx)
-        for (int ty = s.lo[1] / TILE; ty <= s.hi[1] / TILE; ++ty)
-            for (int tz = s.lo[2] / TILE; tz <= s.hi[2] / TILE; ++tz) {
-                const size_t t = ((size_t)tx * tny + ty) * tnz + tz;
-                const int pos = off[t] + atomicAdd(cursor + t, 1);
-                if (pos < pair_capacity) list[pos] = i;
-            }
-}
-
 // Location of population i of cell c in the AA layout (phase = completed steps mod 2).
 template <typename T>
 __device__ __forceinline__ T* pop_slot(T* f, int i, int x, int y, int z, int phase, const Geom& g) {
@@ -173,6 +238,18 @@ __device__ __forceinline__ T* pop_slot(T* f, int i, int x, int y, int z, int pha
     return f + (size_t)opp(i) * g.N + ((size_t)X * g.ny + Y) * g.nz + Z;
 }
 
+// setValues, src/ibProcessors3D.hh:163-174 (com == x for single spheres):
+// u = v + omega x (cell - com), in the reference's double operation order.
+__device__ __forceinline__ void surface_velocity(const SphereDev& s, int X, int Y, int Z, double& u0, double& u1,
+                                                 double& u2) {
+    const double dx = __dsub_rn((double)X, s.x[0]);
+    const double dy = __dsub_rn((double)Y, s.x[1]);
+    const double dz = __dsub_rn((double)Z, s.x[2]);
+    u0 = __dadd_rn(s.v[0], __dsub_rn(__dmul_rn(s.w[1], dz), __dmul_rn(s.w[2], dy)));
+    u1 = __dadd_rn(s.v[1], __dadd_rn(__dmul_rn(-s.w[0], dz), __dmul_rn(s.w[2], dx)));
+    u2 = __dadd_rn(s.v[2], __dsub_rn(__dmul_rn(s.w[0], dy), __dmul_rn(s.w[1], dx)));
+}
+
 // One block per tile; 512 threads, one per cell of the 8^3 tile.
 // INIT_VEL: defineVelocity (src/ibCompositeDynamics3D.hh:118-127) is applied
 // with the uPart the cell holds right after each sphere that covers it fully
@@ -180,9 +257,9 @@ __device__ __forceinline__ T* pop_slot(T* f, int i, int x, int y, int z, int pha
 // such sphere decides the populations written.
 template <typename T, bool INIT_VEL>
 __global__ void __launch_bounds__(TILE_CELLS)
-k_voxelize(const SphereDev* __restrict__ sph, const int* __restrict__ off, const int* __restrict__ list,
-           uint32_t* __restrict__ vox, T* __restrict__ up, T* __restrict__ f, int phase, Geom g,
-           unsigned* __restrict__ err) {
+k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fast, const int* __restrict__ off,
+           const int* __restrict__ list, uint32_t* __restrict__ vox, T* __restrict__ up, T* __restrict__ f,
+           int phase, Geom g, unsigned* __restrict__ err) {
     __shared__ int s_raw[TILE_LIST_MAX];
     __shared__ int s_sorted[TILE_LIST_MAX];
     const int t = blockIdx.x;
@@ -221,31 +298,49 @@ k_voxelize(const SphereDev* __restrict__ sph, const int* __restrict__ off, const
     if (n_old > 0) { u0 = up[c]; u1 = up[g.N + c]; u2 = up[2 * g.N + c]; }
     bool dirty = false, define_vel = false;
     T d0 = T(0), d1 = T(0), d2 = T(0);
-    const double xG = (double)X, yG = (double)Y, zG = (double)Z;
+    const float Xf = (float)X, Yf = (float)Y, Zf = (float)Z;
 
     for (int k = 0; k < cnt; ++k) {
-        const SphereDev& s = sph[s_sorted[k]];
-        if (X < s.lo[0] || X > s.hi[0] || Y < s.lo[1] || Y > s.hi[1] || Z < s.lo[2] || Z > s.hi[2]) continue;
-        const double dx = __dsub_rn(xG, s.x[0]);
-        const double dy = __dsub_rn(yG, s.x[1]);
-        const double dz = __dsub_rn(zG, s.x[2]);
-        const int n = solid_count(dx, dy, dz, s.r);
+        const int si = s_sorted[k];
+        const SphereFast& q = fast[si];
+        if (X < q.lo[0] || X > q.hi[0] || Y < q.lo[1] || Y > q.hi[1] || Z < q.lo[2] || Z > q.hi[2]) continue;
+        const float dxf = (Xf - q.xh[0]) - q.xl[0];
+        const float dyf = (Yf - q.xh[1]) - q.xl[1];
+        const float dzf = (Zf - q.xh[2]) - q.xl[2];
+        const float distf = (dxf * dxf + dyf * dyf) + dzf * dzf;
+        const float M = q.margin;
+        int n;
+        bool exact = fabsf(distf - q.rp2) <= M || fabsf(distf - q.rm2) <= M;
+        if (!exact) {
+            if (distf > q.rp2) n = 0;
+            else if (distf < q.rm2) n = 125;
+            else n = solid_count_fast(dxf, dyf, dzf, q.rsq, M, &exact);
+        }
+        if (exact) {
+            const SphereDev& s = sph[si];
+            n = solid_count_exact(__dsub_rn((double)X, s.x[0]), __dsub_rn((double)Y, s.x[1]),
+                                  __dsub_rn((double)Z, s.x[2]), s);
+        }
         // decFlag, src/ibProcessors3D.hh:85-105 (sf > 0.001 <=> n > 0; sf > sf_old <=> n > n_old)
         const int dec = (n > 0 ? 1 : 0) + (n_old > 0 ? 2 : 0);
         bool set = false, zero = false;
         if (dec == 1) set = true;
-        else if (dec == 2) zero = (id_old == s.tag);
-        else if (dec == 3) set = (n > n_old) || (id_old == s.tag);
+        else if (dec == 2) zero = (id_old == q.tag);
+        else if (dec == 3) set = (n > n_old) || (id_old == q.tag);
         // dec == 0 is setToZero on a cell that is already empty
         if (zero) {
             n_old = 0; id_old = 0; u0 = u1 = u2 = T(0); dirty = true;
         } else if (set) {
-            // setValues, src/ibProcessors3D.hh:163-174 (com == x for single spheres)
-            const double a0 = __dadd_rn(s.v[0], __dsub_rn(__dmul_rn(s.w[1], dz), __dmul_rn(s.w[2], dy)));
-            const double a1 = __dadd_rn(s.v[1], __dadd_rn(__dmul_rn(-s.w[0], dz), __dmul_rn(s.w[2], dx)));
-            const double a2 = __dadd_rn(s.v[2], __dsub_rn(__dmul_rn(s.w[0], dy), __dmul_rn(s.w[1], dx)));
-            u0 = T(a0); u1 = T(a1); u2 = T(a2);
-            n_old = n; id_old = s.tag; dirty = true;
+            if (sizeof(T) == 8) {
+                double a0, a1, a2;
+                surface_velocity(sph[si], X, Y, Z, a0, a1, a2);
+                u0 = T(a0); u1 = T(a1); u2 = T(a2);
+            } else {
+                u0 = T(q.v[0] + (q.w[1] * dzf - q.w[2] * dyf));
+                u1 = T(q.v[1] + (-q.w[0] * dzf + q.w[2] * dxf));
+                u2 = T(q.v[2] + (q.w[0] * dyf - q.w[1] * dxf));
+            }
+            n_old = n; id_old = q.tag; dirty = true;
         }
         if (INIT_VEL && n == 125) { define_vel = true; d0 = u0; d1 = u1; d2 = u2; }
     }
@@ -267,12 +362,18 @@ k_voxelize(const SphereDev* __restrict__ sph, const int* __restrict__ off, const
 
 }  // namespace
 
-cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, int* tile_count,
-                                   int* tag2slot, unsigned* err, Geom g, int max_tag,
-                                   double max_radius, cudaStream_t s) {
+cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
+                                   int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
+                                   cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_prepare_spheres<<<(n + 127) / 128, 128, 0, s>>>(rec, n, sph, tile_count, tag2slot, err, g, max_tag,
+    k_prepare_spheres<<<(n + 127) / 128, 128, 0, s>>>(rec, n, sph, fast, xpf, tag2slot, err, g, max_tag,
                                                      max_radius);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_count_pairs(const SphereFast* fast, int n, int* tile_count, Geom g, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_pairs<false><<<(n + 7) / 8, 256, 0, s>>>(fast, n, tile_count, nullptr, nullptr, nullptr, 0, g);
     return cudaGetLastError();
 }
 
@@ -282,29 +383,28 @@ cudaError_t launch_scan_tiles(int* tile_count, int ntiles, int pair_capacity, in
     return cudaGetLastError();
 }
 
-cudaError_t launch_fill_pairs(const SphereDev* sph, int n, const int* tile_off, int* cursor, int* list,
+cudaError_t launch_fill_pairs(const SphereFast* fast, int n, const int* tile_off, int* cursor, int* list,
                               int pair_capacity, Geom g, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_fill_pairs<<<(n + 127) / 128, 128, 0, s>>>(sph, n, tile_off, cursor, list, pair_capacity, g);
+    k_pairs<true><<<(n + 7) / 8, 256, 0, s>>>(fast, n, nullptr, tile_off, cursor, list, pair_capacity, g);
     return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t launch_voxelize(const SphereDev* sph, const int* tile_off, const int* list, int ntiles,
-                            int pair_capacity, uint32_t* vox, T* up, T* f, int init_vel, int odd_phase,
-                            Geom g, unsigned* err, cudaStream_t s) {
-    (void)pair_capacity;
+cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, const int* tile_off, const int* list,
+                            int ntiles, uint32_t* vox, T* up, T* f, int init_vel, int odd_phase, Geom g,
+                            unsigned* err, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
     if (init_vel)
-        k_voxelize<T, true><<<ntiles, TILE_CELLS, 0, s>>>(sph, tile_off, list, vox, up, f, odd_phase, g, err);
+        k_voxelize<T, true><<<ntiles, TILE_CELLS, 0, s>>>(sph, fast, tile_off, list, vox, up, f, odd_phase, g, err);
     else
-        k_voxelize<T, false><<<ntiles, TILE_CELLS, 0, s>>>(sph, tile_off, list, vox, up, f, odd_phase, g, err);
+        k_voxelize<T, false><<<ntiles, TILE_CELLS, 0, s>>>(sph, fast, tile_off, list, vox, up, f, odd_phase, g, err);
     return cudaGetLastError();
 }
 
-template cudaError_t launch_voxelize<float>(const SphereDev*, const int*, const int*, int, int, uint32_t*,
-                                            float*, float*, int, int, Geom, unsigned*, cudaStream_t);
-template cudaError_t launch_voxelize<double>(const SphereDev*, const int*, const int*, int, int, uint32_t*,
-                                             double*, double*, int, int, Geom, unsigned*, cudaStream_t);
+template cudaError_t launch_voxelize<float>(const SphereDev*, const SphereFast*, const int*, const int*, int,
+                                            uint32_t*, float*, float*, int, int, Geom, unsigned*, cudaStream_t);
+template cudaError_t launch_voxelize<double>(const SphereDev*, const SphereFast*, const int*, const int*, int,
+                                             uint32_t*, double*, double*, int, int, Geom, unsigned*, cudaStream_t);
 
 }  // namespace lbdem

@@ -29,6 +29,8 @@ struct lbdem_handle {
     int cap = 0;
     double* d_rec = nullptr;    // [cap][12]
     SphereDev* d_sph = nullptr; // [cap]
+    SphereFast* d_fast = nullptr; // [cap]
+    float* d_xpf = nullptr;     // [cap][8]
     int* d_tag2slot = nullptr;  // [max_tag + 1]
     int ntiles = 0;
     int* d_tile_off = nullptr;  // [ntiles + 1]
@@ -98,8 +100,8 @@ cudaError_t dalloc(lbdem_handle* h, P** p, size_t bytes) {
 }
 
 void release(lbdem_handle* h) {
-    void* dev[] = {h->f, h->vox, h->up, h->cf, h->btab, h->d_rec, h->d_sph, h->d_tag2slot, h->d_tile_off,
-                   h->d_cursor, h->d_list, h->d_ft, h->d_err, h->d_mass, h->scratch};
+    void* dev[] = {h->f, h->vox, h->up, h->cf, h->btab, h->d_rec, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot,
+                   h->d_tile_off, h->d_cursor, h->d_list, h->d_ft, h->d_err, h->d_mass, h->scratch};
     for (void* p : dev)
         if (p) cudaFree(p);
     void* host[] = {h->h_rec, h->h_ft, h->h_err};
@@ -142,18 +144,19 @@ lbdem_status voxelize(lbdem_handle* h, int n, int init_vel) {
     CK(h, cudaMemsetAsync(h->d_tile_off, 0, sizeof(int) * ((size_t)h->ntiles + 1), s));
     CK(h, cudaMemsetAsync(h->d_tag2slot, 0x7F, sizeof(int) * ((size_t)h->cfg.max_tag + 1), s));
     if (n > 0) {
-        CK(h, launch_prepare_spheres(h->d_rec, n, h->d_sph, h->d_tile_off, h->d_tag2slot, h->d_err, h->g,
+        CK(h, launch_prepare_spheres(h->d_rec, n, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot, h->d_err, h->g,
                                      h->cfg.max_tag, h->cfg.max_radius, s));
+        CK(h, launch_count_pairs(h->d_fast, n, h->d_tile_off, h->g, s));
         CK(h, launch_scan_tiles(h->d_tile_off, h->ntiles, h->pair_cap, h->d_cursor, h->d_err, s));
-        CK(h, launch_fill_pairs(h->d_sph, n, h->d_tile_off, h->d_cursor, h->d_list, h->pair_cap, h->g, s));
+        CK(h, launch_fill_pairs(h->d_fast, n, h->d_tile_off, h->d_cursor, h->d_list, h->pair_cap, h->g, s));
         const int phase = (int)(h->step & 1);
         if (h->prec == LBDEM_PREC_FP64)
-            CK(h, launch_voxelize<double>(h->d_sph, h->d_tile_off, h->d_list, h->ntiles, h->pair_cap, h->vox,
+            CK(h, launch_voxelize<double>(h->d_sph, h->d_fast, h->d_tile_off, h->d_list, h->ntiles, h->vox,
                                           (double*)h->up, (double*)h->f, init_vel, phase, h->g, h->d_err, s));
         else
-            CK(h, launch_voxelize<float>(h->d_sph, h->d_tile_off, h->d_list, h->ntiles, h->pair_cap, h->vox,
+            CK(h, launch_voxelize<float>(h->d_sph, h->d_fast, h->d_tile_off, h->d_list, h->ntiles, h->vox,
                                          (float*)h->up, (float*)h->f, init_vel, phase, h->g, h->d_err, s));
-        h->launches += 4;
+        h->launches += 5;
     }
     h->n_cur = n;
     return LBDEM_OK;
@@ -207,6 +210,8 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
         return LBDEM_ERR_INVALID_ARG;
     const size_t N = (size_t)c.nx * c.ny * c.nz;
     if ((size_t)c.nx * c.ny > 0x7fffffffu || c.nz > 65535 * COLLIDE_BLOCK) return LBDEM_ERR_INVALID_ARG;
+    // cell coordinates must be exact in float (voxelization filter, float torque arm)
+    if (c.nx >= (1 << 24) || c.ny >= (1 << 24) || c.nz >= (1 << 24)) return LBDEM_ERR_INVALID_ARG;
 
     int ndev = 0;
     if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0 || c.device < 0 || c.device >= ndev) {
@@ -258,6 +263,8 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     const size_t capn = (size_t)(h->cap > 0 ? h->cap : 1);
     TRY(dalloc(h, &h->d_rec, capn * REC_STRIDE * sizeof(double)));
     TRY(dalloc(h, &h->d_sph, capn * sizeof(SphereDev)));
+    TRY(dalloc(h, &h->d_fast, capn * sizeof(SphereFast)));
+    TRY(dalloc(h, &h->d_xpf, capn * 8 * sizeof(float)));
     TRY(dalloc(h, &h->d_tag2slot, ((size_t)c.max_tag + 1) * sizeof(int)));
     TRY(dalloc(h, &h->d_tile_off, ((size_t)h->ntiles + 1) * sizeof(int)));
     TRY(dalloc(h, &h->d_cursor, (size_t)h->ntiles * sizeof(int)));
@@ -401,14 +408,14 @@ lbdem_status lbdem_collide_and_stream(lbdem_handle* h) {
     if (h->prec == LBDEM_PREC_FP64) {
         CollideArgs<double> a;
         a.g = h->g; a.f = (double*)h->f; a.vox = h->vox; a.up = (const double*)h->up; a.cf = (double*)h->cf;
-        a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.nslot = n; a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err;
+        a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.xpf = h->d_xpf; a.nslot = n; a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err;
         a.btab = h->btab; a.omega = h->cfg.omega;
         for (int d = 0; d < 3; ++d) a.g3[d] = h->cfg.body_force[d];
         CK(h, launch_collide_stream<double>(a, odd, force, h->stream));
     } else {
         CollideArgs<float> a;
         a.g = h->g; a.f = (float*)h->f; a.vox = h->vox; a.up = (const float*)h->up; a.cf = (float*)h->cf;
-        a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.nslot = n; a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err;
+        a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.xpf = h->d_xpf; a.nslot = n; a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err;
         a.btab = h->btab; a.omega = h->cfg.omega;
         for (int d = 0; d < 3; ++d) a.g3[d] = h->cfg.body_force[d];
         CK(h, launch_collide_stream<float>(a, odd, force, h->stream));

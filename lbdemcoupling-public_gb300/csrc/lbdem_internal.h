@@ -54,6 +54,7 @@ struct CollideArgs {
     T* cf;                   // [3][N] per-cell force (nullptr: not kept)
     const int* tag2slot;     // [max_tag + 1] lowest particle index per tag
     const double* rec;       // [n][12] particle records (positions for the torque arm)
+    const float* xpf;        // [n][8] centre split into float hi/lo (float form's torque arm)
     int nslot;               // particles in the current list
     int max_tag;             // tag2slot has max_tag + 1 entries
     double* ft;              // [6][n]: F (3n) then T (3n)
@@ -63,28 +64,41 @@ struct CollideArgs {
     double g3[3];
 };
 
+// Exact (double) description of one sphere of the list, for the decisions
+// that need the reference's double arithmetic.
 struct SphereDev {
     double x[3], v[3], w[3], r;
+    double rp2, rm2, rsq;    // (r + sqrt(3.1)/2)^2, (r - sqrt(3.1)/2)^2, r^2 in double
+    int tag, valid;
+    int lo[3], hi[3];        // bounding box clipped to the lattice (lo > hi: empty)
+};
+
+// Float description read by every cell of the voxelization fold.
+struct SphereFast {
+    float xh[3], xl[3];      // centre = xh + xl
+    float rp2, rm2, rsq;     // thresholds rounded to float
+    float margin;            // decision band half-width, 2^-15 (r + 5)^2
+    int lo[3], hi[3];        // empty box: lo > hi
     int tag;
-    int lo[3], hi[3];
-    int valid;
+    float v[3], w[3];        // velocity and angular velocity rounded to float
 };
 
 // Launchers (return cudaGetLastError() of the launch).
 template <typename T>
 cudaError_t launch_collide_stream(const CollideArgs<T>& a, bool odd, bool force, cudaStream_t s);
 
-cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, int* tile_count,
-                                   int* tag2slot, unsigned* err, Geom g, int max_tag,
-                                   double max_radius, cudaStream_t s);
+cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
+                                   int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
+                                   cudaStream_t s);
+cudaError_t launch_count_pairs(const SphereFast* fast, int n, int* tile_count, Geom g, cudaStream_t s);
 cudaError_t launch_scan_tiles(int* tile_count, int ntiles, int pair_capacity, int* cursor,
                               unsigned* err, cudaStream_t s);
-cudaError_t launch_fill_pairs(const SphereDev* sph, int n, const int* tile_off, int* cursor,
+cudaError_t launch_fill_pairs(const SphereFast* fast, int n, const int* tile_off, int* cursor,
                               int* list, int pair_capacity, Geom g, cudaStream_t s);
 template <typename T>
-cudaError_t launch_voxelize(const SphereDev* sph, const int* tile_off, const int* list,
-                            int ntiles, int pair_capacity, uint32_t* vox, T* up, T* f,
-                            int init_vel, int odd_phase, Geom g, unsigned* err, cudaStream_t s);
+cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, const int* tile_off,
+                            const int* list, int ntiles, uint32_t* vox, T* up, T* f, int init_vel,
+                            int odd_phase, Geom g, unsigned* err, cudaStream_t s);
 
 // Field helpers.  phase: number of completed steps mod 2 (storage layout).
 template <typename T>

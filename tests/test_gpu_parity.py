@@ -63,10 +63,14 @@ def _run(lbdem, oracle, case, precision, steps, init_steps=(0, 3), seed=7):
         assert np.array_equal(gl.get_field(lbdem.FIELD_SUBCELL_COUNT), ost["n"]), f"step {s}: counts differ"
         assert np.array_equal(gl.get_field(lbdem.FIELD_PARTICLE_ID), ost["id"]), f"step {s}: owner tags differ"
         assert np.array_equal(gl.get_field(lbdem.FIELD_SOLID_FRACTION), ost["sf"]), f"step {s}: sf differs"
-        assert np.array_equal(gl.get_field(lbdem.FIELD_PARTICLE_VELOCITY), ost["up"]), f"step {s}: uPart differs"
+        upg = gl.get_field(lbdem.FIELD_PARTICLE_VELOCITY)
+        if dt == np.float64:   # FP64 form: the reference's double sequence, bit for bit
+            assert np.array_equal(upg, ost["up"]), f"step {s}: uPart differs"
+        else:                  # FP32 form: evaluated in float
+            assert rel_err(upg, ost["up"]) <= 1e-6, f"step {s}: uPart {rel_err(upg, ost['up']):.3e}"
         if iv:
             assert np.array_equal(gl.get_populations(), ol.get_populations()) or \
-                rel_err(gl.get_populations(), ol.get_populations()) <= (1e-14 if dt == np.float64 else 1e-6)
+                rel_err(gl.get_populations(), ol.get_populations()) <= (1e-14 if dt == np.float64 else 2e-5)
         gl.collide_and_stream()
         ol.collide_and_stream()
         Fg, Tg = gl.get_forces()
