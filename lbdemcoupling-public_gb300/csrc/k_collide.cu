@@ -15,9 +15,15 @@
 // is replaced by the cell itself with the direction reversed: half-way
 // bounce-back.  Periodic axes wrap.
 //
-// One thread per cell, a block spans 128 consecutive cells of one z-row, so
-// every population access of a warp is one contiguous 128-float / 256-double
-// segment (shifted by one element for c_z != 0 in the odd phase).
+// Two kernels implement the step:
+//  * k_collide_staged (nz a multiple of 16 bytes of populations): persistent
+//    CTAs of 128 threads walk 128-cell z-segments.  The 19 population rows of
+//    a segment (plus one 16-byte halo chunk per c_z != 0 direction in the odd
+//    phase, and the voxel words) are copied into shared memory with
+//    cp.async.bulk on an mbarrier, double-buffered, so the next segment's
+//    bytes are in flight while the current one is collided.  The staged
+//    pre-collision values double as fPre of the PSM update.
+//  * k_collide_direct (any nz): one thread per cell, direct global loads.
 #include "lbdem_internal.h"
 
 namespace lbdem {
@@ -106,15 +112,15 @@ __device__ __forceinline__ void bgk(T (&f)[Q], T omega, T gx, T gy, T gz) {
     }
 }
 
+
 // PSM collision of a cell with n > 0 solid sub-cells,
-// src/ibCompositeDynamics3D.hh:130-203.  n == 125 is the full-solid branch
-// (no BGK, B = 1, which reduces the weighted update to fPre + bb exactly).
-template <typename T, bool FORCE>
-__device__ __forceinline__ void psm(T (&f)[Q], int n, T up0, T up1, T up2, T B, T omega,
-                                    T gx, T gy, T gz, T& Fx, T& Fy, T& Fz) {
-    T fPre[Q];
-#pragma unroll
-    for (int i = 0; i < Q; ++i) fPre[i] = f[i];
+// src/ibCompositeDynamics3D.hh:130-203.  On entry f holds the pre-collision
+// populations; pre(i) returns the same pre-collision value (fPre).  n == 125 is
+// the full-solid branch (no BGK, B = 1, which reduces the weighted update to
+// fPre + bb exactly).
+template <typename T, bool FORCE, typename Pre>
+__device__ __forceinline__ void psm(T (&f)[Q], int n, T up0, T up1, T up2, T B, T omega, T gx, T gy, T gz,
+                                    const Pre& pre, T& Fx, T& Fy, T& Fz) {
     if (n < 125) bgk<T, FORCE>(f, omega, gx, gy, gz);
     T rhoBar, jx, jy, jz;
     moments(f, rhoBar, jx, jy, jz);                  // post-collision moments, :146-148
@@ -125,7 +131,10 @@ __device__ __forceinline__ void psm(T (&f)[Q], int n, T up0, T up1, T up2, T B, 
     const T baseE = rhoBar - T(1.5) * invRho * (jx * jx + jy * jy + jz * jz);
     const T baseS = rhoBar - T(1.5) * invRho * (ux * ux + uy * uy + uz * uz);
     const T omB = T(1) - B;
-    f[0] = fPre[0] + omB * (f[0] - fPre[0]) + B * (T(wt(0)) * baseE - T(wt(0)) * baseS);
+    {
+        const T p0 = pre(0);
+        f[0] = p0 + omB * (f[0] - p0) + B * (T(wt(0)) * baseE - T(wt(0)) * baseS);
+    }
     Fx = T(0); Fy = T(0); Fz = T(0);
 #pragma unroll
     for (int i = 1; i <= 9; ++i) {
@@ -137,10 +146,11 @@ __device__ __forceinline__ void psm(T (&f)[Q], int n, T up0, T up1, T up2, T B, 
         const T eS = baseS + q45 * cu * cu, sS = T(3) * cu;
         const T fEq_i = t * (eE + sE), fEq_o = t * (eE - sE);
         const T fEqS_i = t * (eS + sS), fEqS_o = t * (eS - sS);
-        const T bb = B * ((fPre[o] - fEq_o) - (fPre[i] - fEqS_i));
-        const T bbOpp = B * ((fPre[i] - fEq_i) - (fPre[o] - fEqS_o));
-        f[i] = fPre[i] + omB * (f[i] - fPre[i]) + bb;
-        f[o] = fPre[o] + omB * (f[o] - fPre[o]) + bbOpp;
+        const T pi = pre(i), po = pre(o);
+        const T bb = B * ((po - fEq_o) - (pi - fEqS_i));
+        const T bbOpp = B * ((pi - fEq_i) - (po - fEqS_o));
+        f[i] = pi + omB * (f[i] - pi) + bb;
+        f[o] = po + omB * (f[o] - po) + bbOpp;
         const T d = bb - bbOpp;                      // F -= c_i (bb - bbOpp), :172-174
         if (cx(i) > 0) Fx -= d; else if (cx(i) < 0) Fx += d;
         if (cy(i) > 0) Fy -= d; else if (cy(i) < 0) Fy += d;
@@ -148,121 +158,67 @@ __device__ __forceinline__ void psm(T (&f)[Q], int n, T up0, T up1, T up2, T B, 
     }
 }
 
-__device__ __forceinline__ int wrap_minus(int v, int n, int per) { return v > 0 ? v - 1 : (per ? n - 1 : -1); }
-__device__ __forceinline__ int wrap_plus(int v, int n, int per) { return v < n - 1 ? v + 1 : (per ? 0 : -1); }
-__device__ __forceinline__ int pick(int c, int m, int v, int p) { return c < 0 ? m : (c > 0 ? p : v); }
-
-template <typename T, bool ODD, bool FORCE>
-__global__ void __launch_bounds__(COLLIDE_BLOCK)
-k_collide_stream(const CollideArgs<T> a) {
-    const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
-    const size_t N = a.g.N;
-    const int row = blockIdx.x;
-    const int x = row / ny;
-    const int y = row - x * ny;
-    const int z = blockIdx.y * COLLIDE_BLOCK + threadIdx.x;
-    const bool valid = z < nz;
-    const size_t c = ((size_t)x * ny + y) * nz + (valid ? z : 0);
-    T* __restrict__ F = a.f;
-
-    // Per-cell force and torque, summed over a warp in the population type
-    // (double for the FP64 form) and accumulated per particle in double.
-    int key = -1;
-    T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-
-    if (valid) {
-        // neighbour coordinates along each axis (-1: beyond a wall)
-        int xm = 0, xp = 0, ym = 0, yp = 0, zm = 0, zp = 0;
-        if (ODD) {
-            xm = wrap_minus(x, nx, a.g.per[0]); xp = wrap_plus(x, nx, a.g.per[0]);
-            ym = wrap_minus(y, ny, a.g.per[1]); yp = wrap_plus(y, ny, a.g.per[1]);
-            zm = wrap_minus(z, nz, a.g.per[2]); zp = wrap_plus(z, nz, a.g.per[2]);
-        }
-        auto nb = [&](int i) -> long long {
-            const int X = pick(cx(i), xm, x, xp), Y = pick(cy(i), ym, y, yp), Z = pick(cz(i), zm, z, zp);
-            if (X < 0 || Y < 0 || Z < 0) return -1;
-            return ((long long)X * ny + Y) * nz + Z;
-        };
-
-        T f[Q];
-        if (!ODD) {
-#pragma unroll
-            for (int i = 0; i < Q; ++i) f[i] = __ldcs(F + (size_t)i * N + c);
-        } else {
-            f[0] = __ldcs(F + c);
-#pragma unroll
-            for (int i = 1; i < Q; ++i) {
-                const long long s = nb(opp(i));
-                f[i] = s >= 0 ? __ldcs(F + (size_t)opp(i) * N + (size_t)s) : __ldcs(F + (size_t)i * N + c);
-            }
-        }
-
-        const uint32_t w = __ldg(a.vox + c);
-        const int n = min((int)(w & VOX_NMASK), 125);
-        const T omega = T(a.omega);
-        const T gx = T(a.g3[0]), gy = T(a.g3[1]), gz = T(a.g3[2]);
-        T Fx = T(0), Fy = T(0), Fz = T(0);
-        if (n == 0) {
-            bgk<T, FORCE>(f, omega, gx, gy, gz);
-        } else {
-            const T up0 = __ldg(a.up + c), up1 = __ldg(a.up + N + c), up2 = __ldg(a.up + 2 * N + c);
-            const T B = T(__ldg(a.btab + n));
-            psm<T, FORCE>(f, n, up0, up1, up2, B, omega, gx, gy, gz, Fx, Fy, Fz);
-        }
-
-        if (!ODD) {
-#pragma unroll
-            for (int i = 0; i < Q; ++i) __stcs(F + (size_t)opp(i) * N + c, f[i]);
-        } else {
-            __stcs(F + c, f[0]);
-#pragma unroll
-            for (int i = 1; i < Q; ++i) {
-                const long long d = nb(i);
-                if (d >= 0) __stcs(F + (size_t)i * N + (size_t)d, f[i]);
-                else __stcs(F + (size_t)opp(i) * N + c, f[i]);
-            }
-        }
-
-        if (a.cf) {
-            a.cf[c] = Fx; a.cf[N + c] = Fy; a.cf[2 * N + c] = Fz;
-        }
-
-        if (n > 0) {
-            const int tag = (int)(w >> VOX_NBITS);
-            const int slot = tag <= a.max_tag ? __ldg(a.tag2slot + tag) : -1;
-            if (slot < 0 || slot >= a.nslot) {
-                atomicOr(a.err, 0x8u);   // LBDEM_DEVERR_UNMAPPED_TAG
-            } else {
-                key = slot;
-                // torque arm with the minimum image of src/ibProcessors3D.hh:230-243
-                T dx, dy, dz;
-                if (sizeof(T) == 8) {
-                    const double* p = a.rec + (size_t)slot * REC_STRIDE;
-                    dx = T((double)x - __ldg(p + 0));
-                    dy = T((double)y - __ldg(p + 1));
-                    dz = T((double)z - __ldg(p + 2));
-                } else {
-                    // centre = hi + lo in float: (x - hi) - lo is the arm to ~1 ulp
-                    const float4* p = reinterpret_cast<const float4*>(a.xpf) + 2 * (size_t)slot;
-                    const float4 h = __ldg(p), l = __ldg(p + 1);
-                    dx = T(((float)x - h.x) - h.w);
-                    dy = T(((float)y - h.y) - l.x);
-                    dz = T(((float)z - h.z) - l.y);
-                }
-                const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
-                if (dx > T(hx)) dx -= T(nx); else if (dx < T(-hx)) dx += T(nx);
-                if (dy > T(hy)) dy -= T(ny); else if (dy < T(-hy)) dy += T(ny);
-                if (dz > T(hz)) dz -= T(nz); else if (dz < T(-hz)) dz += T(nz);
-                v[0] = Fx; v[1] = Fy; v[2] = Fz;
-                v[3] = dy * Fz - dz * Fy;
-                v[4] = -dx * Fz + dz * Fx;
-                v[5] = dx * Fy - dy * Fx;
-            }
-        }
+// Collision of one cell given its pre-collision populations: BGK for fluid
+// cells, PSM for cells with solid sub-cells.  Returns the hydrodynamic force.
+template <typename T, bool FORCE, typename Pre>
+__device__ __forceinline__ void collide_cell(const CollideArgs<T>& a, T (&f)[Q], uint32_t w, size_t c, const Pre& pre,
+                                             T& Fx, T& Fy, T& Fz) {
+    const int n = min((int)(w & VOX_NMASK), 125);
+    Fx = T(0); Fy = T(0); Fz = T(0);
+    if (n == 0) {
+        bgk<T, FORCE>(f, a.omega, a.g3[0], a.g3[1], a.g3[2]);
+    } else {
+        const size_t N = a.g.N;
+        const T up0 = __ldg(a.up + c), up1 = __ldg(a.up + N + c), up2 = __ldg(a.up + 2 * N + c);
+        psm<T, FORCE>(f, n, up0, up1, up2, __ldg(a.btab + n), a.omega, a.g3[0], a.g3[1], a.g3[2], pre, Fx, Fy,
+                      Fz);
     }
+}
 
-    // Warp-segmented sum over runs of equal particle slot (consecutive cells
-    // along z mostly belong to the same sphere), one set of double atomics per run.
+// Per-cell force and torque of a solid cell (SumForceTorque3D,
+// src/ibProcessors3D.hh:203-263): particle slot of the owner tag and the
+// terms F, r x F with the minimum-image arm of :230-243.  Returns the slot or -1.
+template <typename T>
+__device__ __forceinline__ int cell_force_terms(const CollideArgs<T>& a, uint32_t w, int x, int y, int z, T Fx,
+                                                T Fy, T Fz, T (&v)[6]) {
+    if ((w & VOX_NMASK) == 0) return -1;
+    const int tag = (int)(w >> VOX_NBITS);
+    const int slot = tag <= a.max_tag ? __ldg(a.tag2slot + tag) : -1;
+    if (slot < 0 || slot >= a.nslot) {
+        atomicOr(a.err, 0x8u);   // LBDEM_DEVERR_UNMAPPED_TAG
+        return -1;
+    }
+    T dx, dy, dz;
+    if (sizeof(T) == 8) {
+        const double* p = a.rec + (size_t)slot * REC_STRIDE;
+        dx = T((double)x - __ldg(p + 0));
+        dy = T((double)y - __ldg(p + 1));
+        dz = T((double)z - __ldg(p + 2));
+    } else {
+        // centre = hi + lo in float: (x - hi) - lo is the arm to ~1 ulp
+        const float4* p = reinterpret_cast<const float4*>(a.xpf) + 2 * (size_t)slot;
+        const float4 h = __ldg(p), l = __ldg(p + 1);
+        dx = T(((float)x - h.x) - h.w);
+        dy = T(((float)y - h.y) - l.x);
+        dz = T(((float)z - h.z) - l.y);
+    }
+    const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
+    const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
+    if (dx > T(hx)) dx -= T(nx); else if (dx < T(-hx)) dx += T(nx);
+    if (dy > T(hy)) dy -= T(ny); else if (dy < T(-hy)) dy += T(ny);
+    if (dz > T(hz)) dz -= T(nz); else if (dz < T(-hz)) dz += T(nz);
+    v[0] = Fx; v[1] = Fy; v[2] = Fz;
+    v[3] = dy * Fz - dz * Fy;
+    v[4] = -dx * Fz + dz * Fx;
+    v[5] = dx * Fy - dy * Fx;
+    return slot;
+}
+
+// Warp-segmented sum over runs of equal particle slot (consecutive cells along
+// z mostly belong to the same sphere), one set of double atomics per run.
+// Must be reached by all 32 lanes.
+template <typename T>
+__device__ __forceinline__ void reduce_forces(const CollideArgs<T>& a, int key, T (&v)[6]) {
     if (__ballot_sync(FULL, key >= 0) == 0u) return;
     const int lane = threadIdx.x & 31;
     const int prevKey = __shfl_up_sync(FULL, key, 1);
@@ -287,11 +243,338 @@ k_collide_stream(const CollideArgs<T> a) {
     }
 }
 
+__device__ __forceinline__ int wrap_minus(int v, int n, int per) { return v > 0 ? v - 1 : (per ? n - 1 : -1); }
+__device__ __forceinline__ int wrap_plus(int v, int n, int per) { return v < n - 1 ? v + 1 : (per ? 0 : -1); }
+__device__ __forceinline__ int pick(int c, int m, int v, int p) { return c < 0 ? m : (c > 0 ? p : v); }
+
+// ---------------------------------------------------------------------------
+// Direct kernel: one thread per cell, grid (nx * ny, ceil(nz / 128)).
+template <typename T, bool ODD, bool FORCE>
+__global__ void __launch_bounds__(COLLIDE_BLOCK)
+k_collide_direct(const CollideArgs<T> a) {
+    const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
+    const size_t N = a.g.N;
+    const int row = blockIdx.x;
+    const int x = row / ny;
+    const int y = row - x * ny;
+    const int z = blockIdx.y * COLLIDE_BLOCK + threadIdx.x;
+    const bool valid = z < nz;
+    const size_t c = ((size_t)x * ny + y) * nz + (valid ? z : 0);
+    T* __restrict__ F = a.f;
+
+    int key = -1;
+    T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+    if (valid) {
+        int xm = 0, xp = 0, ym = 0, yp = 0, zm = 0, zp = 0;
+        if (ODD) {
+            xm = wrap_minus(x, nx, a.g.per[0]); xp = wrap_plus(x, nx, a.g.per[0]);
+            ym = wrap_minus(y, ny, a.g.per[1]); yp = wrap_plus(y, ny, a.g.per[1]);
+            zm = wrap_minus(z, nz, a.g.per[2]); zp = wrap_plus(z, nz, a.g.per[2]);
+        }
+        auto nb = [&](int i) -> long long {
+            const int X = pick(cx(i), xm, x, xp), Y = pick(cy(i), ym, y, yp), Z = pick(cz(i), zm, z, zp);
+            if (X < 0 || Y < 0 || Z < 0) return -1;
+            return ((long long)X * ny + Y) * nz + Z;
+        };
+        T f[Q];
+        if (!ODD) {
+#pragma unroll
+            for (int i = 0; i < Q; ++i) f[i] = F[(size_t)i * N + c];
+        } else {
+            f[0] = F[c];
+#pragma unroll
+            for (int i = 1; i < Q; ++i) {
+                const long long s = nb(opp(i));
+                f[i] = s >= 0 ? F[(size_t)opp(i) * N + (size_t)s] : F[(size_t)i * N + c];
+            }
+        }
+        T fPre[Q];
+#pragma unroll
+        for (int i = 0; i < Q; ++i) fPre[i] = f[i];
+        const uint32_t w = __ldg(a.vox + c);
+        T Fx, Fy, Fz;
+        collide_cell<T, FORCE>(a, f, w, c, [&](int i) { return fPre[i]; }, Fx, Fy, Fz);
+        if (!ODD) {
+#pragma unroll
+            for (int i = 0; i < Q; ++i) F[(size_t)opp(i) * N + c] = f[i];
+        } else {
+            F[c] = f[0];
+#pragma unroll
+            for (int i = 1; i < Q; ++i) {
+                const long long d = nb(i);
+                if (d >= 0) F[(size_t)i * N + (size_t)d] = f[i];
+                else F[(size_t)opp(i) * N + c] = f[i];
+            }
+        }
+        if (a.cf) { a.cf[c] = Fx; a.cf[N + c] = Fy; a.cf[2 * N + c] = Fz; }
+        key = cell_force_terms(a, w, x, y, z, Fx, Fy, Fz, v);
+    }
+    reduce_forces(a, key, v);
+}
+
+// ---------------------------------------------------------------------------
+// Staged persistent kernel.
+constexpr int SEG = COLLIDE_BLOCK;          // cells per z-segment = threads per CTA
+constexpr int WAIT_LIMIT = 1 << 22;         // bounded mbarrier wait (iterations of try_wait)
+
+template <typename T>
+struct Stage {
+    static constexpr int V = 16 / (int)sizeof(T);   // elements per 16 bytes
+    static constexpr int W = SEG + 2 * V;           // row: V halo | SEG core | V halo
+    T f[2][Q][W];
+    uint32_t vox[2][SEG];
+    unsigned long long bar[2];
+};
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, uint32_t count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_addr(bar)), "r"(count) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive_expect_tx(unsigned long long* bar, uint32_t bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes)
+                 : "memory");
+}
+__device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_addr(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+// Bounded wait: false if the phase did not complete within WAIT_LIMIT tries.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
+    for (int k = 0; k < WAIT_LIMIT; ++k)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+// Global -> shared bulk copy completing on an mbarrier (16-byte aligned, size % 16 == 0).
+__device__ __forceinline__ void bulk_g2s(void* dst, const void* src, uint32_t bytes, unsigned long long* bar) {
+    asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                     smem_addr(dst)),
+                 "l"(src), "r"(bytes), "r"(smem_addr(bar))
+                 : "memory");
+}
+
+// Directions with c_z != 0 (they need a halo element in the odd phase).
+__device__ __forceinline__ int zdir(int k) {
+    // {3, 6, 7, 8, 9, 12, 15, 16, 17, 18} packed in 5-bit fields
+    constexpr unsigned long long D = 3ull | 6ull << 5 | 7ull << 10 | 8ull << 15 | 9ull << 20 | 12ull << 25 |
+                                     15ull << 30 | 16ull << 35 | 17ull << 40 | 18ull << 45;
+    return (int)((D >> (5 * k)) & 31u);
+}
+
+struct SegGeo {
+    int x, y, z0, len;
+    int xm, xp, ym, yp;     // neighbour rows along x and y (-1: beyond a wall)
+    size_t own;             // element offset of the own row (x, y, 0)
+};
+
+__device__ __forceinline__ SegGeo seg_geo(const Geom& g, long long seg, int nzseg) {
+    SegGeo s;
+    const long long row = seg / nzseg;
+    const int zs = (int)(seg - row * nzseg);
+    s.x = (int)(row / g.ny);
+    s.y = (int)(row - (long long)s.x * g.ny);
+    s.z0 = zs * SEG;
+    s.len = min(SEG, g.nz - s.z0);
+    s.xm = wrap_minus(s.x, g.nx, g.per[0]); s.xp = wrap_plus(s.x, g.nx, g.per[0]);
+    s.ym = wrap_minus(s.y, g.ny, g.per[1]); s.yp = wrap_plus(s.y, g.ny, g.per[1]);
+    s.own = ((size_t)s.x * g.ny + s.y) * g.nz;
+    return s;
+}
+
+// Row (x + dx, y + dy) as an element offset, or -1 beyond a wall.
+__device__ __forceinline__ long long row_off(const Geom& g, const SegGeo& s, int dx, int dy) {
+    const int X = pick(dx, s.xm, s.x, s.xp), Y = pick(dy, s.ym, s.y, s.yp);
+    if (X < 0 || Y < 0) return -1;
+    return ((long long)X * g.ny + Y) * g.nz;
+}
+
+// Issued by one warp: the segment's copies into buffer b.
+//   copies 0..18: population rows (even: own row, slot i; odd: row x - c_i,
+//                 slot opp i, or own row slot i when that row is beyond a wall);
+//   copies 19..28 (odd, periodic z): the 16-byte chunk holding the halo element
+//                 of the k-th c_z != 0 direction;
+//   copy 29: voxel words of the segment.
+template <typename T, bool ODD>
+__device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, Stage<T>& st, int b, long long seg,
+                                              int nzseg) {
+    constexpr int V = Stage<T>::V;
+    const int lane = threadIdx.x & 31;
+    const Geom& g = a.g;
+    const SegGeo s = seg_geo(g, seg, nzseg);
+    const size_t N = g.N;
+    const T* src = nullptr;
+    void* dst = nullptr;
+    uint32_t bytes = 0;
+    if (lane < Q) {
+        const int i = lane;
+        size_t off = (size_t)i * N + s.own + s.z0;
+        if (ODD && i != 0) {
+            const long long r = row_off(g, s, -cx(i), -cy(i));
+            if (r >= 0) off = (size_t)opp(i) * N + (size_t)r + s.z0;
+        }
+        src = a.f + off;
+        dst = &st.f[b][i][V];
+        bytes = (uint32_t)(s.len * sizeof(T));
+    } else if (ODD && lane < Q + 10) {
+        const int i = zdir(lane - Q);
+        const long long r = row_off(g, s, -cx(i), -cy(i));
+        if (r >= 0) {
+            int zc;      // first element of the 16-byte chunk (-1: beyond a z wall)
+            if (cz(i) > 0) {
+                zc = s.z0 - V;
+                if (zc < 0) zc = g.per[2] ? zc + g.nz : -1;
+                dst = &st.f[b][i][0];
+            } else {
+                zc = s.z0 + s.len;
+                if (zc >= g.nz) zc = g.per[2] ? zc - g.nz : -1;
+                dst = &st.f[b][i][V + s.len];
+            }
+            if (zc >= 0) {
+                src = a.f + (size_t)opp(i) * N + (size_t)r + zc;
+                bytes = 16;
+            }
+        }
+    } else if (lane == Q + 10) {
+        src = reinterpret_cast<const T*>(a.vox + s.own + s.z0);
+        dst = &st.vox[b][0];
+        bytes = (uint32_t)(s.len * sizeof(uint32_t));
+    }
+    const uint32_t total = __reduce_add_sync(FULL, bytes);
+    if (lane == 0) mbar_arrive_expect_tx(&st.bar[b], total);
+    __syncwarp();
+    if (bytes) bulk_g2s(dst, src, bytes, &st.bar[b]);
+}
+
+template <typename T, bool ODD, bool FORCE>
+__global__ void __launch_bounds__(SEG)
+k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
+    constexpr int V = Stage<T>::V;
+    __shared__ __align__(16) Stage<T> st;
+    const Geom& g = a.g;
+    const size_t N = g.N;
+    const int t = threadIdx.x;
+    const int warp = t >> 5;
+    T* __restrict__ F = a.f;
+    if (t == 0) {
+        mbar_init(&st.bar[0], 1);
+        mbar_init(&st.bar[1], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    __syncthreads();
+    long long seg = blockIdx.x;
+    if (seg >= nseg) return;
+    if (warp == 0) issue_segment<T, ODD>(a, st, 0, seg, nzseg);
+    uint32_t phase = 0;   // bit b: parity expected next on buffer b
+    int b = 0;
+    for (; seg < nseg; seg += gridDim.x, b ^= 1) {
+        const long long next = seg + gridDim.x;
+        if (next < nseg && warp == 0) issue_segment<T, ODD>(a, st, b ^ 1, next, nzseg);
+        const bool ok = mbar_wait(&st.bar[b], (phase >> b) & 1u);
+        phase ^= 1u << b;
+        if (__syncthreads_or(!ok)) {
+            // a copy did not land: report, let in-flight copies finish, leave
+            if (t == 0) atomicOr(a.err, 0x20u);   // LBDEM_DEVERR_TIMEOUT
+            if (next < nseg) mbar_wait(&st.bar[b ^ 1], (phase >> (b ^ 1)) & 1u);
+            return;
+        }
+        const SegGeo s = seg_geo(g, seg, nzseg);
+        // Odd phase with walls along z: the halo element of an edge cell is its
+        // own slot i (half-way bounce-back).
+        if (ODD && !g.per[2] && t < 10 && (s.z0 == 0 || s.z0 + s.len == g.nz)) {
+            const int i = zdir(t);
+            const long long r = row_off(g, s, -cx(i), -cy(i));
+            if (r >= 0) {
+                if (cz(i) > 0 && s.z0 == 0) st.f[b][i][V - 1] = F[(size_t)i * N + s.own];
+                if (cz(i) < 0 && s.z0 + s.len == g.nz) st.f[b][i][V + s.len] = F[(size_t)i * N + s.own + g.nz - 1];
+            }
+        }
+        if (ODD && !g.per[2]) __syncthreads();
+
+        int key = -1;
+        T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+        if (t < s.len) {
+            const int z = s.z0 + t;
+            const size_t c = s.own + z;
+            // smem index of direction i for this thread: V + t - shift_i, where
+            // shift_i = c_z,i when the source row x - c_i exists (odd phase)
+            uint32_t srcrow = 0;   // bit i: source row of direction i lies inside the lattice
+            if (ODD) {
+#pragma unroll
+                for (int i = 1; i < Q; ++i)
+                    if (cz(i) != 0 && (cx(i) == 0 && cy(i) == 0 ? true : row_off(g, s, -cx(i), -cy(i)) >= 0))
+                        srcrow |= 1u << i;
+            }
+            auto at = [&](int i) -> const T& {
+                const int shift = (ODD && cz(i) != 0 && ((srcrow >> i) & 1u)) ? cz(i) : 0;
+                return st.f[b][i][V + t - shift];
+            };
+            T f[Q];
+#pragma unroll
+            for (int i = 0; i < Q; ++i) f[i] = at(i);
+            const uint32_t w = st.vox[b][t];
+            T Fx, Fy, Fz;
+            collide_cell<T, FORCE>(a, f, w, c, [&](int i) { return at(i); }, Fx, Fy, Fz);
+            if (!ODD) {
+#pragma unroll
+                for (int i = 0; i < Q; ++i) F[(size_t)opp(i) * N + c] = f[i];
+            } else {
+                F[c] = f[0];
+                const int zm = wrap_minus(z, g.nz, g.per[2]), zp = wrap_plus(z, g.nz, g.per[2]);
+#pragma unroll
+                for (int i = 1; i < Q; ++i) {
+                    const long long r = row_off(g, s, cx(i), cy(i));
+                    const int zd = pick(cz(i), zm, z, zp);
+                    if (r >= 0 && zd >= 0) F[(size_t)i * N + (size_t)r + zd] = f[i];
+                    else F[(size_t)opp(i) * N + c] = f[i];
+                }
+            }
+            if (a.cf) { a.cf[c] = Fx; a.cf[N + c] = Fy; a.cf[2 * N + c] = Fz; }
+            key = cell_force_terms(a, w, s.x, s.y, z, Fx, Fy, Fz, v);
+        }
+        reduce_forces(a, key, v);
+        __syncthreads();   // buffer b is free for the segment after next
+    }
+}
+
+template <typename T, bool ODD, bool FORCE>
+cudaError_t launch_direct(const CollideArgs<T>& a, cudaStream_t s) {
+    dim3 grid((unsigned)((size_t)a.g.nx * a.g.ny), (unsigned)((a.g.nz + COLLIDE_BLOCK - 1) / COLLIDE_BLOCK));
+    k_collide_direct<T, ODD, FORCE><<<grid, COLLIDE_BLOCK, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+template <typename T, bool ODD, bool FORCE>
+cudaError_t launch_staged(const CollideArgs<T>& a, cudaStream_t s) {
+    static int per_sm = 0, sms = 0;
+    if (per_sm == 0) {
+        int dev = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collide_staged<T, ODD, FORCE>, SEG, 0);
+        if (e != cudaSuccess) return e;
+        if (per_sm < 1) per_sm = 1;
+    }
+    const int nzseg = (a.g.nz + SEG - 1) / SEG;
+    const long long nseg = (long long)a.g.nx * a.g.ny * nzseg;
+    const long long want = (long long)sms * per_sm;
+    const unsigned grid = (unsigned)(nseg < want ? nseg : want);
+    k_collide_staged<T, ODD, FORCE><<<grid, SEG, 0, s>>>(a, nzseg, nseg);
+    return cudaGetLastError();
+}
+
 template <typename T, bool ODD, bool FORCE>
 cudaError_t launch_one(const CollideArgs<T>& a, cudaStream_t s) {
-    dim3 grid((unsigned)((size_t)a.g.nx * a.g.ny), (unsigned)((a.g.nz + COLLIDE_BLOCK - 1) / COLLIDE_BLOCK));
-    k_collide_stream<T, ODD, FORCE><<<grid, COLLIDE_BLOCK, 0, s>>>(a);
-    return cudaGetLastError();
+    // the staged copies need 16-byte aligned rows: nz * sizeof(T) % 16 == 0
+    if ((a.g.nz * sizeof(T)) % 16 == 0) return launch_staged<T, ODD, FORCE>(a, s);
+    return launch_direct<T, ODD, FORCE>(a, s);
 }
 
 }  // namespace

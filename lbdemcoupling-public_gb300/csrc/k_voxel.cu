@@ -3,27 +3,29 @@
 // Replaces setSpheresOnLattice -> SetSingleSphere3D::process for every sphere
 // (src/ibDataExchangeWrappers3D.hh:33-146, src/ibProcessors3D.hh:53-184).
 //
-// The reference applies spheres one after another, and each cell's new state
-// depends on its previous state and on the order of the spheres whose bounding
-// box covers it (decFlag, src/ibProcessors3D.hh:85-105).  The GPU version keeps
-// that order per cell: spheres are binned to 8^3-cell tiles, each tile's list
-// is sorted by sphere index in shared memory, and every cell folds the sorted
-// list through the same state machine.  Cells are independent, so the result
-// equals the sequential sweep exactly.
+// Order.  The reference applies spheres one after another, and a cell's new
+// state depends on its previous state and on the order of the spheres whose
+// bounding box covers it (decFlag, src/ibProcessors3D.hh:85-105).  The GPU
+// keeps that order per cell: every sphere is binned to the 8^3-cell tiles its
+// box overlaps, each tile's bin is sorted by sphere index in shared memory, and
+// every cell folds the sorted list through the same state machine.  Cells are
+// independent, so the result equals the sequential sweep.  A bin holds
+// TILE_BIN spheres; a tile overlapped by more re-collects its spheres by
+// testing every box (slow but exact).
 //
 // Exactness of the sub-cell count.  The reference decides, in IEEE double,
 //   dist = (dx^2 + dy^2) + dz^2  against (r + sqrt(3.1)/2)^2 and (r - sqrt(3.1)/2)^2,
 //   (xs_i + ys_j) + zs_k < r^2   for the 125 sub-cell centres of shell cells.
-// GB300 runs double arithmetic at a small fraction of its float rate, so every
-// comparison is first evaluated in float together with a proven error bound
-// (margin M = 2^-15 (r + 5)^2, at least 8x the worst-case float error for cells
-// inside the box [x - r - 3, x + r + 3] with |x| < 2^24).  A float result
-// farther than M from the threshold decides the comparison exactly as the
-// double computation would; only cells with a comparison inside the band are
-// recomputed with the reference's double sequence (__dadd_rn/__dmul_rn, no
-// fused multiply-add).  The counts n and owner tags are therefore identical to
-// the sequential CPU result, and the FP64 form also reproduces the particle
-// surface velocity bit for bit.
+// GB300 executes double arithmetic at two lanes per clock per SM, so each
+// comparison is first made in float with a margin M = 2^-18 (r + 4)^2.  For a
+// cell inside the box (|dx| < r + 3, centre split x = xh + xl with |x| < 2^24)
+// the float value differs from the double one by at most 27 u (r + 3.5)^2,
+// u = 2^-24 (sample sums), resp. 22 u (r + 3.2)^2 (dist), so a float result
+// farther than M from the threshold decides the comparison as the double
+// computation does.  Only comparisons inside the band are evaluated with the
+// reference's double sequence (__dadd_rn/__dmul_rn: no fused multiply-add).
+// Counts n and owner tags are identical to the sequential CPU result; the
+// FP64 form also reproduces the particle surface velocity bit for bit.
 #include "lbdem_internal.h"
 
 namespace lbdem {
@@ -34,35 +36,58 @@ constexpr double SQRT3HALF = 0.8803408430829505;  // sqrt(3.1)/2, src/ibProcesso
 __device__ __forceinline__ double sub_delta(int i) {
     return i == 0 ? -0.4 : i == 1 ? -0.19999999999999996 : i == 2 ? 0.0 : i == 3 ? 0.20000000000000007 : 0.4;
 }
-__device__ __forceinline__ float sub_delta_f(int i) { return (float)sub_delta(i); }
+__device__ __forceinline__ float sub_delta_f(int i) {
+    return i == 0 ? -0.4f : i == 1 ? -0.2f : i == 2 ? 0.0f : i == 3 ? 0.2f : 0.4f;
+}
 
-// calcSolidFraction in the reference's double sequence, as a count n in [0,125]
-// (sf = n/125 exactly; the early-outs return 0 and 1, i.e. n = 0 and n = 125).
-__device__ __noinline__ int solid_count_exact(double dx_, double dy_, double dz_, const SphereDev& s) {
-    const double dist = __dadd_rn(__dadd_rn(__dmul_rn(dx_, dx_), __dmul_rn(dy_, dy_)), __dmul_rn(dz_, dz_));
+// Region of a cell against the early-out thresholds in the reference's double
+// arithmetic: 0 outside (dist > rp2), 1 inside (dist < rm2), 2 shell.
+__device__ __noinline__ int region_exact(int X, int Y, int Z, const SphereDev& s) {
+    const double dx = __dsub_rn((double)X, s.x[0]);
+    const double dy = __dsub_rn((double)Y, s.x[1]);
+    const double dz = __dsub_rn((double)Z, s.x[2]);
+    const double dist = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
     if (dist > s.rp2) return 0;
-    if (dist < s.rm2) return 125;
+    if (dist < s.rm2) return 1;
+    return 2;
+}
+
+// Float sample count; the samples inside [rsq - M, rsq + M) are decided with
+// the reference's double sequence.
+__device__ __noinline__ int count_resolve(float dxf, float dyf, float dzf, float rsq, float M, int X, int Y, int Z,
+                                          const SphereDev& s) {
+    const double dx = __dsub_rn((double)X, s.x[0]);
+    const double dy = __dsub_rn((double)Y, s.x[1]);
+    const double dz = __dsub_rn((double)Z, s.x[2]);
     double xs[5], ys[5], zs[5];
+    float xf[5], yf[5], zf[5];
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
         const double d = sub_delta(i);
-        const double ax = __dadd_rn(dx_, d); xs[i] = __dmul_rn(ax, ax);
-        const double ay = __dadd_rn(dy_, d); ys[i] = __dmul_rn(ay, ay);
-        const double az = __dadd_rn(dz_, d); zs[i] = __dmul_rn(az, az);
+        const double ax = __dadd_rn(dx, d); xs[i] = __dmul_rn(ax, ax);
+        const double ay = __dadd_rn(dy, d); ys[i] = __dmul_rn(ay, ay);
+        const double az = __dadd_rn(dz, d); zs[i] = __dmul_rn(az, az);
+        const float e = sub_delta_f(i);
+        const float bx = dxf + e; xf[i] = bx * bx;
+        const float by = dyf + e; yf[i] = by * by;
+        const float bz = dzf + e; zf[i] = bz * bz;
     }
+    const float lo = rsq - M, hi = rsq + M;
     int n = 0;
     for (int i = 0; i < 5; ++i)
         for (int j = 0; j < 5; ++j) {
-            const double a = __dadd_rn(xs[i], ys[j]);
-#pragma unroll
-            for (int k = 0; k < 5; ++k) n += (__dadd_rn(a, zs[k]) < s.rsq) ? 1 : 0;
+            const float a = xf[i] + yf[j];
+            for (int k = 0; k < 5; ++k) {
+                const float t = a + zf[k];
+                if (t < lo) ++n;
+                else if (t < hi) n += (__dadd_rn(__dadd_rn(xs[i], ys[j]), zs[k]) < s.rsq) ? 1 : 0;
+            }
         }
     return n;
 }
 
-// Float evaluation of the sample count with the decision band; *unsure is set
-// when any of the 125 comparisons falls inside [rsq - M, rsq + M).
-__device__ __forceinline__ int solid_count_fast(float dxf, float dyf, float dzf, float rsq, float M, bool* unsure) {
+// Float sample count; *unsure is set when a sample falls inside the band.
+__device__ __forceinline__ int count_fast(float dxf, float dyf, float dzf, float rsq, float M, bool* unsure) {
     float xs[5], ys[5], zs[5];
 #pragma unroll
     for (int i = 0; i < 5; ++i) {
@@ -93,9 +118,9 @@ __device__ __forceinline__ int tiles_along(int n) { return (n + TILE - 1) / TILE
 
 // Per sphere: bounding box (double -> integer truncation toward zero,
 // src/ibProcessors3D.h:43-45) intersected with the lattice
-// (src/ibDataExchangeWrappers3D.hh:127-133), thresholds, the float split of the
-// centre, the tag -> lowest list index map (LAMMPS atom->map keeps the owned
-// atom) and the number of tiles the box overlaps.
+// (src/ibDataExchangeWrappers3D.hh:127-133), thresholds, the float split of
+// the centre, and the tag -> lowest list index map (LAMMPS atom->map keeps the
+// owned atom, which precedes its ghost images).
 __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereDev* __restrict__ sph,
                                   SphereFast* __restrict__ fast, float* __restrict__ xpf,
                                   int* __restrict__ tag2slot, unsigned* __restrict__ err, Geom g, int max_tag,
@@ -125,7 +150,7 @@ __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereD
         const double xd = s.x[d];
         q.xh[d] = 0.f; q.xl[d] = 0.f;
         // |x| < 2^24 keeps the integer conversions defined and the float split
-        // accurate; a sphere beyond cannot reach the lattice.
+        // accurate; a sphere farther out cannot reach the lattice.
         if (!(xd > -16777216.0 && xd < 16777216.0)) { s.valid = 0; s.lo[d] = 1; s.hi[d] = 0; continue; }
         q.xh[d] = (float)xd;
         q.xl[d] = (float)(xd - (double)q.xh[d]);
@@ -144,14 +169,16 @@ __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereD
     q.rp2 = (float)s.rp2;
     q.rm2 = (float)s.rm2;
     q.rsq = (float)s.rsq;
-    const float r5 = (float)s.r + 5.0f;
-    q.margin = ldexpf(r5 * r5, -15);
+    const float r4 = (float)s.r + 4.0f;
+    q.margin = ldexpf(r4 * r4, -18);
     for (int d = 0; d < 3; ++d) {
         q.lo[d] = s.valid ? s.lo[d] : 1;
         q.hi[d] = s.valid ? s.hi[d] : 0;
+        q.v[d] = (float)s.v[d];
+        q.w[d] = (float)s.w[d];
     }
     q.tag = s.tag;
-    for (int d = 0; d < 3; ++d) { q.v[d] = (float)s.v[d]; q.w[d] = (float)s.w[d]; }
+    q.pad = 0;
     sph[i] = s;
     fast[i] = q;
     float* xp = xpf + (size_t)i * 8;
@@ -160,12 +187,11 @@ __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereD
     if (s.tag >= 1) atomicMin(tag2slot + s.tag, i);
 }
 
-// One warp per sphere, lanes stride over the tiles its box overlaps.
-// COUNT: tile_count[t] += 1.  FILL: list[off[t] + cursor[t]++] = sphere.
-template <bool FILL>
-__global__ void k_pairs(const SphereFast* __restrict__ fast, int n, int* __restrict__ tile_count,
-                        const int* __restrict__ off, int* __restrict__ cursor, int* __restrict__ list,
-                        int pair_capacity, Geom g) {
+// One warp per sphere, lanes stride over the tiles its box overlaps and
+// append the sphere to each tile's bin (entries past TILE_BIN are dropped; the
+// voxelization of such a tile re-collects its spheres).
+__global__ void k_bin_spheres(const SphereFast* __restrict__ fast, int n, int* __restrict__ tile_cnt,
+                              int* __restrict__ bins, Geom g) {
     const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (i >= n) return;
@@ -179,48 +205,8 @@ __global__ void k_pairs(const SphereFast* __restrict__ fast, int n, int* __restr
         const int kz = k % ez, kr = k / ez;
         const int ky = kr % ey, kx = kr / ey;
         const size_t t = ((size_t)(tx0 + kx) * tny + (ty0 + ky)) * tnz + (tz0 + kz);
-        if (!FILL) {
-            atomicAdd(tile_count + t, 1);
-        } else {
-            const int pos = off[t] + atomicAdd(cursor + t, 1);
-            if (pos < pair_capacity) list[pos] = i;
-        }
-    }
-}
-
-// Exclusive scan of the tile counts (one block): tile_count[t] becomes the
-// offset of tile t's list, tile_count[ntiles] the total.  Also clears the fill
-// cursors.
-constexpr int SCAN_THREADS = 1024;
-__global__ void __launch_bounds__(SCAN_THREADS)
-k_scan_tiles(int* __restrict__ cnt, int ntiles, int pair_capacity, int* __restrict__ cursor,
-             unsigned* __restrict__ err) {
-    __shared__ long long s_sum[SCAN_THREADS];
-    const int t = threadIdx.x;
-    const int per = (ntiles + SCAN_THREADS - 1) / SCAN_THREADS;
-    const int beg = t * per;
-    const int end = min(beg + per, ntiles);
-    long long local = 0;
-    for (int k = beg; k < end; ++k) local += cnt[k];
-    s_sum[t] = local;
-    __syncthreads();
-    for (int off = 1; off < SCAN_THREADS; off <<= 1) {
-        long long add = t >= off ? s_sum[t - off] : 0;
-        __syncthreads();
-        s_sum[t] += add;
-        __syncthreads();
-    }
-    long long run = s_sum[t] - local;  // exclusive prefix
-    for (int k = beg; k < end; ++k) {
-        const int c = cnt[k];
-        cnt[k] = (int)(run < (long long)pair_capacity ? run : pair_capacity);
-        cursor[k] = 0;
-        run += c;
-    }
-    if (t == SCAN_THREADS - 1) {
-        const long long total = s_sum[t];
-        if (total > pair_capacity) atomicOr(err, 0x2u);  // LBDEM_DEVERR_PAIR_CAPACITY
-        cnt[ntiles] = (int)(total < (long long)pair_capacity ? total : pair_capacity);
+        const int pos = atomicAdd(tile_cnt + t, 1);
+        if (pos < TILE_BIN) bins[t * TILE_BIN + pos] = i;
     }
 }
 
@@ -256,21 +242,48 @@ __device__ __forceinline__ void surface_velocity(const SphereDev& s, int X, int 
 // (src/ibProcessors3D.hh:107-108); it depends only on that uPart, so the last
 // such sphere decides the populations written.
 template <typename T, bool INIT_VEL>
-__global__ void __launch_bounds__(TILE_CELLS)
-k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fast, const int* __restrict__ off,
-           const int* __restrict__ list, uint32_t* __restrict__ vox, T* __restrict__ up, T* __restrict__ f,
-           int phase, Geom g, unsigned* __restrict__ err) {
+__global__ void __launch_bounds__(TILE_CELLS, 1)
+k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fast, int nsph,
+           int* __restrict__ tile_cnt, const int* __restrict__ bins, uint32_t* __restrict__ vox, T* __restrict__ up,
+           T* __restrict__ f, int phase, Geom g, unsigned* __restrict__ err) {
     __shared__ int s_raw[TILE_LIST_MAX];
     __shared__ int s_sorted[TILE_LIST_MAX];
+    __shared__ SphereFast s_fast[TILE_STAGE];
+    __shared__ int s_cnt;
     const int t = blockIdx.x;
-    const int beg = off[t];
-    const int cnt = off[t + 1] - beg;
+    const int tny = tiles_along(g.ny), tnz = tiles_along(g.nz);
+    const int tx = t / (tny * tnz);
+    const int rem = t - tx * tny * tnz;
+    const int ty = rem / tnz;
+    const int tz = rem - ty * tnz;
+
+    int cnt = tile_cnt[t];
     if (cnt <= 0) return;
-    if (cnt > TILE_LIST_MAX) {
-        if (threadIdx.x == 0) atomicOr(err, 0x1u);  // LBDEM_DEVERR_TILE_LIST
-        return;
+    __syncthreads();
+    if (threadIdx.x == 0) tile_cnt[t] = 0;   // bins are reused by the next voxelization
+    if (cnt <= TILE_BIN) {
+        for (int k = threadIdx.x; k < cnt; k += blockDim.x) s_raw[k] = bins[(size_t)t * TILE_BIN + k];
+    } else {
+        // bin overflow: collect every sphere whose box overlaps this tile
+        if (threadIdx.x == 0) s_cnt = 0;
+        __syncthreads();
+        const int bx0 = tx * TILE, by0 = ty * TILE, bz0 = tz * TILE;
+        for (int i = threadIdx.x; i < nsph; i += blockDim.x) {
+            const SphereFast& q = fast[i];
+            if (q.lo[0] <= bx0 + TILE - 1 && q.hi[0] >= bx0 && q.lo[1] <= by0 + TILE - 1 && q.hi[1] >= by0 &&
+                q.lo[2] <= bz0 + TILE - 1 && q.hi[2] >= bz0 && q.lo[0] <= q.hi[0] && q.lo[1] <= q.hi[1] &&
+                q.lo[2] <= q.hi[2]) {
+                const int pos = atomicAdd(&s_cnt, 1);
+                if (pos < TILE_LIST_MAX) s_raw[pos] = i;
+            }
+        }
+        __syncthreads();
+        cnt = s_cnt;
+        if (cnt > TILE_LIST_MAX) {
+            if (threadIdx.x == 0) atomicOr(err, 0x1u);  // LBDEM_DEVERR_TILE_LIST
+            return;
+        }
     }
-    for (int k = threadIdx.x; k < cnt; k += blockDim.x) s_raw[k] = list[beg + k];
     __syncthreads();
     // rank sort by sphere index (the indices of one list are distinct)
     for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
@@ -280,12 +293,16 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
         s_sorted[rank] = vk;
     }
     __syncthreads();
+    const int staged = cnt < TILE_STAGE ? cnt : TILE_STAGE;
+    {
+        const int words = (int)(sizeof(SphereFast) / 4);
+        for (int k = threadIdx.x; k < staged * words; k += blockDim.x) {
+            const int e = k / words, wd = k - e * words;
+            reinterpret_cast<int*>(&s_fast[e])[wd] = reinterpret_cast<const int*>(&fast[s_sorted[e]])[wd];
+        }
+    }
+    __syncthreads();
 
-    const int tny = tiles_along(g.ny), tnz = tiles_along(g.nz);
-    const int tx = t / (tny * tnz);
-    const int rem = t - tx * tny * tnz;
-    const int ty = rem / tnz;
-    const int tz = rem - ty * tnz;
     const int lx = threadIdx.x >> 6, ly = (threadIdx.x >> 3) & 7, lz = threadIdx.x & 7;
     const int X = tx * TILE + lx, Y = ty * TILE + ly, Z = tz * TILE + lz;
     if (X >= g.nx || Y >= g.ny || Z >= g.nz) return;
@@ -302,24 +319,21 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
 
     for (int k = 0; k < cnt; ++k) {
         const int si = s_sorted[k];
-        const SphereFast& q = fast[si];
+        const SphereFast& q = k < TILE_STAGE ? s_fast[k] : fast[si];
         if (X < q.lo[0] || X > q.hi[0] || Y < q.lo[1] || Y > q.hi[1] || Z < q.lo[2] || Z > q.hi[2]) continue;
         const float dxf = (Xf - q.xh[0]) - q.xl[0];
         const float dyf = (Yf - q.xh[1]) - q.xl[1];
         const float dzf = (Zf - q.xh[2]) - q.xl[2];
         const float distf = (dxf * dxf + dyf * dyf) + dzf * dzf;
         const float M = q.margin;
-        int n;
-        bool exact = fabsf(distf - q.rp2) <= M || fabsf(distf - q.rm2) <= M;
-        if (!exact) {
-            if (distf > q.rp2) n = 0;
-            else if (distf < q.rm2) n = 125;
-            else n = solid_count_fast(dxf, dyf, dzf, q.rsq, M, &exact);
-        }
-        if (exact) {
-            const SphereDev& s = sph[si];
-            n = solid_count_exact(__dsub_rn((double)X, s.x[0]), __dsub_rn((double)Y, s.x[1]),
-                                  __dsub_rn((double)Z, s.x[2]), s);
+        int region;
+        if (fabsf(distf - q.rp2) <= M || fabsf(distf - q.rm2) <= M) region = region_exact(X, Y, Z, sph[si]);
+        else region = distf > q.rp2 ? 0 : (distf < q.rm2 ? 1 : 2);
+        int n = region == 1 ? 125 : 0;
+        if (region == 2) {
+            bool unsure;
+            n = count_fast(dxf, dyf, dzf, q.rsq, M, &unsure);
+            if (unsure) n = count_resolve(dxf, dyf, dzf, q.rsq, M, X, Y, Z, sph[si]);
         }
         // decFlag, src/ibProcessors3D.hh:85-105 (sf > 0.001 <=> n > 0; sf > sf_old <=> n > n_old)
         const int dec = (n > 0 ? 1 : 0) + (n_old > 0 ? 2 : 0);
@@ -371,40 +385,29 @@ cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, Sph
     return cudaGetLastError();
 }
 
-cudaError_t launch_count_pairs(const SphereFast* fast, int n, int* tile_count, Geom g, cudaStream_t s) {
+cudaError_t launch_bin_spheres(const SphereFast* fast, int n, int* tile_cnt, int* bins, Geom g, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_pairs<false><<<(n + 7) / 8, 256, 0, s>>>(fast, n, tile_count, nullptr, nullptr, nullptr, 0, g);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_scan_tiles(int* tile_count, int ntiles, int pair_capacity, int* cursor, unsigned* err,
-                              cudaStream_t s) {
-    k_scan_tiles<<<1, SCAN_THREADS, 0, s>>>(tile_count, ntiles, pair_capacity, cursor, err);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_fill_pairs(const SphereFast* fast, int n, const int* tile_off, int* cursor, int* list,
-                              int pair_capacity, Geom g, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    k_pairs<true><<<(n + 7) / 8, 256, 0, s>>>(fast, n, nullptr, tile_off, cursor, list, pair_capacity, g);
+    k_bin_spheres<<<(n + 7) / 8, 256, 0, s>>>(fast, n, tile_cnt, bins, g);
     return cudaGetLastError();
 }
 
 template <typename T>
-cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, const int* tile_off, const int* list,
+cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, int n, int* tile_cnt, const int* bins,
                             int ntiles, uint32_t* vox, T* up, T* f, int init_vel, int odd_phase, Geom g,
                             unsigned* err, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
     if (init_vel)
-        k_voxelize<T, true><<<ntiles, TILE_CELLS, 0, s>>>(sph, fast, tile_off, list, vox, up, f, odd_phase, g, err);
+        k_voxelize<T, true><<<ntiles, TILE_CELLS, 0, s>>>(sph, fast, n, tile_cnt, bins, vox, up, f, odd_phase, g,
+                                                          err);
     else
-        k_voxelize<T, false><<<ntiles, TILE_CELLS, 0, s>>>(sph, fast, tile_off, list, vox, up, f, odd_phase, g, err);
+        k_voxelize<T, false><<<ntiles, TILE_CELLS, 0, s>>>(sph, fast, n, tile_cnt, bins, vox, up, f, odd_phase, g,
+                                                           err);
     return cudaGetLastError();
 }
 
-template cudaError_t launch_voxelize<float>(const SphereDev*, const SphereFast*, const int*, const int*, int,
+template cudaError_t launch_voxelize<float>(const SphereDev*, const SphereFast*, int, int*, const int*, int,
                                             uint32_t*, float*, float*, int, int, Geom, unsigned*, cudaStream_t);
-template cudaError_t launch_voxelize<double>(const SphereDev*, const SphereFast*, const int*, const int*, int,
+template cudaError_t launch_voxelize<double>(const SphereDev*, const SphereFast*, int, int*, const int*, int,
                                              uint32_t*, double*, double*, int, int, Geom, unsigned*, cudaStream_t);
 
 }  // namespace lbdem

@@ -24,7 +24,8 @@ struct lbdem_handle {
     uint32_t* vox = nullptr;    // [N] n | tag << 7
     void* up = nullptr;         // [3][N]
     void* cf = nullptr;         // [3][N] optional
-    double* btab = nullptr;     // [126]
+    double* btab = nullptr;     // [126] B(n), double
+    float* btabf = nullptr;     // [126] B(n) rounded to float
 
     int cap = 0;
     double* d_rec = nullptr;    // [cap][12]
@@ -33,10 +34,8 @@ struct lbdem_handle {
     float* d_xpf = nullptr;     // [cap][8]
     int* d_tag2slot = nullptr;  // [max_tag + 1]
     int ntiles = 0;
-    int* d_tile_off = nullptr;  // [ntiles + 1]
-    int* d_cursor = nullptr;    // [ntiles]
-    int pair_cap = 0;
-    int* d_list = nullptr;      // [pair_cap]
+    int* d_tile_cnt = nullptr;  // [ntiles] spheres binned per tile (zero between calls)
+    int* d_bins = nullptr;      // [ntiles][TILE_BIN]
     double* d_ft = nullptr;     // [6][cap]
     unsigned* d_err = nullptr;
     double* d_mass = nullptr;
@@ -100,8 +99,8 @@ cudaError_t dalloc(lbdem_handle* h, P** p, size_t bytes) {
 }
 
 void release(lbdem_handle* h) {
-    void* dev[] = {h->f, h->vox, h->up, h->cf, h->btab, h->d_rec, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot,
-                   h->d_tile_off, h->d_cursor, h->d_list, h->d_ft, h->d_err, h->d_mass, h->scratch};
+    void* dev[] = {h->f, h->vox, h->up, h->cf, h->btab, h->btabf, h->d_rec, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot,
+                   h->d_tile_cnt, h->d_bins, h->d_ft, h->d_err, h->d_mass, h->scratch};
     for (void* p : dev)
         if (p) cudaFree(p);
     void* host[] = {h->h_rec, h->h_ft, h->h_err};
@@ -109,12 +108,6 @@ void release(lbdem_handle* h) {
         if (p) cudaFreeHost(p);
     if (h->ev_staged) cudaEventDestroy(h->ev_staged);
     if (h->own_stream) cudaStreamDestroy(h->own_stream);
-}
-
-int tiles_per_axis_bound(double max_radius) {
-    // cells covered per axis <= 2 r + 7 (box [x - r - 2, x + r + 2] plus truncation)
-    const int cells = (int)std::ceil(2.0 * max_radius + 7.0);
-    return (cells - 1) / TILE + 2;
 }
 
 lbdem_status ensure_scratch(lbdem_handle* h, size_t bytes) {
@@ -141,22 +134,19 @@ lbdem_status wait_staging(lbdem_handle* h) {
 // Voxelization of the particle table already in h->d_rec (n records).
 lbdem_status voxelize(lbdem_handle* h, int n, int init_vel) {
     cudaStream_t s = h->stream;
-    CK(h, cudaMemsetAsync(h->d_tile_off, 0, sizeof(int) * ((size_t)h->ntiles + 1), s));
     CK(h, cudaMemsetAsync(h->d_tag2slot, 0x7F, sizeof(int) * ((size_t)h->cfg.max_tag + 1), s));
     if (n > 0) {
         CK(h, launch_prepare_spheres(h->d_rec, n, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot, h->d_err, h->g,
                                      h->cfg.max_tag, h->cfg.max_radius, s));
-        CK(h, launch_count_pairs(h->d_fast, n, h->d_tile_off, h->g, s));
-        CK(h, launch_scan_tiles(h->d_tile_off, h->ntiles, h->pair_cap, h->d_cursor, h->d_err, s));
-        CK(h, launch_fill_pairs(h->d_fast, n, h->d_tile_off, h->d_cursor, h->d_list, h->pair_cap, h->g, s));
+        CK(h, launch_bin_spheres(h->d_fast, n, h->d_tile_cnt, h->d_bins, h->g, s));
         const int phase = (int)(h->step & 1);
         if (h->prec == LBDEM_PREC_FP64)
-            CK(h, launch_voxelize<double>(h->d_sph, h->d_fast, h->d_tile_off, h->d_list, h->ntiles, h->vox,
+            CK(h, launch_voxelize<double>(h->d_sph, h->d_fast, n, h->d_tile_cnt, h->d_bins, h->ntiles, h->vox,
                                           (double*)h->up, (double*)h->f, init_vel, phase, h->g, h->d_err, s));
         else
-            CK(h, launch_voxelize<float>(h->d_sph, h->d_fast, h->d_tile_off, h->d_list, h->ntiles, h->vox,
+            CK(h, launch_voxelize<float>(h->d_sph, h->d_fast, n, h->d_tile_cnt, h->d_bins, h->ntiles, h->vox,
                                          (float*)h->up, (float*)h->f, init_vel, phase, h->g, h->d_err, s));
-        h->launches += 5;
+        h->launches += 3;
     }
     h->n_cur = n;
     return LBDEM_OK;
@@ -234,11 +224,11 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     h->g.N = N;
     h->cap = c.max_particles;
     const int tnx = (c.nx + TILE - 1) / TILE, tny = (c.ny + TILE - 1) / TILE, tnz = (c.nz + TILE - 1) / TILE;
+    if ((long long)tnx * tny * tnz > 0x7fffffffLL) {
+        delete h;
+        return LBDEM_ERR_INVALID_ARG;
+    }
     h->ntiles = tnx * tny * tnz;
-    const long long tpa = tiles_per_axis_bound(c.max_radius);
-    long long pc = (long long)h->cap * tpa * tpa * tpa;
-    if (pc > 0x3fffffffLL) pc = 0x3fffffffLL;
-    h->pair_cap = (int)(pc > 0 ? pc : 1);
 
     DeviceGuard dg(h->device);
     auto bail = [&](lbdem_status s) {
@@ -260,15 +250,16 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     TRY(dalloc(h, &h->up, 3 * N * h->esz));
     if (c.flags & LBDEM_FLAG_CELL_FORCE) TRY(dalloc(h, &h->cf, 3 * N * h->esz));
     TRY(dalloc(h, &h->btab, 126 * sizeof(double)));
+    TRY(dalloc(h, &h->btabf, 126 * sizeof(float)));
     const size_t capn = (size_t)(h->cap > 0 ? h->cap : 1);
     TRY(dalloc(h, &h->d_rec, capn * REC_STRIDE * sizeof(double)));
     TRY(dalloc(h, &h->d_sph, capn * sizeof(SphereDev)));
     TRY(dalloc(h, &h->d_fast, capn * sizeof(SphereFast)));
     TRY(dalloc(h, &h->d_xpf, capn * 8 * sizeof(float)));
     TRY(dalloc(h, &h->d_tag2slot, ((size_t)c.max_tag + 1) * sizeof(int)));
-    TRY(dalloc(h, &h->d_tile_off, ((size_t)h->ntiles + 1) * sizeof(int)));
-    TRY(dalloc(h, &h->d_cursor, (size_t)h->ntiles * sizeof(int)));
-    TRY(dalloc(h, &h->d_list, (size_t)h->pair_cap * sizeof(int)));
+    TRY(dalloc(h, &h->d_tile_cnt, (size_t)h->ntiles * sizeof(int)));
+    TRY(dalloc(h, &h->d_bins, (size_t)h->ntiles * TILE_BIN * sizeof(int)));
+    TRY(cudaMemset(h->d_tile_cnt, 0, (size_t)h->ntiles * sizeof(int)));
     TRY(dalloc(h, &h->d_ft, 6 * capn * sizeof(double)));
     TRY(dalloc(h, &h->d_err, sizeof(unsigned)));
     TRY(dalloc(h, &h->d_mass, sizeof(double)));
@@ -287,6 +278,9 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     bt[0] = 0.0;
     bt[125] = 1.0;
     TRY(cudaMemcpy(h->btab, bt, sizeof(bt), cudaMemcpyHostToDevice));
+    float btf[126];
+    for (int n = 0; n < 126; ++n) btf[n] = (float)bt[n];
+    TRY(cudaMemcpy(h->btabf, btf, sizeof(btf), cudaMemcpyHostToDevice));
     TRY(cudaMemset(h->f, 0, (size_t)Q * N * h->esz));   // f̄ = 0: rho = 1, u = 0
     TRY(cudaMemset(h->vox, 0, N * sizeof(uint32_t)));
     TRY(cudaMemset(h->up, 0, 3 * N * h->esz));
@@ -416,8 +410,8 @@ lbdem_status lbdem_collide_and_stream(lbdem_handle* h) {
         CollideArgs<float> a;
         a.g = h->g; a.f = (float*)h->f; a.vox = h->vox; a.up = (const float*)h->up; a.cf = (float*)h->cf;
         a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.xpf = h->d_xpf; a.nslot = n; a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err;
-        a.btab = h->btab; a.omega = h->cfg.omega;
-        for (int d = 0; d < 3; ++d) a.g3[d] = h->cfg.body_force[d];
+        a.btab = h->btabf; a.omega = (float)h->cfg.omega;
+        for (int d = 0; d < 3; ++d) a.g3[d] = (float)h->cfg.body_force[d];
         CK(h, launch_collide_stream<float>(a, odd, force, h->stream));
     }
     h->launches += 1;

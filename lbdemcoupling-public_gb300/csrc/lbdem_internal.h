@@ -13,7 +13,9 @@ namespace lbdem {
 constexpr int Q = 19;
 constexpr int TILE = 8;                 // voxelization tile edge (cells)
 constexpr int TILE_CELLS = TILE * TILE * TILE;
-constexpr int TILE_LIST_MAX = 2048;     // spheres overlapping one tile, held in shared memory
+constexpr int TILE_BIN = 64;            // sphere slots per tile bin
+constexpr int TILE_LIST_MAX = 2048;     // spheres per tile when a bin overflows (shared memory)
+constexpr int TILE_STAGE = 64;          // sphere records staged in shared memory per tile
 constexpr int REC_STRIDE = 12;          // doubles per particle record {x3, v3, w3, r, tag, 0}
 constexpr int VOX_NBITS = 7;            // voxel word: sub-cell count n (7 bits) | tag << 7
 constexpr uint32_t VOX_NMASK = (1u << VOX_NBITS) - 1u;
@@ -59,9 +61,9 @@ struct CollideArgs {
     int max_tag;             // tag2slot has max_tag + 1 entries
     double* ft;              // [6][n]: F (3n) then T (3n)
     unsigned* err;
-    const double* btab;      // [126] B(n) = sf ooo / ((1 - sf) + ooo), double
-    double omega;
-    double g3[3];
+    const T* btab;           // [126] B(n) = sf ooo / ((1 - sf) + ooo), evaluated in double
+    T omega;                 // BGK relaxation frequency
+    T g3[3];                 // Guo body-force acceleration
 };
 
 // Exact (double) description of one sphere of the list, for the decisions
@@ -81,7 +83,9 @@ struct SphereFast {
     int lo[3], hi[3];        // empty box: lo > hi
     int tag;
     float v[3], w[3];        // velocity and angular velocity rounded to float
+    int pad;
 };
+static_assert(sizeof(SphereFast) == 96, "SphereFast is staged as 24 words");
 
 // Launchers (return cudaGetLastError() of the launch).
 template <typename T>
@@ -90,15 +94,12 @@ cudaError_t launch_collide_stream(const CollideArgs<T>& a, bool odd, bool force,
 cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
                                    int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
                                    cudaStream_t s);
-cudaError_t launch_count_pairs(const SphereFast* fast, int n, int* tile_count, Geom g, cudaStream_t s);
-cudaError_t launch_scan_tiles(int* tile_count, int ntiles, int pair_capacity, int* cursor,
-                              unsigned* err, cudaStream_t s);
-cudaError_t launch_fill_pairs(const SphereFast* fast, int n, const int* tile_off, int* cursor,
-                              int* list, int pair_capacity, Geom g, cudaStream_t s);
+// tile_cnt must be zero on entry; launch_voxelize leaves it zero again.
+cudaError_t launch_bin_spheres(const SphereFast* fast, int n, int* tile_cnt, int* bins, Geom g, cudaStream_t s);
 template <typename T>
-cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, const int* tile_off,
-                            const int* list, int ntiles, uint32_t* vox, T* up, T* f, int init_vel,
-                            int odd_phase, Geom g, unsigned* err, cudaStream_t s);
+cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, int n, int* tile_cnt, const int* bins,
+                            int ntiles, uint32_t* vox, T* up, T* f, int init_vel, int odd_phase, Geom g,
+                            unsigned* err, cudaStream_t s);
 
 // Field helpers.  phase: number of completed steps mod 2 (storage layout).
 template <typename T>

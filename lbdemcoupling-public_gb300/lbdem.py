@@ -36,7 +36,6 @@ FIELD_VELOCITY = 6
 FIELD_SUBCELL_COUNT = 7
 
 DEVERR_TILE_LIST = 0x1
-DEVERR_PAIR_CAPACITY = 0x2
 DEVERR_TAG_RANGE = 0x4
 DEVERR_UNMAPPED_TAG = 0x8
 DEVERR_RADIUS = 0x10

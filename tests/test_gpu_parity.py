@@ -22,6 +22,9 @@ CASES = {
     "channel_force": ((20, 24, 18), (1, 0, 1), 1 / 0.55, 4, 2.5, 4.5, False, (1e-5, 0.0, 2e-6)),
     "closed_box": ((16, 18, 40), (0, 0, 0), 1 / 0.6, 2, 4.0, 5.0, False, (0.0, 0.0, 0.0)),
     "tiny_radius": ((13, 11, 9), (1, 1, 1), 1.7, 5, 0.6, 1.6, True, (0.0, 0.0, 0.0)),
+    # z-rows longer than one 128-cell staged segment, last segment partial
+    "long_z_walls": ((6, 7, 200), (0, 1, 0), 1 / 0.6, 6, 1.5, 2.5, True, (0.0, 0.0, 1e-5)),
+    "long_z_periodic": ((5, 6, 264), (1, 1, 1), 1 / 0.55, 6, 1.5, 2.4, True, (0.0, 0.0, 0.0)),
 }
 
 
@@ -100,7 +103,7 @@ def test_fp64_parity(gpu, oracle, case):
     assert any(np.abs(r[2]).max() > 0 for r in res), "no force was exercised"
 
 
-@pytest.mark.parametrize("case", ["periodic_overlap", "channel_force"])
+@pytest.mark.parametrize("case", ["periodic_overlap", "channel_force", "long_z_walls", "long_z_periodic"])
 def test_fp32_dev_parity(gpu, oracle, case):
     res = _run(gpu, oracle, case, gpu.PREC_FP32_DEV, steps=6)
     for s, (fg, fo, Fg, Fo, Tg, To, ost, g, cfg) in enumerate(res):
