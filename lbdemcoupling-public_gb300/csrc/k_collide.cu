@@ -323,8 +323,12 @@ struct Stage {
     static constexpr int W = SEG + 2 * V;           // row: V halo | SEG core | V halo
     T f[2][Q][W];
     uint32_t vox[2][SEG];
+    long long row[2][9];   // element offset of row (x + dx, y + dy) at [3 (dx + 1) + dy + 1]; -1 beyond a wall
+    int geo[2][4];         // x, y, z0, len of the segment held in buffer b
     unsigned long long bar[2];
 };
+
+__device__ __forceinline__ constexpr int row_slot(int dx, int dy) { return 3 * (dx + 1) + dy + 1; }
 
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
@@ -409,6 +413,9 @@ __device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, Stage<T>&
     const Geom& g = a.g;
     const SegGeo s = seg_geo(g, seg, nzseg);
     const size_t N = g.N;
+    // segment geometry for the compute threads (read after the next barrier)
+    if (lane < 9) st.row[b][lane] = row_off(g, s, lane / 3 - 1, lane % 3 - 1);
+    if (lane == 9) { st.geo[b][0] = s.x; st.geo[b][1] = s.y; st.geo[b][2] = s.z0; st.geo[b][3] = s.len; }
     const T* src = nullptr;
     void* dst = nullptr;
     uint32_t bytes = 0;
@@ -484,32 +491,31 @@ k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
             if (next < nseg) mbar_wait(&st.bar[b ^ 1], (phase >> (b ^ 1)) & 1u);
             return;
         }
-        const SegGeo s = seg_geo(g, seg, nzseg);
+        const int sx = st.geo[b][0], sy = st.geo[b][1], z0 = st.geo[b][2], len = st.geo[b][3];
+        const size_t own = (size_t)st.row[b][row_slot(0, 0)];
         // Odd phase with walls along z: the halo element of an edge cell is its
         // own slot i (half-way bounce-back).
-        if (ODD && !g.per[2] && t < 10 && (s.z0 == 0 || s.z0 + s.len == g.nz)) {
+        if (ODD && !g.per[2] && t < 10 && (z0 == 0 || z0 + len == g.nz)) {
             const int i = zdir(t);
-            const long long r = row_off(g, s, -cx(i), -cy(i));
-            if (r >= 0) {
-                if (cz(i) > 0 && s.z0 == 0) st.f[b][i][V - 1] = F[(size_t)i * N + s.own];
-                if (cz(i) < 0 && s.z0 + s.len == g.nz) st.f[b][i][V + s.len] = F[(size_t)i * N + s.own + g.nz - 1];
+            if (st.row[b][row_slot(-cx(i), -cy(i))] >= 0) {
+                if (cz(i) > 0 && z0 == 0) st.f[b][i][V - 1] = F[(size_t)i * N + own];
+                if (cz(i) < 0 && z0 + len == g.nz) st.f[b][i][V + len] = F[(size_t)i * N + own + g.nz - 1];
             }
         }
         if (ODD && !g.per[2]) __syncthreads();
 
         int key = -1;
         T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-        if (t < s.len) {
-            const int z = s.z0 + t;
-            const size_t c = s.own + z;
+        if (t < len) {
+            const int z = z0 + t;
+            const size_t c = own + z;
             // smem index of direction i for this thread: V + t - shift_i, where
             // shift_i = c_z,i when the source row x - c_i exists (odd phase)
             uint32_t srcrow = 0;   // bit i: source row of direction i lies inside the lattice
             if (ODD) {
 #pragma unroll
                 for (int i = 1; i < Q; ++i)
-                    if (cz(i) != 0 && (cx(i) == 0 && cy(i) == 0 ? true : row_off(g, s, -cx(i), -cy(i)) >= 0))
-                        srcrow |= 1u << i;
+                    if (cz(i) != 0 && st.row[b][row_slot(-cx(i), -cy(i))] >= 0) srcrow |= 1u << i;
             }
             auto at = [&](int i) -> const T& {
                 const int shift = (ODD && cz(i) != 0 && ((srcrow >> i) & 1u)) ? cz(i) : 0;
@@ -529,14 +535,14 @@ k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
                 const int zm = wrap_minus(z, g.nz, g.per[2]), zp = wrap_plus(z, g.nz, g.per[2]);
 #pragma unroll
                 for (int i = 1; i < Q; ++i) {
-                    const long long r = row_off(g, s, cx(i), cy(i));
+                    const long long r = st.row[b][row_slot(cx(i), cy(i))];
                     const int zd = pick(cz(i), zm, z, zp);
                     if (r >= 0 && zd >= 0) F[(size_t)i * N + (size_t)r + zd] = f[i];
                     else F[(size_t)opp(i) * N + c] = f[i];
                 }
             }
             if (a.cf) { a.cf[c] = Fx; a.cf[N + c] = Fy; a.cf[2 * N + c] = Fz; }
-            key = cell_force_terms(a, w, s.x, s.y, z, Fx, Fy, Fz, v);
+            key = cell_force_terms(a, w, sx, sy, z, Fx, Fy, Fz, v);
         }
         reduce_forces(a, key, v);
         __syncthreads();   // buffer b is free for the segment after next
@@ -572,8 +578,9 @@ cudaError_t launch_staged(const CollideArgs<T>& a, cudaStream_t s) {
 
 template <typename T, bool ODD, bool FORCE>
 cudaError_t launch_one(const CollideArgs<T>& a, cudaStream_t s) {
-    // the staged copies need 16-byte aligned rows: nz * sizeof(T) % 16 == 0
-    if ((a.g.nz * sizeof(T)) % 16 == 0) return launch_staged<T, ODD, FORCE>(a, s);
+    // The staged bulk copies need every row start and length 16-byte aligned:
+    // population rows (nz * sizeof(T)) and voxel-word rows (nz * 4), i.e. nz % 4 == 0.
+    if (a.g.nz % 4 == 0) return launch_staged<T, ODD, FORCE>(a, s);
     return launch_direct<T, ODD, FORCE>(a, s);
 }
 
