@@ -118,10 +118,9 @@ __device__ __forceinline__ void bgk(T (&f)[Q], T omega, T gx, T gy, T gz) {
 // populations; pre(i) returns the same pre-collision value (fPre).  n == 125 is
 // the full-solid branch (no BGK, B = 1, which reduces the weighted update to
 // fPre + bb exactly).
-template <typename T, bool FORCE, typename Pre>
-__device__ __forceinline__ void psm(T (&f)[Q], int n, T up0, T up1, T up2, T B, T omega, T gx, T gy, T gz,
-                                    const Pre& pre, T& Fx, T& Fy, T& Fz) {
-    if (n < 125) bgk<T, FORCE>(f, omega, gx, gy, gz);
+template <typename T, typename Pre>
+__device__ __forceinline__ void psm(T (&f)[Q], T up0, T up1, T up2, T B, const Pre& pre, T& Fx, T& Fy, T& Fz) {
+    // on entry f holds the BGK post-collision state (or fPre itself for n == 125)
     T rhoBar, jx, jy, jz;
     moments(f, rhoBar, jx, jy, jz);                  // post-collision moments, :146-148
     const T rho = T(1) + rhoBar;
@@ -165,15 +164,28 @@ __device__ __forceinline__ void collide_cell(const CollideArgs<T>& a, T (&f)[Q],
                                              T& Fx, T& Fy, T& Fz) {
     const int n = min((int)(w & VOX_NMASK), 125);
     Fx = T(0); Fy = T(0); Fz = T(0);
-    if (n == 0) {
-        bgk<T, FORCE>(f, a.omega, a.g3[0], a.g3[1], a.g3[2]);
-    } else {
+    // BGK of the base dynamics for every cell below full coverage
+    // (src/ibCompositeDynamics3D.hh:139-140), then the solid correction.
+    // Written as two convergent blocks so that a warp mixing fluid and solid
+    // cells runs the BGK once.
+    if (n < 125) bgk<T, FORCE>(f, a.omega, a.g3[0], a.g3[1], a.g3[2]);
+    if (n > 0) {
         const size_t N = a.g.N;
         const T up0 = __ldg(a.up + c), up1 = __ldg(a.up + N + c), up2 = __ldg(a.up + 2 * N + c);
-        psm<T, FORCE>(f, n, up0, up1, up2, __ldg(a.btab + n), a.omega, a.g3[0], a.g3[1], a.g3[2], pre, Fx, Fy,
-                      Fz);
+        psm<T>(f, up0, up1, up2, __ldg(a.btab + n), pre, Fx, Fy, Fz);
     }
 }
+
+// float -> double by bit manipulation (exact for normal numbers; subnormal
+// floats become signed zero).  Keeps the conversion off GB300's narrow FP64 pipe.
+__device__ __forceinline__ double widen(float x) {
+    const uint32_t b = __float_as_uint(x);
+    const uint32_t s = b & 0x80000000u, e = (b >> 23) & 0xffu, m = b & 0x7fffffu;
+    if (e == 0) return __hiloint2double((int)s, 0);
+    const uint32_t ed = e == 0xffu ? 0x7ffu : e + 896u;   // rebias 127 -> 1023
+    return __hiloint2double((int)(s | (ed << 20) | (m >> 3)), (int)(m << 29));
+}
+__device__ __forceinline__ double widen(double x) { return x; }
 
 // Per-cell force and torque of a solid cell (SumForceTorque3D,
 // src/ibProcessors3D.hh:203-263): particle slot of the owner tag and the
@@ -238,8 +250,8 @@ __device__ __forceinline__ void reduce_forces(const CollideArgs<T>& a, int key, 
     if (tail && key >= 0) {
         double* Fp = a.ft + 3 * (size_t)key;
         double* Tp = a.ft + 3 * (size_t)a.nslot + 3 * (size_t)key;
-        atomicAdd(Fp + 0, (double)v[0]); atomicAdd(Fp + 1, (double)v[1]); atomicAdd(Fp + 2, (double)v[2]);
-        atomicAdd(Tp + 0, (double)v[3]); atomicAdd(Tp + 1, (double)v[4]); atomicAdd(Tp + 2, (double)v[5]);
+        atomicAdd(Fp + 0, widen(v[0])); atomicAdd(Fp + 1, widen(v[1])); atomicAdd(Fp + 2, widen(v[2]));
+        atomicAdd(Tp + 0, widen(v[3])); atomicAdd(Tp + 1, widen(v[4])); atomicAdd(Tp + 2, widen(v[5]));
     }
 }
 
@@ -313,16 +325,19 @@ k_collide_direct(const CollideArgs<T> a) {
 }
 
 // ---------------------------------------------------------------------------
-// Staged persistent kernel.
-constexpr int SEG = COLLIDE_BLOCK;          // cells per z-segment = threads per CTA
+// Staged persistent kernel: every warp runs its own double-buffered pipeline
+// over SEGW-cell z-segments (no block-wide barriers, so a warp with solid
+// cells does not hold up the others).
+constexpr int WARPS = COLLIDE_BLOCK / 32;    // warps per CTA
+constexpr int SEGW = 64;                    // cells per warp segment (2 per lane)
 constexpr int WAIT_LIMIT = 1 << 22;         // bounded mbarrier wait (iterations of try_wait)
 
 template <typename T>
-struct Stage {
+struct WarpStage {
     static constexpr int V = 16 / (int)sizeof(T);   // elements per 16 bytes
-    static constexpr int W = SEG + 2 * V;           // row: V halo | SEG core | V halo
+    static constexpr int W = SEGW + 2 * V;          // row: V halo | SEGW core | V halo
     T f[2][Q][W];
-    uint32_t vox[2][SEG];
+    uint32_t vox[2][SEGW];
     long long row[2][9];   // element offset of row (x + dx, y + dy) at [3 (dx + 1) + dy + 1]; -1 beyond a wall
     int geo[2][4];         // x, y, z0, len of the segment held in buffer b
     unsigned long long bar[2];
@@ -375,7 +390,6 @@ __device__ __forceinline__ int zdir(int k) {
 struct SegGeo {
     int x, y, z0, len;
     int xm, xp, ym, yp;     // neighbour rows along x and y (-1: beyond a wall)
-    size_t own;             // element offset of the own row (x, y, 0)
 };
 
 __device__ __forceinline__ SegGeo seg_geo(const Geom& g, long long seg, int nzseg) {
@@ -384,11 +398,10 @@ __device__ __forceinline__ SegGeo seg_geo(const Geom& g, long long seg, int nzse
     const int zs = (int)(seg - row * nzseg);
     s.x = (int)(row / g.ny);
     s.y = (int)(row - (long long)s.x * g.ny);
-    s.z0 = zs * SEG;
-    s.len = min(SEG, g.nz - s.z0);
+    s.z0 = zs * SEGW;
+    s.len = min(SEGW, g.nz - s.z0);
     s.xm = wrap_minus(s.x, g.nx, g.per[0]); s.xp = wrap_plus(s.x, g.nx, g.per[0]);
     s.ym = wrap_minus(s.y, g.ny, g.per[1]); s.yp = wrap_plus(s.y, g.ny, g.per[1]);
-    s.own = ((size_t)s.x * g.ny + s.y) * g.nz;
     return s;
 }
 
@@ -399,21 +412,22 @@ __device__ __forceinline__ long long row_off(const Geom& g, const SegGeo& s, int
     return ((long long)X * g.ny + Y) * g.nz;
 }
 
-// Issued by one warp: the segment's copies into buffer b.
-//   copies 0..18: population rows (even: own row, slot i; odd: row x - c_i,
+// Issued by one warp for its segment into buffer b:
+//   lanes 0..18:  population rows (even: own row, slot i; odd: row x - c_i,
 //                 slot opp i, or own row slot i when that row is beyond a wall);
-//   copies 19..28 (odd, periodic z): the 16-byte chunk holding the halo element
-//                 of the k-th c_z != 0 direction;
-//   copy 29: voxel words of the segment.
+//   lanes 19..28: odd phase, the 16-byte chunk holding the halo element of the
+//                 (lane-19)-th c_z != 0 direction (none beyond a z wall);
+//   lane 29:      voxel words of the segment.
+// Lanes 0..9 also publish the segment geometry for the compute pass.
 template <typename T, bool ODD>
-__device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, Stage<T>& st, int b, long long seg,
+__device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, WarpStage<T>& st, int b, long long seg,
                                               int nzseg) {
-    constexpr int V = Stage<T>::V;
+    constexpr int V = WarpStage<T>::V;
     const int lane = threadIdx.x & 31;
     const Geom& g = a.g;
     const SegGeo s = seg_geo(g, seg, nzseg);
     const size_t N = g.N;
-    // segment geometry for the compute threads (read after the next barrier)
+    const long long own = ((long long)s.x * g.ny + s.y) * g.nz;
     if (lane < 9) st.row[b][lane] = row_off(g, s, lane / 3 - 1, lane % 3 - 1);
     if (lane == 9) { st.geo[b][0] = s.x; st.geo[b][1] = s.y; st.geo[b][2] = s.z0; st.geo[b][3] = s.len; }
     const T* src = nullptr;
@@ -421,7 +435,7 @@ __device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, Stage<T>&
     uint32_t bytes = 0;
     if (lane < Q) {
         const int i = lane;
-        size_t off = (size_t)i * N + s.own + s.z0;
+        size_t off = (size_t)i * N + (size_t)own + s.z0;
         if (ODD && i != 0) {
             const long long r = row_off(g, s, -cx(i), -cy(i));
             if (r >= 0) off = (size_t)opp(i) * N + (size_t)r + s.z0;
@@ -449,7 +463,7 @@ __device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, Stage<T>&
             }
         }
     } else if (lane == Q + 10) {
-        src = reinterpret_cast<const T*>(a.vox + s.own + s.z0);
+        src = reinterpret_cast<const T*>(a.vox + own + s.z0);
         dst = &st.vox[b][0];
         bytes = (uint32_t)(s.len * sizeof(uint32_t));
     }
@@ -460,34 +474,36 @@ __device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, Stage<T>&
 }
 
 template <typename T, bool ODD, bool FORCE>
-__global__ void __launch_bounds__(SEG)
+__global__ void __launch_bounds__(COLLIDE_BLOCK)
 k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
-    constexpr int V = Stage<T>::V;
-    __shared__ __align__(16) Stage<T> st;
+    constexpr int V = WarpStage<T>::V;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int lane = threadIdx.x & 31;
+    const int warp = threadIdx.x >> 5;
+    WarpStage<T>& st = reinterpret_cast<WarpStage<T>*>(smem_raw)[warp];
     const Geom& g = a.g;
     const size_t N = g.N;
-    const int t = threadIdx.x;
-    const int warp = t >> 5;
     T* __restrict__ F = a.f;
-    if (t == 0) {
+    if (lane == 0) {
         mbar_init(&st.bar[0], 1);
         mbar_init(&st.bar[1], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    __syncthreads();
-    long long seg = blockIdx.x;
+    __syncwarp();
+    const long long stride = (long long)gridDim.x * WARPS;
+    long long seg = (long long)blockIdx.x * WARPS + warp;
     if (seg >= nseg) return;
-    if (warp == 0) issue_segment<T, ODD>(a, st, 0, seg, nzseg);
+    issue_segment<T, ODD>(a, st, 0, seg, nzseg);
     uint32_t phase = 0;   // bit b: parity expected next on buffer b
     int b = 0;
-    for (; seg < nseg; seg += gridDim.x, b ^= 1) {
-        const long long next = seg + gridDim.x;
-        if (next < nseg && warp == 0) issue_segment<T, ODD>(a, st, b ^ 1, next, nzseg);
+    for (; seg < nseg; seg += stride, b ^= 1) {
+        const long long next = seg + stride;
+        if (next < nseg) issue_segment<T, ODD>(a, st, b ^ 1, next, nzseg);
         const bool ok = mbar_wait(&st.bar[b], (phase >> b) & 1u);
         phase ^= 1u << b;
-        if (__syncthreads_or(!ok)) {
+        if (__any_sync(FULL, !ok)) {
             // a copy did not land: report, let in-flight copies finish, leave
-            if (t == 0) atomicOr(a.err, 0x20u);   // LBDEM_DEVERR_TIMEOUT
+            if (lane == 0) atomicOr(a.err, 0x20u);   // LBDEM_DEVERR_TIMEOUT
             if (next < nseg) mbar_wait(&st.bar[b ^ 1], (phase >> (b ^ 1)) & 1u);
             return;
         }
@@ -495,57 +511,61 @@ k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
         const size_t own = (size_t)st.row[b][row_slot(0, 0)];
         // Odd phase with walls along z: the halo element of an edge cell is its
         // own slot i (half-way bounce-back).
-        if (ODD && !g.per[2] && t < 10 && (z0 == 0 || z0 + len == g.nz)) {
-            const int i = zdir(t);
-            if (st.row[b][row_slot(-cx(i), -cy(i))] >= 0) {
-                if (cz(i) > 0 && z0 == 0) st.f[b][i][V - 1] = F[(size_t)i * N + own];
-                if (cz(i) < 0 && z0 + len == g.nz) st.f[b][i][V + len] = F[(size_t)i * N + own + g.nz - 1];
-            }
-        }
-        if (ODD && !g.per[2]) __syncthreads();
-
-        int key = -1;
-        T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-        if (t < len) {
-            const int z = z0 + t;
-            const size_t c = own + z;
-            // smem index of direction i for this thread: V + t - shift_i, where
-            // shift_i = c_z,i when the source row x - c_i exists (odd phase)
-            uint32_t srcrow = 0;   // bit i: source row of direction i lies inside the lattice
-            if (ODD) {
-#pragma unroll
-                for (int i = 1; i < Q; ++i)
-                    if (cz(i) != 0 && st.row[b][row_slot(-cx(i), -cy(i))] >= 0) srcrow |= 1u << i;
-            }
-            auto at = [&](int i) -> const T& {
-                const int shift = (ODD && cz(i) != 0 && ((srcrow >> i) & 1u)) ? cz(i) : 0;
-                return st.f[b][i][V + t - shift];
-            };
-            T f[Q];
-#pragma unroll
-            for (int i = 0; i < Q; ++i) f[i] = at(i);
-            const uint32_t w = st.vox[b][t];
-            T Fx, Fy, Fz;
-            collide_cell<T, FORCE>(a, f, w, c, [&](int i) { return at(i); }, Fx, Fy, Fz);
-            if (!ODD) {
-#pragma unroll
-                for (int i = 0; i < Q; ++i) F[(size_t)opp(i) * N + c] = f[i];
-            } else {
-                F[c] = f[0];
-                const int zm = wrap_minus(z, g.nz, g.per[2]), zp = wrap_plus(z, g.nz, g.per[2]);
-#pragma unroll
-                for (int i = 1; i < Q; ++i) {
-                    const long long r = st.row[b][row_slot(cx(i), cy(i))];
-                    const int zd = pick(cz(i), zm, z, zp);
-                    if (r >= 0 && zd >= 0) F[(size_t)i * N + (size_t)r + zd] = f[i];
-                    else F[(size_t)opp(i) * N + c] = f[i];
+        if (ODD && !g.per[2] && (z0 == 0 || z0 + len == g.nz)) {
+            if (lane < 10) {
+                const int i = zdir(lane);
+                if (st.row[b][row_slot(-cx(i), -cy(i))] >= 0) {
+                    if (cz(i) > 0 && z0 == 0) st.f[b][i][V - 1] = F[(size_t)i * N + own];
+                    if (cz(i) < 0 && z0 + len == g.nz) st.f[b][i][V + len] = F[(size_t)i * N + own + g.nz - 1];
                 }
             }
-            if (a.cf) { a.cf[c] = Fx; a.cf[N + c] = Fy; a.cf[2 * N + c] = Fz; }
-            key = cell_force_terms(a, w, sx, sy, z, Fx, Fy, Fz, v);
+            __syncwarp();
         }
-        reduce_forces(a, key, v);
-        __syncthreads();   // buffer b is free for the segment after next
+        uint32_t srcrow = 0;   // bit i: source row of direction i lies inside the lattice
+        if (ODD) {
+#pragma unroll
+            for (int i = 1; i < Q; ++i)
+                if (cz(i) != 0 && st.row[b][row_slot(-cx(i), -cy(i))] >= 0) srcrow |= 1u << i;
+        }
+#pragma unroll 1
+        for (int j = lane; j < SEGW; j += 32) {
+            int key = -1;
+            T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+            if (j < len) {
+                const int z = z0 + j;
+                const size_t c = own + z;
+                // smem index of direction i: V + j - shift_i, shift_i = c_z,i when
+                // the source row x - c_i exists (odd phase)
+                auto at = [&](int i) -> const T& {
+                    const int shift = (ODD && cz(i) != 0 && ((srcrow >> i) & 1u)) ? cz(i) : 0;
+                    return st.f[b][i][V + j - shift];
+                };
+                T f[Q];
+#pragma unroll
+                for (int i = 0; i < Q; ++i) f[i] = at(i);
+                const uint32_t w = st.vox[b][j];
+                T Fx, Fy, Fz;
+                collide_cell<T, FORCE>(a, f, w, c, [&](int i) { return at(i); }, Fx, Fy, Fz);
+                if (!ODD) {
+#pragma unroll
+                    for (int i = 0; i < Q; ++i) F[(size_t)opp(i) * N + c] = f[i];
+                } else {
+                    F[c] = f[0];
+                    const int zm = wrap_minus(z, g.nz, g.per[2]), zp = wrap_plus(z, g.nz, g.per[2]);
+#pragma unroll
+                    for (int i = 1; i < Q; ++i) {
+                        const long long r = st.row[b][row_slot(cx(i), cy(i))];
+                        const int zd = pick(cz(i), zm, z, zp);
+                        if (r >= 0 && zd >= 0) F[(size_t)i * N + (size_t)r + zd] = f[i];
+                        else F[(size_t)opp(i) * N + c] = f[i];
+                    }
+                }
+                if (a.cf) { a.cf[c] = Fx; a.cf[N + c] = Fy; a.cf[2 * N + c] = Fz; }
+                key = cell_force_terms(a, w, sx, sy, z, Fx, Fy, Fz, v);
+            }
+            reduce_forces(a, key, v);
+        }
+        __syncwarp();   // buffer b is free for the segment after next
     }
 }
 
@@ -558,21 +578,27 @@ cudaError_t launch_direct(const CollideArgs<T>& a, cudaStream_t s) {
 
 template <typename T, bool ODD, bool FORCE>
 cudaError_t launch_staged(const CollideArgs<T>& a, cudaStream_t s) {
+    constexpr size_t smem = WARPS * sizeof(WarpStage<T>);
     static int per_sm = 0, sms = 0;
     if (per_sm == 0) {
         int dev = 0;
         cudaError_t e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collide_staged<T, ODD, FORCE>, SEG, 0);
+            e = cudaFuncSetAttribute(k_collide_staged<T, ODD, FORCE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collide_staged<T, ODD, FORCE>,
+                                                              COLLIDE_BLOCK, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
-    const int nzseg = (a.g.nz + SEG - 1) / SEG;
+    const int nzseg = (a.g.nz + SEGW - 1) / SEGW;
     const long long nseg = (long long)a.g.nx * a.g.ny * nzseg;
     const long long want = (long long)sms * per_sm;
-    const unsigned grid = (unsigned)(nseg < want ? nseg : want);
-    k_collide_staged<T, ODD, FORCE><<<grid, SEG, 0, s>>>(a, nzseg, nseg);
+    const long long blocks = (nseg + WARPS - 1) / WARPS;
+    const unsigned grid = (unsigned)(blocks < want ? blocks : want);
+    k_collide_staged<T, ODD, FORCE><<<grid, COLLIDE_BLOCK, smem, s>>>(a, nzseg, nseg);
     return cudaGetLastError();
 }
 
