@@ -236,20 +236,52 @@ __device__ __forceinline__ void surface_velocity(const SphereDev& s, int X, int 
     u2 = __dadd_rn(s.v[2], __dsub_rn(__dmul_rn(s.w[0], dy), __dmul_rn(s.w[1], dx)));
 }
 
-// One block per tile; 512 threads, one per cell of the 8^3 tile.
+// Shared memory of one voxelization block.
+constexpr int VOX_THREADS = 256;            // two cells of the 8^3 tile per thread
+constexpr int VOX_CHUNK = 64;               // spheres classified per pass
+constexpr int VOX_QUEUE = 4096;             // shell (sphere, cell) pairs counted per pass
+constexpr uint8_t N_NONE = 255;             // cell outside the sphere's box
+constexpr uint8_t N_PENDING = 254;          // shell cell whose count is queued
+
+struct VoxSmem {
+    int raw[TILE_LIST_MAX];
+    int sorted[TILE_LIST_MAX];
+    SphereFast q[VOX_CHUNK];
+    uint8_t n[VOX_CHUNK][TILE_CELLS];       // sub-cell count of (sphere k, cell)
+    uint16_t queue[VOX_QUEUE];              // (k << 9) | cell
+    int qcount;
+    int cnt;
+};
+
+// Sub-cell count of a shell cell (float filter, exact where unsure).
+__device__ __forceinline__ int shell_count(const SphereFast& q, const SphereDev& s, int X, int Y, int Z) {
+    const float dxf = ((float)X - q.xh[0]) - q.xl[0];
+    const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
+    const float dzf = ((float)Z - q.xh[2]) - q.xl[2];
+    bool unsure;
+    int n = count_fast(dxf, dyf, dzf, q.rsq, q.margin, &unsure);
+    if (unsure) n = count_resolve(dxf, dyf, dzf, q.rsq, q.margin, X, Y, Z, s);
+    return n;
+}
+
+// One block per 8^3 tile, 256 threads, two cells per thread.  Spheres are taken
+// in sorted chunks of VOX_CHUNK; each chunk runs three phases:
+//  A  classify every (sphere, cell) pair in float: outside the box, outside
+//     (n = 0) and inside (n = 125) are final, shell cells are queued;
+//  B  all threads drain the queue, so the 125-sample counts run at full width;
+//  C  every cell folds the chunk's counts, in sphere order, through decFlag.
 // INIT_VEL: defineVelocity (src/ibCompositeDynamics3D.hh:118-127) is applied
 // with the uPart the cell holds right after each sphere that covers it fully
 // (src/ibProcessors3D.hh:107-108); it depends only on that uPart, so the last
 // such sphere decides the populations written.
 template <typename T, bool INIT_VEL>
-__global__ void __launch_bounds__(TILE_CELLS, 1)
+__global__ void __launch_bounds__(VOX_THREADS, 2)
 k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fast, int nsph,
            int* __restrict__ tile_cnt, const int* __restrict__ bins, uint32_t* __restrict__ vox, T* __restrict__ up,
            T* __restrict__ f, int phase, Geom g, unsigned* __restrict__ err) {
-    __shared__ int s_raw[TILE_LIST_MAX];
-    __shared__ int s_sorted[TILE_LIST_MAX];
-    __shared__ SphereFast s_fast[TILE_STAGE];
-    __shared__ int s_cnt;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    VoxSmem& S = *reinterpret_cast<VoxSmem*>(smem_raw);
+    const int tid = threadIdx.x;
     const int t = blockIdx.x;
     const int tny = tiles_along(g.ny), tnz = tiles_along(g.nz);
     const int tx = t / (tny * tnz);
@@ -260,116 +292,171 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
     int cnt = tile_cnt[t];
     if (cnt <= 0) return;
     __syncthreads();
-    if (threadIdx.x == 0) tile_cnt[t] = 0;   // bins are reused by the next voxelization
+    if (tid == 0) tile_cnt[t] = 0;   // bins are reused by the next voxelization
     if (cnt <= TILE_BIN) {
-        for (int k = threadIdx.x; k < cnt; k += blockDim.x) s_raw[k] = bins[(size_t)t * TILE_BIN + k];
+        for (int k = tid; k < cnt; k += VOX_THREADS) S.raw[k] = bins[(size_t)t * TILE_BIN + k];
     } else {
         // bin overflow: collect every sphere whose box overlaps this tile
-        if (threadIdx.x == 0) s_cnt = 0;
+        if (tid == 0) S.cnt = 0;
         __syncthreads();
         const int bx0 = tx * TILE, by0 = ty * TILE, bz0 = tz * TILE;
-        for (int i = threadIdx.x; i < nsph; i += blockDim.x) {
+        for (int i = tid; i < nsph; i += VOX_THREADS) {
             const SphereFast& q = fast[i];
             if (q.lo[0] <= bx0 + TILE - 1 && q.hi[0] >= bx0 && q.lo[1] <= by0 + TILE - 1 && q.hi[1] >= by0 &&
                 q.lo[2] <= bz0 + TILE - 1 && q.hi[2] >= bz0 && q.lo[0] <= q.hi[0] && q.lo[1] <= q.hi[1] &&
                 q.lo[2] <= q.hi[2]) {
-                const int pos = atomicAdd(&s_cnt, 1);
-                if (pos < TILE_LIST_MAX) s_raw[pos] = i;
+                const int pos = atomicAdd(&S.cnt, 1);
+                if (pos < TILE_LIST_MAX) S.raw[pos] = i;
             }
         }
         __syncthreads();
-        cnt = s_cnt;
+        cnt = S.cnt;
         if (cnt > TILE_LIST_MAX) {
-            if (threadIdx.x == 0) atomicOr(err, 0x1u);  // LBDEM_DEVERR_TILE_LIST
+            if (tid == 0) atomicOr(err, 0x1u);  // LBDEM_DEVERR_TILE_LIST
             return;
         }
     }
     __syncthreads();
     // rank sort by sphere index (the indices of one list are distinct)
-    for (int k = threadIdx.x; k < cnt; k += blockDim.x) {
-        const int vk = s_raw[k];
+    for (int k = tid; k < cnt; k += VOX_THREADS) {
+        const int vk = S.raw[k];
         int rank = 0;
-        for (int m = 0; m < cnt; ++m) rank += (s_raw[m] < vk) ? 1 : 0;
-        s_sorted[rank] = vk;
+        for (int m = 0; m < cnt; ++m) rank += (S.raw[m] < vk) ? 1 : 0;
+        S.sorted[rank] = vk;
     }
-    __syncthreads();
-    const int staged = cnt < TILE_STAGE ? cnt : TILE_STAGE;
-    {
-        const int words = (int)(sizeof(SphereFast) / 4);
-        for (int k = threadIdx.x; k < staged * words; k += blockDim.x) {
-            const int e = k / words, wd = k - e * words;
-            reinterpret_cast<int*>(&s_fast[e])[wd] = reinterpret_cast<const int*>(&fast[s_sorted[e]])[wd];
-        }
-    }
-    __syncthreads();
 
-    const int lx = threadIdx.x >> 6, ly = (threadIdx.x >> 3) & 7, lz = threadIdx.x & 7;
-    const int X = tx * TILE + lx, Y = ty * TILE + ly, Z = tz * TILE + lz;
-    if (X >= g.nx || Y >= g.ny || Z >= g.nz) return;
-    const size_t c = ((size_t)X * g.ny + Y) * g.nz + Z;
-
-    const uint32_t w0 = vox[c];
-    int n_old = (int)(w0 & VOX_NMASK);
-    int id_old = (int)(w0 >> VOX_NBITS);
-    T u0 = T(0), u1 = T(0), u2 = T(0);
-    if (n_old > 0) { u0 = up[c]; u1 = up[g.N + c]; u2 = up[2 * g.N + c]; }
-    bool dirty = false, define_vel = false;
-    T d0 = T(0), d1 = T(0), d2 = T(0);
-    const float Xf = (float)X, Yf = (float)Y, Zf = (float)Z;
-
-    for (int k = 0; k < cnt; ++k) {
-        const int si = s_sorted[k];
-        const SphereFast& q = k < TILE_STAGE ? s_fast[k] : fast[si];
-        if (X < q.lo[0] || X > q.hi[0] || Y < q.lo[1] || Y > q.hi[1] || Z < q.lo[2] || Z > q.hi[2]) continue;
-        const float dxf = (Xf - q.xh[0]) - q.xl[0];
-        const float dyf = (Yf - q.xh[1]) - q.xl[1];
-        const float dzf = (Zf - q.xh[2]) - q.xl[2];
-        const float distf = (dxf * dxf + dyf * dyf) + dzf * dzf;
-        const float M = q.margin;
-        int region;
-        if (fabsf(distf - q.rp2) <= M || fabsf(distf - q.rm2) <= M) region = region_exact(X, Y, Z, sph[si]);
-        else region = distf > q.rp2 ? 0 : (distf < q.rm2 ? 1 : 2);
-        int n = region == 1 ? 125 : 0;
-        if (region == 2) {
-            bool unsure;
-            n = count_fast(dxf, dyf, dzf, q.rsq, M, &unsure);
-            if (unsure) n = count_resolve(dxf, dyf, dzf, q.rsq, M, X, Y, Z, sph[si]);
-        }
-        // decFlag, src/ibProcessors3D.hh:85-105 (sf > 0.001 <=> n > 0; sf > sf_old <=> n > n_old)
-        const int dec = (n > 0 ? 1 : 0) + (n_old > 0 ? 2 : 0);
-        bool set = false, zero = false;
-        if (dec == 1) set = true;
-        else if (dec == 2) zero = (id_old == q.tag);
-        else if (dec == 3) set = (n > n_old) || (id_old == q.tag);
-        // dec == 0 is setToZero on a cell that is already empty
-        if (zero) {
-            n_old = 0; id_old = 0; u0 = u1 = u2 = T(0); dirty = true;
-        } else if (set) {
-            if (sizeof(T) == 8) {
-                double a0, a1, a2;
-                surface_velocity(sph[si], X, Y, Z, a0, a1, a2);
-                u0 = T(a0); u1 = T(a1); u2 = T(a2);
-            } else {
-                u0 = T(q.v[0] + (q.w[1] * dzf - q.w[2] * dyf));
-                u1 = T(q.v[1] + (-q.w[0] * dzf + q.w[2] * dxf));
-                u2 = T(q.v[2] + (q.w[0] * dyf - q.w[1] * dxf));
-            }
-            n_old = n; id_old = q.tag; dirty = true;
-        }
-        if (INIT_VEL && n == 125) { define_vel = true; d0 = u0; d1 = u1; d2 = u2; }
-    }
-    if (dirty) {
-        vox[c] = (uint32_t)n_old | ((uint32_t)id_old << VOX_NBITS);
-        up[c] = u0; up[g.N + c] = u1; up[2 * g.N + c] = u2;
-    }
-    if (INIT_VEL && define_vel) {
-        // f̄_i = feq_i(rhoBar = 0, invRho = 1, j = u)
-        const T uSqr = d0 * d0 + d1 * d1 + d2 * d2;
+    // the thread's two cells: local index l = lx * 64 + ly * 8 + lz
+    int X[2], Y[2], Z[2];
+    bool in[2];
+    uint32_t nold[2], idold[2];
+    T u[2][3], d[2][3];
+    bool dirty[2] = {false, false}, defv[2] = {false, false};
+    size_t c[2];
 #pragma unroll
-        for (int i = 0; i < Q; ++i) {
-            const T cu = T(cx(i)) * d0 + T(cy(i)) * d1 + T(cz(i)) * d2;
-            const T e = T(wt(i)) * (T(3) * cu + (T(4.5) * cu * cu - T(1.5) * uSqr));
-            *pop_slot(f, i, X, Y, Z, phase, g) = e;
+    for (int h = 0; h < 2; ++h) {
+        const int l = tid + h * VOX_THREADS;
+        X[h] = tx * TILE + (l >> 6); Y[h] = ty * TILE + ((l >> 3) & 7); Z[h] = tz * TILE + (l & 7);
+        in[h] = X[h] < g.nx && Y[h] < g.ny && Z[h] < g.nz;
+        c[h] = in[h] ? ((size_t)X[h] * g.ny + Y[h]) * g.nz + Z[h] : 0;
+        const uint32_t w0 = in[h] ? vox[c[h]] : 0u;
+        nold[h] = w0 & VOX_NMASK;
+        idold[h] = w0 >> VOX_NBITS;
+        u[h][0] = u[h][1] = u[h][2] = T(0);
+        d[h][0] = d[h][1] = d[h][2] = T(0);
+        if (nold[h] > 0) { u[h][0] = up[c[h]]; u[h][1] = up[g.N + c[h]]; u[h][2] = up[2 * g.N + c[h]]; }
+    }
+
+    for (int base = 0; base < cnt; base += VOX_CHUNK) {
+        const int m = min(VOX_CHUNK, cnt - base);
+        __syncthreads();   // sorted list ready / previous chunk finished with S.q and S.n
+        {
+            const int words = (int)(sizeof(SphereFast) / 4);
+            for (int k = tid; k < m * words; k += VOX_THREADS) {
+                const int e = k / words, wd = k - e * words;
+                reinterpret_cast<int*>(&S.q[e])[wd] = reinterpret_cast<const int*>(&fast[S.sorted[base + e]])[wd];
+            }
+        }
+        if (tid == 0) S.qcount = 0;
+        __syncthreads();
+        // Phase A
+        for (int k = 0; k < m; ++k) {
+            const SphereFast& q = S.q[k];
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int l = tid + h * VOX_THREADS;
+                uint8_t n = N_NONE;
+                if (in[h] && X[h] >= q.lo[0] && X[h] <= q.hi[0] && Y[h] >= q.lo[1] && Y[h] <= q.hi[1] &&
+                    Z[h] >= q.lo[2] && Z[h] <= q.hi[2]) {
+                    const float dxf = ((float)X[h] - q.xh[0]) - q.xl[0];
+                    const float dyf = ((float)Y[h] - q.xh[1]) - q.xl[1];
+                    const float dzf = ((float)Z[h] - q.xh[2]) - q.xl[2];
+                    const float distf = (dxf * dxf + dyf * dyf) + dzf * dzf;
+                    const float M = q.margin;
+                    int region;
+                    if (fabsf(distf - q.rp2) <= M || fabsf(distf - q.rm2) <= M)
+                        region = region_exact(X[h], Y[h], Z[h], sph[S.sorted[base + k]]);
+                    else
+                        region = distf > q.rp2 ? 0 : (distf < q.rm2 ? 1 : 2);
+                    if (region == 0) n = 0;
+                    else if (region == 1) n = 125;
+                    else {
+                        const int pos = atomicAdd(&S.qcount, 1);
+                        if (pos < VOX_QUEUE) {
+                            S.queue[pos] = (uint16_t)((k << 9) | l);
+                            n = N_PENDING;
+                        } else {
+                            n = (uint8_t)shell_count(q, sph[S.sorted[base + k]], X[h], Y[h], Z[h]);
+                        }
+                    }
+                }
+                S.n[k][l] = n;
+            }
+        }
+        __syncthreads();
+        // Phase B
+        {
+            const int qn = min(S.qcount, VOX_QUEUE);
+            for (int e = tid; e < qn; e += VOX_THREADS) {
+                const int k = S.queue[e] >> 9, l = S.queue[e] & 511;
+                const int Xe = tx * TILE + (l >> 6), Ye = ty * TILE + ((l >> 3) & 7), Ze = tz * TILE + (l & 7);
+                S.n[k][l] = (uint8_t)shell_count(S.q[k], sph[S.sorted[base + k]], Xe, Ye, Ze);
+            }
+        }
+        __syncthreads();
+        // Phase C: decFlag, src/ibProcessors3D.hh:85-105 (sf > 0.001 <=> n > 0; sf > sf_old <=> n > n_old)
+        for (int k = 0; k < m; ++k) {
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int l = tid + h * VOX_THREADS;
+                const int n = S.n[k][l];
+                if (n == N_NONE) continue;
+                const SphereFast& q = S.q[k];
+                const int dec = (n > 0 ? 1 : 0) + (nold[h] > 0 ? 2 : 0);
+                bool set = false, zero = false;
+                if (dec == 1) set = true;
+                else if (dec == 2) zero = (idold[h] == (uint32_t)q.tag);
+                else if (dec == 3) set = (n > (int)nold[h]) || (idold[h] == (uint32_t)q.tag);
+                // dec == 0 is setToZero on a cell that is already empty
+                if (zero) {
+                    nold[h] = 0; idold[h] = 0; u[h][0] = u[h][1] = u[h][2] = T(0); dirty[h] = true;
+                } else if (set) {
+                    // setValues, src/ibProcessors3D.hh:163-174 (com == x for single spheres)
+                    if (sizeof(T) == 8) {
+                        double a0, a1, a2;
+                        surface_velocity(sph[S.sorted[base + k]], X[h], Y[h], Z[h], a0, a1, a2);
+                        u[h][0] = T(a0); u[h][1] = T(a1); u[h][2] = T(a2);
+                    } else {
+                        const float dxf = ((float)X[h] - q.xh[0]) - q.xl[0];
+                        const float dyf = ((float)Y[h] - q.xh[1]) - q.xl[1];
+                        const float dzf = ((float)Z[h] - q.xh[2]) - q.xl[2];
+                        u[h][0] = T(q.v[0] + (q.w[1] * dzf - q.w[2] * dyf));
+                        u[h][1] = T(q.v[1] + (-q.w[0] * dzf + q.w[2] * dxf));
+                        u[h][2] = T(q.v[2] + (q.w[0] * dyf - q.w[1] * dxf));
+                    }
+                    nold[h] = (uint32_t)n; idold[h] = (uint32_t)q.tag; dirty[h] = true;
+                }
+                if (INIT_VEL && n == 125) { defv[h] = true; d[h][0] = u[h][0]; d[h][1] = u[h][1]; d[h][2] = u[h][2]; }
+            }
+        }
+    }
+
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        if (!in[h]) continue;
+        if (dirty[h]) {
+            vox[c[h]] = nold[h] | (idold[h] << VOX_NBITS);
+            up[c[h]] = u[h][0]; up[g.N + c[h]] = u[h][1]; up[2 * g.N + c[h]] = u[h][2];
+        }
+        if (INIT_VEL && defv[h]) {
+            // f̄_i = feq_i(rhoBar = 0, invRho = 1, j = u)
+            const T d0 = d[h][0], d1 = d[h][1], d2 = d[h][2];
+            const T uSqr = d0 * d0 + d1 * d1 + d2 * d2;
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                const T cu = T(cx(i)) * d0 + T(cy(i)) * d1 + T(cz(i)) * d2;
+                const T e = T(wt(i)) * (T(3) * cu + (T(4.5) * cu * cu - T(1.5) * uSqr));
+                *pop_slot(f, i, X[h], Y[h], Z[h], phase, g) = e;
+            }
         }
     }
 }
@@ -396,12 +483,21 @@ cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, int n,
                             int ntiles, uint32_t* vox, T* up, T* f, int init_vel, int odd_phase, Geom g,
                             unsigned* err, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
+    constexpr size_t smem = sizeof(VoxSmem);
+    static bool attr = false;
+    if (!attr) {
+        cudaError_t e = cudaFuncSetAttribute(k_voxelize<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_voxelize<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (e != cudaSuccess) return e;
+        attr = true;
+    }
     if (init_vel)
-        k_voxelize<T, true><<<ntiles, TILE_CELLS, 0, s>>>(sph, fast, n, tile_cnt, bins, vox, up, f, odd_phase, g,
-                                                          err);
+        k_voxelize<T, true><<<ntiles, VOX_THREADS, smem, s>>>(sph, fast, n, tile_cnt, bins, vox, up, f, odd_phase, g,
+                                                              err);
     else
-        k_voxelize<T, false><<<ntiles, TILE_CELLS, 0, s>>>(sph, fast, n, tile_cnt, bins, vox, up, f, odd_phase, g,
-                                                           err);
+        k_voxelize<T, false><<<ntiles, VOX_THREADS, smem, s>>>(sph, fast, n, tile_cnt, bins, vox, up, f, odd_phase, g,
+                                                               err);
     return cudaGetLastError();
 }
 

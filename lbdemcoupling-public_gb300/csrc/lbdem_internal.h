@@ -14,8 +14,7 @@ constexpr int Q = 19;
 constexpr int TILE = 8;                 // voxelization tile edge (cells)
 constexpr int TILE_CELLS = TILE * TILE * TILE;
 constexpr int TILE_BIN = 64;            // sphere slots per tile bin
-constexpr int TILE_LIST_MAX = 2048;     // spheres per tile when a bin overflows (shared memory)
-constexpr int TILE_STAGE = 64;          // sphere records staged in shared memory per tile
+constexpr int TILE_LIST_MAX = 1024;     // spheres per tile when a bin overflows (shared memory)
 constexpr int REC_STRIDE = 12;          // doubles per particle record {x3, v3, w3, r, tag, 0}
 constexpr int VOX_NBITS = 7;            // voxel word: sub-cell count n (7 bits) | tag << 7
 constexpr uint32_t VOX_NMASK = (1u << VOX_NBITS) - 1u;
