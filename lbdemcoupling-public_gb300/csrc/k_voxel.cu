@@ -52,68 +52,6 @@ __device__ __noinline__ int region_exact(int X, int Y, int Z, const SphereDev& s
     return 2;
 }
 
-// Float sample count; the samples inside [rsq - M, rsq + M) are decided with
-// the reference's double sequence.
-__device__ __noinline__ int count_resolve(float dxf, float dyf, float dzf, float rsq, float M, int X, int Y, int Z,
-                                          const SphereDev& s) {
-    const double dx = __dsub_rn((double)X, s.x[0]);
-    const double dy = __dsub_rn((double)Y, s.x[1]);
-    const double dz = __dsub_rn((double)Z, s.x[2]);
-    double xs[5], ys[5], zs[5];
-    float xf[5], yf[5], zf[5];
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-        const double d = sub_delta(i);
-        const double ax = __dadd_rn(dx, d); xs[i] = __dmul_rn(ax, ax);
-        const double ay = __dadd_rn(dy, d); ys[i] = __dmul_rn(ay, ay);
-        const double az = __dadd_rn(dz, d); zs[i] = __dmul_rn(az, az);
-        const float e = sub_delta_f(i);
-        const float bx = dxf + e; xf[i] = bx * bx;
-        const float by = dyf + e; yf[i] = by * by;
-        const float bz = dzf + e; zf[i] = bz * bz;
-    }
-    const float lo = rsq - M, hi = rsq + M;
-    int n = 0;
-    for (int i = 0; i < 5; ++i)
-        for (int j = 0; j < 5; ++j) {
-            const float a = xf[i] + yf[j];
-            for (int k = 0; k < 5; ++k) {
-                const float t = a + zf[k];
-                if (t < lo) ++n;
-                else if (t < hi) n += (__dadd_rn(__dadd_rn(xs[i], ys[j]), zs[k]) < s.rsq) ? 1 : 0;
-            }
-        }
-    return n;
-}
-
-// Float sample count; *unsure is set when a sample falls inside the band.
-__device__ __forceinline__ int count_fast(float dxf, float dyf, float dzf, float rsq, float M, bool* unsure) {
-    float xs[5], ys[5], zs[5];
-#pragma unroll
-    for (int i = 0; i < 5; ++i) {
-        const float d = sub_delta_f(i);
-        const float ax = dxf + d; xs[i] = ax * ax;
-        const float ay = dyf + d; ys[i] = ay * ay;
-        const float az = dzf + d; zs[i] = az * az;
-    }
-    const float lo = rsq - M, hi = rsq + M;
-    int n_lo = 0, n_hi = 0;
-#pragma unroll
-    for (int i = 0; i < 5; ++i)
-#pragma unroll
-        for (int j = 0; j < 5; ++j) {
-            const float a = xs[i] + ys[j];
-#pragma unroll
-            for (int k = 0; k < 5; ++k) {
-                const float t = a + zs[k];
-                n_lo += t < lo ? 1 : 0;
-                n_hi += t < hi ? 1 : 0;
-            }
-        }
-    *unsure = n_lo != n_hi;
-    return n_lo;
-}
-
 __device__ __forceinline__ int tiles_along(int n) { return (n + TILE - 1) / TILE; }
 
 // Per sphere: bounding box (double -> integer truncation toward zero,
@@ -236,39 +174,106 @@ __device__ __forceinline__ void surface_velocity(const SphereDev& s, int X, int 
     u2 = __dadd_rn(s.v[2], __dsub_rn(__dmul_rn(s.w[0], dy), __dmul_rn(s.w[1], dx)));
 }
 
+// Sub-cell count of one x-slice (i fixed: 25 of the 125 samples) of a shell
+// cell in float; *unsure is set when a sample falls inside the decision band.
+__device__ __forceinline__ int slice_count_fast(float dxf, float dyf, float dzf, int i, float rsq, float M,
+                                                bool* unsure) {
+    const float ax = dxf + sub_delta_f(i);
+    const float xs = ax * ax;
+    float ys[5], zs[5];
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        const float d = sub_delta_f(j);
+        const float ay = dyf + d; ys[j] = ay * ay;
+        const float az = dzf + d; zs[j] = az * az;
+    }
+    const float lo = rsq - M, hi = rsq + M;
+    int n_lo = 0, n_hi = 0;
+#pragma unroll
+    for (int j = 0; j < 5; ++j) {
+        const float a = xs + ys[j];
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const float t = a + zs[k];
+            n_lo += t < lo ? 1 : 0;
+            n_hi += t < hi ? 1 : 0;
+        }
+    }
+    *unsure = n_lo != n_hi;
+    return n_lo;
+}
+
+// The same slice with the samples inside the band decided by the reference's
+// double sequence ((xs_i + ys_j) + zs_k < r^2, src/ibProcessors3D.hh:141-155).
+__device__ __noinline__ int slice_count_resolve(float dxf, float dyf, float dzf, int i, float rsq, float M, int X,
+                                                int Y, int Z, const SphereDev& s) {
+    const double dx = __dsub_rn((double)X, s.x[0]);
+    const double dy = __dsub_rn((double)Y, s.x[1]);
+    const double dz = __dsub_rn((double)Z, s.x[2]);
+    const double axd = __dadd_rn(dx, sub_delta(i));
+    const double xsd = __dmul_rn(axd, axd);
+    const float ax = dxf + sub_delta_f(i);
+    const float xs = ax * ax;
+    const float lo = rsq - M, hi = rsq + M;
+    int n = 0;
+    for (int j = 0; j < 5; ++j) {
+        const float ay = dyf + sub_delta_f(j);
+        const float a = xs + ay * ay;
+        double ad = 0.0;
+        bool have_ad = false;
+        for (int k = 0; k < 5; ++k) {
+            const float az = dzf + sub_delta_f(k);
+            const float t = a + az * az;
+            if (t < lo) {
+                ++n;
+            } else if (t < hi) {
+                if (!have_ad) {
+                    const double ayd = __dadd_rn(dy, sub_delta(j));
+                    ad = __dadd_rn(xsd, __dmul_rn(ayd, ayd));
+                    have_ad = true;
+                }
+                const double azd = __dadd_rn(dz, sub_delta(k));
+                n += (__dadd_rn(ad, __dmul_rn(azd, azd)) < s.rsq) ? 1 : 0;
+            }
+        }
+    }
+    return n;
+}
+
 // Shared memory of one voxelization block.
 constexpr int VOX_THREADS = 256;            // two cells of the 8^3 tile per thread
-constexpr int VOX_CHUNK = 64;               // spheres classified per pass
-constexpr int VOX_QUEUE = 4096;             // shell (sphere, cell) pairs counted per pass
-constexpr uint8_t N_NONE = 255;             // cell outside the sphere's box
-constexpr uint8_t N_PENDING = 254;          // shell cell whose count is queued
+constexpr int VOX_CHUNK = 32;               // spheres classified per pass
+constexpr int VOX_QUEUE = 2048;             // shell (sphere, cell) pairs per pass
+constexpr uint32_t N_NONE = 255;            // cell outside the sphere's box
 
+template <typename T, bool INIT_VEL>
 struct VoxSmem {
     int raw[TILE_LIST_MAX];
     int sorted[TILE_LIST_MAX];
     SphereFast q[VOX_CHUNK];
-    uint8_t n[VOX_CHUNK][TILE_CELLS];       // sub-cell count of (sphere k, cell)
-    uint16_t queue[VOX_QUEUE];              // (k << 9) | cell
+    uint32_t n4[VOX_CHUNK][TILE_CELLS / 4];   // count of (sphere k, cell), one byte per cell
+    uint16_t queue[VOX_QUEUE];                // (k << 9) | cell of the queued shell pairs
+    T u[3][TILE_CELLS];                       // cell state carried across chunks
+    T d[INIT_VEL ? 3 : 1][INIT_VEL ? TILE_CELLS : 1];
+    uint32_t id[TILE_CELLS];
+    uint8_t n[TILE_CELLS];
+    uint8_t flags[TILE_CELLS];                // bit 0: state changed, bit 1: define velocity
     int qcount;
     int cnt;
 };
 
-// Sub-cell count of a shell cell (float filter, exact where unsure).
-__device__ __forceinline__ int shell_count(const SphereFast& q, const SphereDev& s, int X, int Y, int Z) {
-    const float dxf = ((float)X - q.xh[0]) - q.xl[0];
-    const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
-    const float dzf = ((float)Z - q.xh[2]) - q.xl[2];
-    bool unsure;
-    int n = count_fast(dxf, dyf, dzf, q.rsq, q.margin, &unsure);
-    if (unsure) n = count_resolve(dxf, dyf, dzf, q.rsq, q.margin, X, Y, Z, s);
-    return n;
+__device__ __forceinline__ uint32_t get_n(const uint32_t* row, int l) { return (row[l >> 2] >> (8 * (l & 3))) & 0xffu; }
+__device__ __forceinline__ void set_n(uint32_t* row, int l, uint32_t n) {
+    uint8_t* b = reinterpret_cast<uint8_t*>(row);
+    b[l] = (uint8_t)n;
 }
 
-// One block per 8^3 tile, 256 threads, two cells per thread.  Spheres are taken
-// in sorted chunks of VOX_CHUNK; each chunk runs three phases:
+// One block per 8^3 tile, 256 threads.  Spheres are taken in sorted chunks of
+// VOX_CHUNK; each chunk runs three phases separated by block barriers:
 //  A  classify every (sphere, cell) pair in float: outside the box, outside
-//     (n = 0) and inside (n = 125) are final, shell cells are queued;
-//  B  all threads drain the queue, so the 125-sample counts run at full width;
+//     (n = 0) and inside (n = 125) are final, shell pairs are queued with n = 0;
+//  B  the queue is split into x-slices (25 samples each) and drained by all
+//     threads, slice counts added into the pair's byte with shared atomics;
 //  C  every cell folds the chunk's counts, in sphere order, through decFlag.
 // INIT_VEL: defineVelocity (src/ibCompositeDynamics3D.hh:118-127) is applied
 // with the uPart the cell holds right after each sphere that covers it fully
@@ -280,7 +285,7 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
            int* __restrict__ tile_cnt, const int* __restrict__ bins, uint32_t* __restrict__ vox, T* __restrict__ up,
            T* __restrict__ f, int phase, Geom g, unsigned* __restrict__ err) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    VoxSmem& S = *reinterpret_cast<VoxSmem*>(smem_raw);
+    VoxSmem<T, INIT_VEL>& S = *reinterpret_cast<VoxSmem<T, INIT_VEL>*>(smem_raw);
     const int tid = threadIdx.x;
     const int t = blockIdx.x;
     const int tny = tiles_along(g.ny), tnz = tiles_along(g.nz);
@@ -288,6 +293,7 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
     const int rem = t - tx * tny * tnz;
     const int ty = rem / tnz;
     const int tz = rem - ty * tnz;
+    const int X0 = tx * TILE, Y0 = ty * TILE, Z0 = tz * TILE;
 
     int cnt = tile_cnt[t];
     if (cnt <= 0) return;
@@ -299,11 +305,10 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
         // bin overflow: collect every sphere whose box overlaps this tile
         if (tid == 0) S.cnt = 0;
         __syncthreads();
-        const int bx0 = tx * TILE, by0 = ty * TILE, bz0 = tz * TILE;
         for (int i = tid; i < nsph; i += VOX_THREADS) {
             const SphereFast& q = fast[i];
-            if (q.lo[0] <= bx0 + TILE - 1 && q.hi[0] >= bx0 && q.lo[1] <= by0 + TILE - 1 && q.hi[1] >= by0 &&
-                q.lo[2] <= bz0 + TILE - 1 && q.hi[2] >= bz0 && q.lo[0] <= q.hi[0] && q.lo[1] <= q.hi[1] &&
+            if (q.lo[0] <= X0 + TILE - 1 && q.hi[0] >= X0 && q.lo[1] <= Y0 + TILE - 1 && q.hi[1] >= Y0 &&
+                q.lo[2] <= Z0 + TILE - 1 && q.hi[2] >= Z0 && q.lo[0] <= q.hi[0] && q.lo[1] <= q.hi[1] &&
                 q.lo[2] <= q.hi[2]) {
                 const int pos = atomicAdd(&S.cnt, 1);
                 if (pos < TILE_LIST_MAX) S.raw[pos] = i;
@@ -316,6 +321,23 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
             return;
         }
     }
+    // cell state into shared memory
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int l = tid + h * VOX_THREADS;
+        const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
+        uint32_t w0 = 0;
+        if (X < g.nx && Y < g.ny && Z < g.nz) w0 = vox[((size_t)X * g.ny + Y) * g.nz + Z];
+        S.n[l] = (uint8_t)(w0 & VOX_NMASK);
+        S.id[l] = w0 >> VOX_NBITS;
+        S.flags[l] = 0;
+        T u0 = T(0), u1 = T(0), u2 = T(0);
+        if ((w0 & VOX_NMASK) > 0) {
+            const size_t c = ((size_t)X * g.ny + Y) * g.nz + Z;
+            u0 = up[c]; u1 = up[g.N + c]; u2 = up[2 * g.N + c];
+        }
+        S.u[0][l] = u0; S.u[1][l] = u1; S.u[2][l] = u2;
+    }
     __syncthreads();
     // rank sort by sphere index (the indices of one list are distinct)
     for (int k = tid; k < cnt; k += VOX_THREADS) {
@@ -325,30 +347,9 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
         S.sorted[rank] = vk;
     }
 
-    // the thread's two cells: local index l = lx * 64 + ly * 8 + lz
-    int X[2], Y[2], Z[2];
-    bool in[2];
-    uint32_t nold[2], idold[2];
-    T u[2][3], d[2][3];
-    bool dirty[2] = {false, false}, defv[2] = {false, false};
-    size_t c[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int l = tid + h * VOX_THREADS;
-        X[h] = tx * TILE + (l >> 6); Y[h] = ty * TILE + ((l >> 3) & 7); Z[h] = tz * TILE + (l & 7);
-        in[h] = X[h] < g.nx && Y[h] < g.ny && Z[h] < g.nz;
-        c[h] = in[h] ? ((size_t)X[h] * g.ny + Y[h]) * g.nz + Z[h] : 0;
-        const uint32_t w0 = in[h] ? vox[c[h]] : 0u;
-        nold[h] = w0 & VOX_NMASK;
-        idold[h] = w0 >> VOX_NBITS;
-        u[h][0] = u[h][1] = u[h][2] = T(0);
-        d[h][0] = d[h][1] = d[h][2] = T(0);
-        if (nold[h] > 0) { u[h][0] = up[c[h]]; u[h][1] = up[g.N + c[h]]; u[h][2] = up[2 * g.N + c[h]]; }
-    }
-
     for (int base = 0; base < cnt; base += VOX_CHUNK) {
         const int m = min(VOX_CHUNK, cnt - base);
-        __syncthreads();   // sorted list ready / previous chunk finished with S.q and S.n
+        __syncthreads();   // sorted list ready / previous chunk finished with S.q and S.n4
         {
             const int words = (int)(sizeof(SphereFast) / 4);
             for (int k = tid; k < m * words; k += VOX_THREADS) {
@@ -361,101 +362,132 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
         // Phase A
         for (int k = 0; k < m; ++k) {
             const SphereFast& q = S.q[k];
-#pragma unroll
+#pragma unroll 1
             for (int h = 0; h < 2; ++h) {
                 const int l = tid + h * VOX_THREADS;
-                uint8_t n = N_NONE;
-                if (in[h] && X[h] >= q.lo[0] && X[h] <= q.hi[0] && Y[h] >= q.lo[1] && Y[h] <= q.hi[1] &&
-                    Z[h] >= q.lo[2] && Z[h] <= q.hi[2]) {
-                    const float dxf = ((float)X[h] - q.xh[0]) - q.xl[0];
-                    const float dyf = ((float)Y[h] - q.xh[1]) - q.xl[1];
-                    const float dzf = ((float)Z[h] - q.xh[2]) - q.xl[2];
+                const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
+                uint32_t n = N_NONE;
+                if (X < g.nx && Y < g.ny && Z < g.nz && X >= q.lo[0] && X <= q.hi[0] && Y >= q.lo[1] &&
+                    Y <= q.hi[1] && Z >= q.lo[2] && Z <= q.hi[2]) {
+                    const float dxf = ((float)X - q.xh[0]) - q.xl[0];
+                    const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
+                    const float dzf = ((float)Z - q.xh[2]) - q.xl[2];
                     const float distf = (dxf * dxf + dyf * dyf) + dzf * dzf;
                     const float M = q.margin;
                     int region;
                     if (fabsf(distf - q.rp2) <= M || fabsf(distf - q.rm2) <= M)
-                        region = region_exact(X[h], Y[h], Z[h], sph[S.sorted[base + k]]);
+                        region = region_exact(X, Y, Z, sph[S.sorted[base + k]]);
                     else
                         region = distf > q.rp2 ? 0 : (distf < q.rm2 ? 1 : 2);
-                    if (region == 0) n = 0;
-                    else if (region == 1) n = 125;
-                    else {
+                    if (region == 0) {
+                        n = 0;
+                    } else if (region == 1) {
+                        n = 125;
+                    } else {
+                        n = 0;   // the queued slice counts are added to it
                         const int pos = atomicAdd(&S.qcount, 1);
                         if (pos < VOX_QUEUE) {
                             S.queue[pos] = (uint16_t)((k << 9) | l);
-                            n = N_PENDING;
                         } else {
-                            n = (uint8_t)shell_count(q, sph[S.sorted[base + k]], X[h], Y[h], Z[h]);
+                            const SphereDev& s = sph[S.sorted[base + k]];
+                            for (int i = 0; i < 5; ++i) {
+                                bool unsure;
+                                int c = slice_count_fast(dxf, dyf, dzf, i, q.rsq, M, &unsure);
+                                if (unsure) c = slice_count_resolve(dxf, dyf, dzf, i, q.rsq, M, X, Y, Z, s);
+                                n += (uint32_t)c;
+                            }
                         }
                     }
                 }
-                S.n[k][l] = n;
+                set_n(S.n4[k], l, n);
             }
         }
         __syncthreads();
-        // Phase B
+        // Phase B: five x-slices per queued pair
         {
             const int qn = min(S.qcount, VOX_QUEUE);
-            for (int e = tid; e < qn; e += VOX_THREADS) {
+            for (int wi = tid; wi < 5 * qn; wi += VOX_THREADS) {
+                const int e = wi / 5, i = wi - 5 * e;
                 const int k = S.queue[e] >> 9, l = S.queue[e] & 511;
-                const int Xe = tx * TILE + (l >> 6), Ye = ty * TILE + ((l >> 3) & 7), Ze = tz * TILE + (l & 7);
-                S.n[k][l] = (uint8_t)shell_count(S.q[k], sph[S.sorted[base + k]], Xe, Ye, Ze);
+                const SphereFast& q = S.q[k];
+                const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
+                const float dxf = ((float)X - q.xh[0]) - q.xl[0];
+                const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
+                const float dzf = ((float)Z - q.xh[2]) - q.xl[2];
+                bool unsure;
+                int c = slice_count_fast(dxf, dyf, dzf, i, q.rsq, q.margin, &unsure);
+                if (unsure) c = slice_count_resolve(dxf, dyf, dzf, i, q.rsq, q.margin, X, Y, Z, sph[S.sorted[base + k]]);
+                if (c) atomicAdd(&S.n4[k][l >> 2], (uint32_t)c << (8 * (l & 3)));
             }
         }
         __syncthreads();
         // Phase C: decFlag, src/ibProcessors3D.hh:85-105 (sf > 0.001 <=> n > 0; sf > sf_old <=> n > n_old)
-        for (int k = 0; k < m; ++k) {
-#pragma unroll
-            for (int h = 0; h < 2; ++h) {
-                const int l = tid + h * VOX_THREADS;
-                const int n = S.n[k][l];
+#pragma unroll 1
+        for (int h = 0; h < 2; ++h) {
+            const int l = tid + h * VOX_THREADS;
+            const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
+            uint32_t nold = S.n[l], idold = S.id[l];
+            T u0 = S.u[0][l], u1 = S.u[1][l], u2 = S.u[2][l];
+            uint32_t fl = S.flags[l];
+            for (int k = 0; k < m; ++k) {
+                const uint32_t n = get_n(S.n4[k], l);
                 if (n == N_NONE) continue;
                 const SphereFast& q = S.q[k];
-                const int dec = (n > 0 ? 1 : 0) + (nold[h] > 0 ? 2 : 0);
+                const int dec = (n > 0 ? 1 : 0) + (nold > 0 ? 2 : 0);
                 bool set = false, zero = false;
                 if (dec == 1) set = true;
-                else if (dec == 2) zero = (idold[h] == (uint32_t)q.tag);
-                else if (dec == 3) set = (n > (int)nold[h]) || (idold[h] == (uint32_t)q.tag);
+                else if (dec == 2) zero = (idold == (uint32_t)q.tag);
+                else if (dec == 3) set = (n > nold) || (idold == (uint32_t)q.tag);
                 // dec == 0 is setToZero on a cell that is already empty
                 if (zero) {
-                    nold[h] = 0; idold[h] = 0; u[h][0] = u[h][1] = u[h][2] = T(0); dirty[h] = true;
+                    nold = 0; idold = 0; u0 = u1 = u2 = T(0); fl |= 1u;
                 } else if (set) {
                     // setValues, src/ibProcessors3D.hh:163-174 (com == x for single spheres)
                     if (sizeof(T) == 8) {
                         double a0, a1, a2;
-                        surface_velocity(sph[S.sorted[base + k]], X[h], Y[h], Z[h], a0, a1, a2);
-                        u[h][0] = T(a0); u[h][1] = T(a1); u[h][2] = T(a2);
+                        surface_velocity(sph[S.sorted[base + k]], X, Y, Z, a0, a1, a2);
+                        u0 = T(a0); u1 = T(a1); u2 = T(a2);
                     } else {
-                        const float dxf = ((float)X[h] - q.xh[0]) - q.xl[0];
-                        const float dyf = ((float)Y[h] - q.xh[1]) - q.xl[1];
-                        const float dzf = ((float)Z[h] - q.xh[2]) - q.xl[2];
-                        u[h][0] = T(q.v[0] + (q.w[1] * dzf - q.w[2] * dyf));
-                        u[h][1] = T(q.v[1] + (-q.w[0] * dzf + q.w[2] * dxf));
-                        u[h][2] = T(q.v[2] + (q.w[0] * dyf - q.w[1] * dxf));
+                        const float dxf = ((float)X - q.xh[0]) - q.xl[0];
+                        const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
+                        const float dzf = ((float)Z - q.xh[2]) - q.xl[2];
+                        u0 = T(q.v[0] + (q.w[1] * dzf - q.w[2] * dyf));
+                        u1 = T(q.v[1] + (-q.w[0] * dzf + q.w[2] * dxf));
+                        u2 = T(q.v[2] + (q.w[0] * dyf - q.w[1] * dxf));
                     }
-                    nold[h] = (uint32_t)n; idold[h] = (uint32_t)q.tag; dirty[h] = true;
+                    nold = n; idold = (uint32_t)q.tag; fl |= 1u;
                 }
-                if (INIT_VEL && n == 125) { defv[h] = true; d[h][0] = u[h][0]; d[h][1] = u[h][1]; d[h][2] = u[h][2]; }
+                if (INIT_VEL && n == 125) {
+                    fl |= 2u;
+                    S.d[0][l] = u0; S.d[1][l] = u1; S.d[2][l] = u2;
+                }
             }
+            S.n[l] = (uint8_t)nold; S.id[l] = idold; S.flags[l] = (uint8_t)fl;
+            S.u[0][l] = u0; S.u[1][l] = u1; S.u[2][l] = u2;
         }
     }
 
-#pragma unroll
+    // write back (each thread its own two cells; no barrier needed)
+#pragma unroll 1
     for (int h = 0; h < 2; ++h) {
-        if (!in[h]) continue;
-        if (dirty[h]) {
-            vox[c[h]] = nold[h] | (idold[h] << VOX_NBITS);
-            up[c[h]] = u[h][0]; up[g.N + c[h]] = u[h][1]; up[2 * g.N + c[h]] = u[h][2];
+        const int l = tid + h * VOX_THREADS;
+        const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
+        if (X >= g.nx || Y >= g.ny || Z >= g.nz) continue;
+        const size_t c = ((size_t)X * g.ny + Y) * g.nz + Z;
+        const uint32_t fl = S.flags[l];
+        if (fl & 1u) {
+            vox[c] = (uint32_t)S.n[l] | (S.id[l] << VOX_NBITS);
+            up[c] = S.u[0][l]; up[g.N + c] = S.u[1][l]; up[2 * g.N + c] = S.u[2][l];
         }
-        if (INIT_VEL && defv[h]) {
+        if (INIT_VEL && (fl & 2u)) {
             // f̄_i = feq_i(rhoBar = 0, invRho = 1, j = u)
-            const T d0 = d[h][0], d1 = d[h][1], d2 = d[h][2];
+            const T d0 = S.d[0][l], d1 = S.d[1][l], d2 = S.d[2][l];
             const T uSqr = d0 * d0 + d1 * d1 + d2 * d2;
 #pragma unroll
             for (int i = 0; i < Q; ++i) {
                 const T cu = T(cx(i)) * d0 + T(cy(i)) * d1 + T(cz(i)) * d2;
                 const T e = T(wt(i)) * (T(3) * cu + (T(4.5) * cu * cu - T(1.5) * uSqr));
-                *pop_slot(f, i, X[h], Y[h], Z[h], phase, g) = e;
+                *pop_slot(f, i, X, Y, Z, phase, g) = e;
             }
         }
     }
@@ -483,18 +515,19 @@ cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, int n,
                             int ntiles, uint32_t* vox, T* up, T* f, int init_vel, int odd_phase, Geom g,
                             unsigned* err, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
-    constexpr size_t smem = sizeof(VoxSmem);
+    constexpr size_t smem_iv = sizeof(VoxSmem<T, true>), smem = sizeof(VoxSmem<T, false>);
     static bool attr = false;
     if (!attr) {
-        cudaError_t e = cudaFuncSetAttribute(k_voxelize<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        cudaError_t e =
+            cudaFuncSetAttribute(k_voxelize<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_iv);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_voxelize<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e != cudaSuccess) return e;
         attr = true;
     }
     if (init_vel)
-        k_voxelize<T, true><<<ntiles, VOX_THREADS, smem, s>>>(sph, fast, n, tile_cnt, bins, vox, up, f, odd_phase, g,
-                                                              err);
+        k_voxelize<T, true><<<ntiles, VOX_THREADS, smem_iv, s>>>(sph, fast, n, tile_cnt, bins, vox, up, f, odd_phase,
+                                                                 g, err);
     else
         k_voxelize<T, false><<<ntiles, VOX_THREADS, smem, s>>>(sph, fast, n, tile_cnt, bins, vox, up, f, odd_phase, g,
                                                                err);
