@@ -280,7 +280,7 @@ __device__ __forceinline__ void set_n(uint32_t* row, int l, uint32_t n) {
 // (src/ibProcessors3D.hh:107-108); it depends only on that uPart, so the last
 // such sphere decides the populations written.
 template <typename T, bool INIT_VEL>
-__global__ void __launch_bounds__(VOX_THREADS, 2)
+__global__ void __launch_bounds__(VOX_THREADS, 4)   // 4 blocks per SM (measured best; a few spills)
 k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fast, int nsph,
            int* __restrict__ tile_cnt, const int* __restrict__ bins, uint32_t* __restrict__ vox, T* __restrict__ up,
            T* __restrict__ f, int phase, Geom g, unsigned* __restrict__ err) {
