@@ -179,6 +179,40 @@ lbdem_status lbdem_device_bytes(lbdem_handle* h, size_t* bytes);
  * library; memset/memcpy not counted). */
 lbdem_status lbdem_get_launch_count(lbdem_handle* h, int64_t* count);
 
+/* ---- Voxelization that allocates nothing ---------------------------------
+ * No counterpart in the reference.  For callers that cannot have a library
+ * allocate device memory: an application that gives the whole GPU to its own
+ * pool allocator, or a coupling loop that must not pay the device-wide
+ * synchronisation of cudaMalloc/cudaFree.  Applies SetSingleSphere3D for n
+ * spheres, in list order, to cell state the caller owns -- exactly what
+ * lbdem_set_particles does to a handle's state -- without a handle and
+ * without any allocation: its scratch (sphere tables, tile bins, tag map) is
+ * one static device array of LBDEM_STATIC_SCRATCH_BYTES that every GPU which
+ * loads the library keeps until the process exits.
+ *   nx, ny, nz   lattice extent; at most LBDEM_STATIC_MAX_TILES tiles of 8^3
+ *                cells (e.g. 128^3 cells)
+ *   precision    element type of dev_up (lbdem_precision)
+ *   n, dev_rec   particle table in device memory, [n][12] doubles as for
+ *                lbdem_set_particles_device; n <= LBDEM_STATIC_MAX_SPHERES,
+ *                tags 1..LBDEM_STATIC_MAX_TAG
+ *   dev_vox      [N] voxel words (count n | tag << 7), read and updated
+ *   dev_up       [3][N] particle surface velocity, read and updated
+ *   dev_err      one device word; LBDEM_DEVERR_* bits are OR-ed into it
+ *   cuda_stream  stream of the work (NULL: the legacy default stream)
+ * Sizes beyond the limits return LBDEM_ERR_CAPACITY before any GPU work.
+ * The work is queued and not synchronized.  The first call on a device, with
+ * that device current, resolves the array's device address; make that first
+ * call before any stream capture.  Every call uses the same array: calls
+ * whose GPU work overlaps (on different streams or threads) race on it.  Each
+ * call clears the tile counters and the tag map before using them. */
+#define LBDEM_STATIC_MAX_SPHERES 4096
+#define LBDEM_STATIC_MAX_TILES 4096
+#define LBDEM_STATIC_MAX_TAG 65535
+#define LBDEM_STATIC_SCRATCH_BYTES (3u << 20)
+lbdem_status lbdem_voxelize_static(int32_t nx, int32_t ny, int32_t nz, int32_t precision, int32_t n,
+                                   const double* dev_rec, uint32_t* dev_vox, void* dev_up, uint32_t* dev_err,
+                                   void* cuda_stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -80,7 +80,21 @@ SIGNATURES = {
     "lbdem_get_step": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "lbdem_device_bytes": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
     "lbdem_get_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "lbdem_voxelize_static": (C.c_int, [_I, _I, _I, _I, _I, _P, _P, _P, _P, _P]),
 }
+
+# Limits of lbdem_voxelize_static (include/lbdem_gpu.h).
+STATIC_MAX_SPHERES = 4096
+STATIC_MAX_TILES = 4096
+STATIC_MAX_TAG = 65535
+
+
+def voxelize_static(shape, precision, n, rec_ptr, vox_ptr, up_ptr, err_ptr, stream_ptr=None) -> int:
+    """lbdem_voxelize_static on device pointers; returns the lbdem_status."""
+    lib = load()
+    nx, ny, nz = (int(s) for s in shape)
+    return int(lib.lbdem_voxelize_static(nx, ny, nz, int(precision), int(n), _P(rec_ptr), _P(vox_ptr),
+                                         _P(up_ptr), _P(err_ptr), _P(stream_ptr) if stream_ptr else None))
 
 _lib = None
 
