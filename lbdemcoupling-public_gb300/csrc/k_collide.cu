@@ -473,7 +473,8 @@ __device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, WarpStage
     if (bytes) bulk_g2s(dst, src, bytes, &st.bar[b]);
 }
 
-template <typename T, bool ODD, bool FORCE>
+// PER: every axis periodic (no wall cases; shifts and neighbour rows are fixed).
+template <typename T, bool ODD, bool FORCE, bool PER>
 __global__ void __launch_bounds__(COLLIDE_BLOCK)
 k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
     constexpr int V = WarpStage<T>::V;
@@ -511,7 +512,7 @@ k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
         const size_t own = (size_t)st.row[b][row_slot(0, 0)];
         // Odd phase with walls along z: the halo element of an edge cell is its
         // own slot i (half-way bounce-back).
-        if (ODD && !g.per[2] && (z0 == 0 || z0 + len == g.nz)) {
+        if (ODD && !PER && !g.per[2] && (z0 == 0 || z0 + len == g.nz)) {
             if (lane < 10) {
                 const int i = zdir(lane);
                 if (st.row[b][row_slot(-cx(i), -cy(i))] >= 0) {
@@ -522,7 +523,7 @@ k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
             __syncwarp();
         }
         uint32_t srcrow = 0;   // bit i: source row of direction i lies inside the lattice
-        if (ODD) {
+        if (ODD && !PER) {
 #pragma unroll
             for (int i = 1; i < Q; ++i)
                 if (cz(i) != 0 && st.row[b][row_slot(-cx(i), -cy(i))] >= 0) srcrow |= 1u << i;
@@ -537,7 +538,7 @@ k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
                 // smem index of direction i: V + j - shift_i, shift_i = c_z,i when
                 // the source row x - c_i exists (odd phase)
                 auto at = [&](int i) -> const T& {
-                    const int shift = (ODD && cz(i) != 0 && ((srcrow >> i) & 1u)) ? cz(i) : 0;
+                    const int shift = (ODD && cz(i) != 0 && (PER || ((srcrow >> i) & 1u))) ? cz(i) : 0;
                     return st.f[b][i][V + j - shift];
                 };
                 T f[Q];
@@ -551,12 +552,13 @@ k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
                     for (int i = 0; i < Q; ++i) F[(size_t)opp(i) * N + c] = f[i];
                 } else {
                     F[c] = f[0];
-                    const int zm = wrap_minus(z, g.nz, g.per[2]), zp = wrap_plus(z, g.nz, g.per[2]);
+                    const int zm = wrap_minus(z, g.nz, PER ? 1 : g.per[2]);
+                    const int zp = wrap_plus(z, g.nz, PER ? 1 : g.per[2]);
 #pragma unroll
                     for (int i = 1; i < Q; ++i) {
                         const long long r = st.row[b][row_slot(cx(i), cy(i))];
                         const int zd = pick(cz(i), zm, z, zp);
-                        if (r >= 0 && zd >= 0) F[(size_t)i * N + (size_t)r + zd] = f[i];
+                        if (PER || (r >= 0 && zd >= 0)) F[(size_t)i * N + (size_t)r + zd] = f[i];
                         else F[(size_t)opp(i) * N + c] = f[i];
                     }
                 }
@@ -576,7 +578,7 @@ cudaError_t launch_direct(const CollideArgs<T>& a, cudaStream_t s) {
     return cudaGetLastError();
 }
 
-template <typename T, bool ODD, bool FORCE>
+template <typename T, bool ODD, bool FORCE, bool PER>
 cudaError_t launch_staged(const CollideArgs<T>& a, cudaStream_t s) {
     constexpr size_t smem = WARPS * sizeof(WarpStage<T>);
     static int per_sm = 0, sms = 0;
@@ -585,10 +587,10 @@ cudaError_t launch_staged(const CollideArgs<T>& a, cudaStream_t s) {
         cudaError_t e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_collide_staged<T, ODD, FORCE>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)smem);
+            e = cudaFuncSetAttribute(k_collide_staged<T, ODD, FORCE, PER>,
+                                     cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collide_staged<T, ODD, FORCE>,
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collide_staged<T, ODD, FORCE, PER>,
                                                               COLLIDE_BLOCK, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
@@ -598,7 +600,7 @@ cudaError_t launch_staged(const CollideArgs<T>& a, cudaStream_t s) {
     const long long want = (long long)sms * per_sm;
     const long long blocks = (nseg + WARPS - 1) / WARPS;
     const unsigned grid = (unsigned)(blocks < want ? blocks : want);
-    k_collide_staged<T, ODD, FORCE><<<grid, COLLIDE_BLOCK, smem, s>>>(a, nzseg, nseg);
+    k_collide_staged<T, ODD, FORCE, PER><<<grid, COLLIDE_BLOCK, smem, s>>>(a, nzseg, nseg);
     return cudaGetLastError();
 }
 
@@ -606,7 +608,10 @@ template <typename T, bool ODD, bool FORCE>
 cudaError_t launch_one(const CollideArgs<T>& a, cudaStream_t s) {
     // The staged bulk copies need every row start and length 16-byte aligned:
     // population rows (nz * sizeof(T)) and voxel-word rows (nz * 4), i.e. nz % 4 == 0.
-    if (a.g.nz % 4 == 0) return launch_staged<T, ODD, FORCE>(a, s);
+    if (a.g.nz % 4 == 0) {
+        if (a.g.per[0] && a.g.per[1] && a.g.per[2]) return launch_staged<T, ODD, FORCE, true>(a, s);
+        return launch_staged<T, ODD, FORCE, false>(a, s);
+    }
     return launch_direct<T, ODD, FORCE>(a, s);
 }
 
