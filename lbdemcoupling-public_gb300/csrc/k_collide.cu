@@ -66,17 +66,31 @@ __device__ __forceinline__ void moments(const T (&f)[Q], T& rhoBar, T& jx, T& jy
     jz = ((f[12] + f[15]) + (f[17] + f[7]) + f[9]) - ((f[3] + f[6]) + (f[8] + f[16]) + f[18]);
 }
 
+// Zeroth and first moments of a cell, rhoBar = sum f̄, j = sum c f̄, with 1/rho.
+template <typename T>
+struct Mom {
+    T rhoBar, jx, jy, jz, invRho;
+};
+
+template <typename T>
+__device__ __forceinline__ Mom<T> cell_moments(const T (&f)[Q]) {
+    Mom<T> m;
+    moments(f, m.rhoBar, m.jx, m.jy, m.jz);
+    m.invRho = recip(T(1) + m.rhoBar);
+    return m;
+}
+
 // BGK relaxation towards the second-order equilibrium
 // feq_i = t_i [rhoBar + 3 c.j + invRho (4.5 (c.j)^2 - 1.5 j.j)], written per
-// opposite pair (feq_i and feq_{i+9} differ only in the sign of 3 c.j).
+// opposite pair (feq_i and feq_{i+9} differ only in the sign of 3 c.j), given
+// the cell's pre-collision moments.
 // With FORCE the Guo scheme is used (equilibrium momentum j + rho g / 2 plus
 // the forcing term t_i (1 - omega/2) rho [3 (c - u).g + 9 (c.u)(c.g)]).
 template <typename T, bool FORCE>
-__device__ __forceinline__ void bgk(T (&f)[Q], T omega, T gx, T gy, T gz) {
-    T rhoBar, jx, jy, jz;
-    moments(f, rhoBar, jx, jy, jz);
+__device__ __forceinline__ void bgk(T (&f)[Q], const Mom<T>& m, T omega, T gx, T gy, T gz) {
+    const T rhoBar = m.rhoBar, invRho = m.invRho;
+    T jx = m.jx, jy = m.jy, jz = m.jz;
     const T rho = T(1) + rhoBar;
-    const T invRho = recip(rho);
     if (FORCE) {
         const T h = T(0.5) * rho;
         jx += h * gx; jy += h * gy; jz += h * gz;
@@ -112,27 +126,30 @@ __device__ __forceinline__ void bgk(T (&f)[Q], T omega, T gx, T gy, T gz) {
     }
 }
 
-
-// PSM collision of a cell with n > 0 solid sub-cells,
-// src/ibCompositeDynamics3D.hh:130-203.  On entry f holds the pre-collision
-// populations; pre(i) returns the same pre-collision value (fPre).  n == 125 is
-// the full-solid branch (no BGK, B = 1, which reduces the weighted update to
-// fPre + bb exactly).
+// Solid correction of a cell with n > 0 solid sub-cells,
+// src/ibCompositeDynamics3D.hh:150-200.  On entry f holds the BGK
+// post-collision state (fPre itself for n == 125, where B = 1 reduces the
+// weighted update to fPre + bb exactly), m its moments, and pre(i) returns
+// the pre-collision value fPre_i.  With feq (m) and the solid equilibrium
+// feqS (rhoBar, uPart (1 + rhoBar)) written per opposite pair,
+//   bb    = B ((fPre_o - feq_o) - (fPre_i - feqS_i)) = B (D + A + S)
+//   bbOpp = B ((fPre_i - feq_i) - (fPre_o - feqS_o)) = B (A - D - S)
+// with D = fPre_o - fPre_i, A = t_i (eS - eE), S = 3 t_i (c.j + c.uP), so the
+// force term bb - bbOpp = 2 B (D + S).
 template <typename T, typename Pre>
-__device__ __forceinline__ void psm(T (&f)[Q], T up0, T up1, T up2, T B, const Pre& pre, T& Fx, T& Fy, T& Fz) {
-    // on entry f holds the BGK post-collision state (or fPre itself for n == 125)
-    T rhoBar, jx, jy, jz;
-    moments(f, rhoBar, jx, jy, jz);                  // post-collision moments, :146-148
+__device__ __forceinline__ void psm(T (&f)[Q], const Mom<T>& m, T up0, T up1, T up2, T B, const Pre& pre, T& Fx,
+                                    T& Fy, T& Fz) {
+    const T rhoBar = m.rhoBar, jx = m.jx, jy = m.jy, jz = m.jz, invRho = m.invRho;
     const T rho = T(1) + rhoBar;
-    const T invRho = recip(rho);
     const T ux = up0 * rho, uy = up1 * rho, uz = up2 * rho;   // uPart (1 + rhoBar), :154
     const T q45 = T(4.5) * invRho;
-    const T baseE = rhoBar - T(1.5) * invRho * (jx * jx + jy * jy + jz * jz);
-    const T baseS = rhoBar - T(1.5) * invRho * (ux * ux + uy * uy + uz * uz);
+    // eS - eE for c = 0: -1.5 invRho (uP^2 - j^2)
+    const T dB = T(-1.5) * invRho * ((ux * ux + uy * uy + uz * uz) - (jx * jx + jy * jy + jz * jz));
     const T omB = T(1) - B;
+    const T B2 = B + B;
     {
         const T p0 = pre(0);
-        f[0] = p0 + omB * (f[0] - p0) + B * (T(wt(0)) * baseE - T(wt(0)) * baseS);
+        f[0] = p0 + omB * (f[0] - p0) - B * (T(wt(0)) * dB);   // B (feq_0 - feqS_0)
     }
     Fx = T(0); Fy = T(0); Fz = T(0);
 #pragma unroll
@@ -141,38 +158,41 @@ __device__ __forceinline__ void psm(T (&f)[Q], T up0, T up1, T up2, T B, const P
         const T t = T(wt(i));
         const T cj = cdot(i, jx, jy, jz);
         const T cu = cdot(i, ux, uy, uz);
-        const T eE = baseE + q45 * cj * cj, sE = T(3) * cj;
-        const T eS = baseS + q45 * cu * cu, sS = T(3) * cu;
-        const T fEq_i = t * (eE + sE), fEq_o = t * (eE - sE);
-        const T fEqS_i = t * (eS + sS), fEqS_o = t * (eS - sS);
+        const T A = t * (dB + q45 * ((cu - cj) * (cu + cj)));
+        const T S = (T(3) * t) * (cj + cu);
         const T pi = pre(i), po = pre(o);
-        const T bb = B * ((po - fEq_o) - (pi - fEqS_i));
-        const T bbOpp = B * ((pi - fEq_i) - (po - fEqS_o));
+        const T D = po - pi;
+        const T bb = B * (D + A + S);
+        const T bbOpp = B * (A - D - S);
         f[i] = pi + omB * (f[i] - pi) + bb;
         f[o] = po + omB * (f[o] - po) + bbOpp;
-        const T d = bb - bbOpp;                      // F -= c_i (bb - bbOpp), :172-174
+        const T d = B2 * (D + S);                    // bb - bbOpp; F -= c_i (bb - bbOpp), :172-174
         if (cx(i) > 0) Fx -= d; else if (cx(i) < 0) Fx += d;
         if (cy(i) > 0) Fy -= d; else if (cy(i) < 0) Fy += d;
         if (cz(i) > 0) Fz -= d; else if (cz(i) < 0) Fz += d;
     }
 }
 
-// Collision of one cell given its pre-collision populations: BGK for fluid
-// cells, PSM for cells with solid sub-cells.  Returns the hydrodynamic force.
+// Collision of one cell given its pre-collision populations: BGK for every
+// cell below full coverage (src/ibCompositeDynamics3D.hh:139-140), then the
+// solid correction for cells with n > 0.  Written as two convergent blocks so
+// that a warp mixing fluid and solid cells runs the BGK once.  Without a body
+// force BGK conserves rhoBar and j, so the solid correction reuses the
+// pre-collision moments (the reference recomputes them from the post-collision
+// populations, :146-148; the two differ by rounding only); with the Guo force
+// the post-collision moments are recomputed.
 template <typename T, bool FORCE, typename Pre>
 __device__ __forceinline__ void collide_cell(const CollideArgs<T>& a, T (&f)[Q], uint32_t w, size_t c, const Pre& pre,
                                              T& Fx, T& Fy, T& Fz) {
     const int n = min((int)(w & VOX_NMASK), 125);
     Fx = T(0); Fy = T(0); Fz = T(0);
-    // BGK of the base dynamics for every cell below full coverage
-    // (src/ibCompositeDynamics3D.hh:139-140), then the solid correction.
-    // Written as two convergent blocks so that a warp mixing fluid and solid
-    // cells runs the BGK once.
-    if (n < 125) bgk<T, FORCE>(f, a.omega, a.g3[0], a.g3[1], a.g3[2]);
+    Mom<T> m = cell_moments(f);
+    if (n < 125) bgk<T, FORCE>(f, m, a.omega, a.g3[0], a.g3[1], a.g3[2]);
     if (n > 0) {
+        if (FORCE && n < 125) m = cell_moments(f);
         const size_t N = a.g.N;
         const T up0 = __ldg(a.up + c), up1 = __ldg(a.up + N + c), up2 = __ldg(a.up + 2 * N + c);
-        psm<T>(f, up0, up1, up2, __ldg(a.btab + n), pre, Fx, Fy, Fz);
+        psm<T>(f, m, up0, up1, up2, __ldg(a.btab + n), pre, Fx, Fy, Fz);
     }
 }
 
@@ -231,8 +251,24 @@ __device__ __forceinline__ int cell_force_terms(const CollideArgs<T>& a, uint32_
 // Must be reached by all 32 lanes.
 template <typename T>
 __device__ __forceinline__ void reduce_forces(const CollideArgs<T>& a, int key, T (&v)[6]) {
-    if (__ballot_sync(FULL, key >= 0) == 0u) return;
+    const unsigned solid = __ballot_sync(FULL, key >= 0);
+    if (solid == 0u) return;
     const int lane = threadIdx.x & 31;
+    const int first = __shfl_sync(FULL, key, __ffs(solid) - 1);
+    if (__all_sync(FULL, key < 0 || key == first)) {
+        // one particle in the group: butterfly sum, lane 0 adds
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1)
+#pragma unroll
+            for (int k = 0; k < 6; ++k) v[k] += __shfl_xor_sync(FULL, v[k], d);
+        if (lane == 0) {
+            double* Fp = a.ft + 3 * (size_t)first;
+            double* Tp = a.ft + 3 * (size_t)a.nslot + 3 * (size_t)first;
+            atomicAdd(Fp + 0, widen(v[0])); atomicAdd(Fp + 1, widen(v[1])); atomicAdd(Fp + 2, widen(v[2]));
+            atomicAdd(Tp + 0, widen(v[3])); atomicAdd(Tp + 1, widen(v[4])); atomicAdd(Tp + 2, widen(v[5]));
+        }
+        return;
+    }
     const int prevKey = __shfl_up_sync(FULL, key, 1);
     const bool head = (lane == 0) || (prevKey != key);
     const unsigned heads = __ballot_sync(FULL, head);
@@ -339,6 +375,7 @@ struct WarpStage {
     T f[2][Q][W];
     uint32_t vox[2][SEGW];
     long long row[2][9];   // element offset of row (x + dx, y + dy) at [3 (dx + 1) + dy + 1]; -1 beyond a wall
+    long long dst[2][Q];   // odd phase: i N + row (x + c_i) (where f_i is stored), -1 beyond an x/y wall
     int geo[2][4];         // x, y, z0, len of the segment held in buffer b
     unsigned long long bar[2];
 };
@@ -429,6 +466,10 @@ __device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, WarpStage
     const size_t N = g.N;
     const long long own = ((long long)s.x * g.ny + s.y) * g.nz;
     if (lane < 9) st.row[b][lane] = row_off(g, s, lane / 3 - 1, lane % 3 - 1);
+    if (ODD && lane < Q) {
+        const long long r = row_off(g, s, cx(lane), cy(lane));
+        st.dst[b][lane] = r >= 0 ? (long long)lane * (long long)N + r : -1;
+    }
     if (lane == 9) { st.geo[b][0] = s.x; st.geo[b][1] = s.y; st.geo[b][2] = s.z0; st.geo[b][3] = s.len; }
     const T* src = nullptr;
     void* dst = nullptr;
@@ -556,9 +597,9 @@ k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
                     const int zp = wrap_plus(z, g.nz, PER ? 1 : g.per[2]);
 #pragma unroll
                     for (int i = 1; i < Q; ++i) {
-                        const long long r = st.row[b][row_slot(cx(i), cy(i))];
+                        const long long r = st.dst[b][i];
                         const int zd = pick(cz(i), zm, z, zp);
-                        if (PER || (r >= 0 && zd >= 0)) F[(size_t)i * N + (size_t)r + zd] = f[i];
+                        if (PER || (r >= 0 && zd >= 0)) F[r + zd] = f[i];
                         else F[(size_t)opp(i) * N + c] = f[i];
                     }
                 }
