@@ -375,7 +375,6 @@ struct WarpStage {
     T f[2][Q][W];
     uint32_t vox[2][SEGW];
     long long row[2][9];   // element offset of row (x + dx, y + dy) at [3 (dx + 1) + dy + 1]; -1 beyond a wall
-    long long dst[2][Q];   // odd phase: i N + row (x + c_i) (where f_i is stored), -1 beyond an x/y wall
     int geo[2][4];         // x, y, z0, len of the segment held in buffer b
     unsigned long long bar[2];
 };
@@ -466,10 +465,7 @@ __device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, WarpStage
     const size_t N = g.N;
     const long long own = ((long long)s.x * g.ny + s.y) * g.nz;
     if (lane < 9) st.row[b][lane] = row_off(g, s, lane / 3 - 1, lane % 3 - 1);
-    if (ODD && lane < Q) {
-        const long long r = row_off(g, s, cx(lane), cy(lane));
-        st.dst[b][lane] = r >= 0 ? (long long)lane * (long long)N + r : -1;
-    }
+
     if (lane == 9) { st.geo[b][0] = s.x; st.geo[b][1] = s.y; st.geo[b][2] = s.z0; st.geo[b][3] = s.len; }
     const T* src = nullptr;
     void* dst = nullptr;
@@ -597,9 +593,9 @@ k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
                     const int zp = wrap_plus(z, g.nz, PER ? 1 : g.per[2]);
 #pragma unroll
                     for (int i = 1; i < Q; ++i) {
-                        const long long r = st.dst[b][i];
+                        const long long r = st.row[b][row_slot(cx(i), cy(i))];
                         const int zd = pick(cz(i), zm, z, zp);
-                        if (PER || (r >= 0 && zd >= 0)) F[r + zd] = f[i];
+                        if (PER || (r >= 0 && zd >= 0)) F[(size_t)i * N + (size_t)r + zd] = f[i];
                         else F[(size_t)opp(i) * N + c] = f[i];
                     }
                 }
