@@ -1,0 +1,1 @@
+// Stand-in (reference harness only).
