@@ -1,0 +1,154 @@
+// Host-side C++ surface of the GB300 PSM step in the reference's vocabulary.
+//
+// The LBDEMcoupling coupling loop (examples/sedimentingSphere/sedimentingSphere.cpp:212-238)
+//
+//     setSpheresOnLattice(lattice, wrapper, units, initVel);
+//     lattice.collideAndStream();
+//     getForcesFromLattice(lattice, wrapper, units);
+//     wrapper.run(demSubsteps);
+//
+// compiles unchanged against this header with `lattice` a plb::GpuLattice3D.
+// The particle side is read from and written to LIGGGHTS exactly as the
+// reference's wrappers do (src/ibDataExchangeWrappers3D.hh:33-246): sphere list
+// = local atoms then ghost images, excludeType filter, PhysUnits3D conversions,
+// fix arrays zeroed then accumulated through atom->map(tag), reverse
+// communication.  The wrapper and units are template parameters, so the same
+// code builds against LIGGGHTS (LiggghtsCouplingWrapper, FixLbCouplingOnetoone)
+// or against any stand-in with the same members.
+#ifndef LBDEM_PLB_H
+#define LBDEM_PLB_H
+
+#include <algorithm>
+#include <cstdint>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "lbdem_gpu.h"
+
+namespace plb {
+
+// Construction options of GpuLattice3D.
+struct GpuLatticeOptions {
+    bool periodic[3] = {false, false, false};   // Palabos lattice.periodicity().toggle(d, ...)
+    int32_t precision = LBDEM_PREC_FP64;         // LBDEM_PREC_FP32_DEV for the deviation form
+    int32_t maxParticles = 4096;                 // list capacity, ghost images included
+    int32_t maxTag = 1 << 20;
+    double maxRadius = 32.0;                     // lattice units
+    double bodyForce[3] = {0, 0, 0};             // Guo forcing (not part of the reference)
+    int32_t device = 0;
+    int32_t flags = 0;
+};
+
+// A D3Q19 PSM lattice resident on the GPU; replaces
+// MultiBlockLattice3D<T, D3Q19Descriptor> populated with
+// IBcompositeDynamics<T, D3Q19Descriptor>(new BGKdynamics(omega)).
+class GpuLattice3D {
+public:
+    using Options = GpuLatticeOptions;
+
+    GpuLattice3D(int32_t nx, int32_t ny, int32_t nz, double omega, Options const& o = Options()) {
+        lbdem_config c;
+        lbdem_config_default(&c);
+        c.nx = nx; c.ny = ny; c.nz = nz;
+        c.omega = omega;
+        for (int d = 0; d < 3; ++d) { c.periodic[d] = o.periodic[d] ? 1 : 0; c.body_force[d] = o.bodyForce[d]; }
+        c.precision = o.precision;
+        c.max_particles = o.maxParticles;
+        c.max_tag = o.maxTag;
+        c.max_radius = o.maxRadius;
+        c.device = o.device;
+        c.flags = o.flags;
+        const lbdem_status s = lbdem_create(&c, &h_);
+        if (s != LBDEM_OK) throw std::runtime_error(std::string("lbdem_create: ") + lbdem_status_string(s));
+        nx_ = nx; ny_ = ny; nz_ = nz;
+    }
+    ~GpuLattice3D() { if (h_) lbdem_destroy(h_); }
+    GpuLattice3D(GpuLattice3D const&) = delete;
+    GpuLattice3D& operator=(GpuLattice3D const&) = delete;
+
+    int32_t getNx() const { return nx_; }
+    int32_t getNy() const { return ny_; }
+    int32_t getNz() const { return nz_; }
+    lbdem_handle* handle() { return h_; }
+
+    // lattice.initialize() of a lattice at rest, or initializeAtEquilibrium with uniform rho, u.
+    void initialize(double rho = 1.0, double ux = 0, double uy = 0, double uz = 0) {
+        const double u[3] = {ux, uy, uz};
+        check(lbdem_init_equilibrium(h_, rho - 1.0, u));
+    }
+    void collideAndStream() { check(lbdem_collide_and_stream(h_)); }
+
+    void check(lbdem_status s) const {
+        if (s != LBDEM_OK)
+            throw std::runtime_error(std::string(lbdem_status_string(s)) + ": " + lbdem_last_error(h_));
+    }
+
+    // Particle list of the last setSpheresOnLattice (lattice units), kept for the force read.
+    std::vector<double> x, v, w, r, F, T;
+    std::vector<int32_t> tag;
+
+private:
+    lbdem_handle* h_ = nullptr;
+    int32_t nx_ = 0, ny_ = 0, nz_ = 0;
+};
+
+// setSpheresOnLattice, src/ibDataExchangeWrappers3D.hh:33-146.
+template <class Wrapper, class Units>
+void setSpheresOnLattice(GpuLattice3D& lattice, Wrapper& wrapper, Units const& units,
+                         std::vector<long>& excludeType, bool initVelFlag) {
+    auto* atom = wrapper.lmp->atom;
+    const long nPart = atom->nlocal + atom->nghost;
+    lattice.x.clear(); lattice.v.clear(); lattice.w.clear(); lattice.r.clear(); lattice.tag.clear();
+    for (long iS = 0; iS < nPart; ++iS) {
+        const long type = (long)atom->type[iS];
+        if (std::find(excludeType.begin(), excludeType.end(), type) != excludeType.end()) continue;
+        for (int i = 0; i < 3; ++i) {
+            lattice.x.push_back(units.getLbPosition(atom->x[iS][i]));
+            lattice.v.push_back(units.getLbVel(atom->v[iS][i]));
+            lattice.w.push_back(units.getLbFreq(atom->omega[iS][i]));
+        }
+        lattice.r.push_back(units.getLbLength(atom->radius[iS]));
+        lattice.tag.push_back((int32_t)atom->tag[iS]);
+    }
+    const int32_t n = (int32_t)lattice.r.size();
+    lattice.check(lbdem_set_particles(lattice.handle(), n, lattice.x.data(), lattice.v.data(), lattice.w.data(),
+                                      lattice.r.data(), lattice.tag.data(), initVelFlag ? 1 : 0));
+}
+
+template <class Wrapper, class Units>
+void setSpheresOnLattice(GpuLattice3D& lattice, Wrapper& wrapper, Units const& units, bool initVelFlag) {
+    std::vector<long> none;
+    setSpheresOnLattice(lattice, wrapper, units, none, initVelFlag);
+}
+
+// getForcesFromLattice, src/ibDataExchangeWrappers3D.hh:160-246.  FixType is the
+// LIGGGHTS coupling fix (LAMMPS_NS::FixLbCouplingOnetoone).
+template <class FixType, class Wrapper, class Units>
+void getForcesFromLattice(GpuLattice3D& lattice, Wrapper& wrapper, Units const& units) {
+    auto* atom = wrapper.lmp->atom;
+    const long nPart = atom->nlocal + atom->nghost;
+    if (nPart == 0) return;   // no particles - no work (:174)
+    const int32_t n = (int32_t)lattice.r.size();
+    lattice.F.assign(3 * (size_t)n, 0.0);
+    lattice.T.assign(3 * (size_t)n, 0.0);
+    lattice.check(lbdem_get_forces(lattice.handle(), n, lattice.F.data(), lattice.T.data()));
+    FixType* couplingFix = dynamic_cast<FixType*>(wrapper.lmp->modify->find_fix_style("couple/lb/onetoone", 0));
+    if (!couplingFix) throw std::runtime_error("getForcesFromLattice: fix couple/lb/onetoone not found");
+    double** f_liggghts = couplingFix->get_force_ptr();
+    double** t_liggghts = couplingFix->get_torque_ptr();
+    for (long iPart = 0; iPart < nPart; ++iPart)
+        for (int j = 0; j < 3; ++j) { f_liggghts[iPart][j] = 0; t_liggghts[iPart][j] = 0; }
+    for (int32_t k = 0; k < n; ++k) {
+        const int ind = atom->map(lattice.tag[k]);
+        for (int j = 0; j < 3; ++j) {
+            f_liggghts[ind][j] += units.getPhysForce(lattice.F[3 * (size_t)k + j]);
+            t_liggghts[ind][j] += units.getPhysTorque(lattice.T[3 * (size_t)k + j]);
+        }
+    }
+    couplingFix->comm_force_torque();
+}
+
+}  // namespace plb
+
+#endif  // LBDEM_PLB_H
