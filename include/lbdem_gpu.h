@@ -179,6 +179,50 @@ lbdem_status lbdem_device_bytes(lbdem_handle* h, size_t* bytes);
  * library; memset/memcpy not counted). */
 lbdem_status lbdem_get_launch_count(lbdem_handle* h, int64_t* count);
 
+/* ---- Periodic pressure drop and initial profiles ---------------------------
+ * Boxes are Palabos Box3D: {x0, x1, y0, y1, z0, z1}, inclusive. */
+
+/* Palabos computeAverageDensity(lattice, box) = 1 + mean rhoBar over the box.
+ * Synchronizes. */
+lbdem_status lbdem_average_density(lbdem_handle* h, const int32_t box[6], double* rho);
+
+/* ZhangPeriodicPressureFunctional3D(rho_target, rho_avg, dimension, direction)
+ * applied on box: f_i + t_i <- (f_i + t_i) rho_target / rho_avg for the
+ * populations with c_i[dimension] == direction
+ * (src/periodicPressureFunctionals3D.hh:121-159). */
+lbdem_status lbdem_zhang_rescale(lbdem_handle* h, const int32_t box[6], int32_t dimension,
+                                 int32_t direction, double rho_target, double rho_avg);
+
+/* The pressure-driven periodic channel of examples/showcaseRectChannel
+ * (showcaseRectChannel.cpp:253-273) done inside every lbdem_collide_and_stream:
+ * the inlet and outlet average densities are those of the state before the
+ * step, and after streaming the inlet populations with c[dimension] ==
+ * in_direction are rescaled towards rho_in with the outlet average, the outlet
+ * populations with c[dimension] == out_direction towards rho_out with the inlet
+ * average.  One fused plane launch per step, no host synchronization. */
+typedef struct {
+    int32_t dimension;        /* 0 = x, 1 = y, 2 = z */
+    int32_t inlet[6];         /* Box3D */
+    int32_t outlet[6];        /* Box3D, disjoint from the inlet */
+    int32_t in_direction;     /* +1 in the reference */
+    int32_t out_direction;    /* -1 in the reference */
+    double rho_in, rho_out;   /* rhoHi, rhoLo */
+} lbdem_pressure_drop;
+
+/* NULL switches the pressure drop off. */
+lbdem_status lbdem_set_pressure_drop(lbdem_handle* h, const lbdem_pressure_drop* drop);
+
+/* Equilibrium initial profiles (Palabos initializeAtEquilibrium over the whole
+ * lattice with the reference's functors, src/periodicPressureFunctionals3D.hh):
+ *   LBDEM_PROFILE_PRESSURE_GRADIENT: PressureGradient(rho_hi, rho_lo, n[dimension], dimension)
+ *   LBDEM_PROFILE_POISEUILLE: PoiseuilleProfileAndPressureGradient(rho_hi, rho_lo, u_max,
+ *                             n[0], n[1], n[2], dimension)
+ * density = rho_hi - (rho_hi - rho_lo) i / (n - 1) along dimension; the Poiseuille
+ * velocity u_max (1 - a^2)(1 - b^2), a = (i - n/2) / (n/2) in each other direction. */
+typedef enum { LBDEM_PROFILE_PRESSURE_GRADIENT = 0, LBDEM_PROFILE_POISEUILLE = 1 } lbdem_profile;
+lbdem_status lbdem_init_profile(lbdem_handle* h, int32_t kind, double rho_hi, double rho_lo,
+                                double u_max, const int32_t n[3], int32_t dimension);
+
 /* ---- Voxelization that allocates nothing ---------------------------------
  * No counterpart in the reference.  For callers that cannot have a library
  * allocate device memory: an application that gives the whole GPU to its own

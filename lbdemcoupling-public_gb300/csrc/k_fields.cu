@@ -7,20 +7,6 @@
 namespace lbdem {
 namespace {
 
-// Index of the slot that holds population i of cell (x,y,z) in the AA layout.
-// phase 0 (even number of completed steps): slot (i, x).
-// phase 1: slot (opp i, x - c_i), or (i, x) when x - c_i is beyond a wall.
-__device__ __forceinline__ size_t slot_index(int i, int x, int y, int z, int phase, const Geom& g) {
-    if (phase == 0 || i == 0) return (size_t)i * g.N + ((size_t)x * g.ny + y) * g.nz + z;
-    int X = x - cx(i), Y = y - cy(i), Z = z - cz(i);
-    bool out = false;
-    if (X < 0 || X >= g.nx) { if (g.per[0]) X = X < 0 ? X + g.nx : X - g.nx; else out = true; }
-    if (Y < 0 || Y >= g.ny) { if (g.per[1]) Y = Y < 0 ? Y + g.ny : Y - g.ny; else out = true; }
-    if (Z < 0 || Z >= g.nz) { if (g.per[2]) Z = Z < 0 ? Z + g.nz : Z - g.nz; else out = true; }
-    if (out) return (size_t)i * g.N + ((size_t)x * g.ny + y) * g.nz + z;
-    return (size_t)opp(i) * g.N + ((size_t)X * g.ny + Y) * g.nz + Z;
-}
-
 __device__ __forceinline__ void decompose(size_t c, const Geom& g, int& x, int& y, int& z) {
     z = (int)(c % g.nz);
     const size_t r = c / g.nz;

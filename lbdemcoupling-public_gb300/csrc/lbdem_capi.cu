@@ -3,6 +3,7 @@
 #include "lbdem_gpu.h"
 #include "lbdem_internal.h"
 
+#include <algorithm>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -45,6 +46,18 @@ struct lbdem_handle {
     unsigned* h_err = nullptr;
     cudaEvent_t ev_staged = nullptr;
     bool staged_pending = false;
+
+    // periodic pressure drop: plane jobs 0 (inlet) and 1 (outlet) of the fused
+    // mode, job 2 for the single-box calls; average slots [2 parities][4]:
+    // 0 inlet, 1 outlet, 2 single-box result, 3 single-box given average
+    PlaneJob* d_jobs = nullptr;
+    double* d_pavg = nullptr;
+    double* d_ppart = nullptr;  // [3][PLANE_BLOCKS_MAX]
+    unsigned* d_pcount = nullptr; // [3]
+    double* h_pavg = nullptr;   // pinned
+    bool pdrop_on = false;
+    bool pavg_valid = false;
+    int pdrop_bpj = 1;
 
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
@@ -100,10 +113,11 @@ cudaError_t dalloc(lbdem_handle* h, P** p, size_t bytes) {
 
 void release(lbdem_handle* h) {
     void* dev[] = {h->f, h->vox, h->up, h->cf, h->btab, h->btabf, h->d_rec, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot,
-                   h->d_tile_cnt, h->d_bins, h->d_ft, h->d_err, h->d_mass, h->scratch};
+                   h->d_tile_cnt, h->d_bins, h->d_ft, h->d_err, h->d_mass, h->scratch, h->d_jobs, h->d_pavg,
+                   h->d_ppart, h->d_pcount};
     for (void* p : dev)
         if (p) cudaFree(p);
-    void* host[] = {h->h_rec, h->h_ft, h->h_err};
+    void* host[] = {h->h_rec, h->h_ft, h->h_err, h->h_pavg};
     for (void* p : host)
         if (p) cudaFreeHost(p);
     if (h->ev_staged) cudaEventDestroy(h->ev_staged);
@@ -147,9 +161,48 @@ lbdem_status voxelize(lbdem_handle* h, int n, int init_vel) {
             CK(h, launch_voxelize<float>(h->d_sph, h->d_fast, n, h->d_tile_cnt, h->d_bins, h->ntiles, h->vox,
                                          (float*)h->up, (float*)h->f, init_vel, phase, h->g, h->d_err, s));
         h->launches += 3;
+        if (init_vel) h->pavg_valid = false;
     }
     h->n_cur = n;
     return LBDEM_OK;
+}
+
+bool box_ok(const lbdem_handle* h, const int32_t* b) {
+    const int ext[3] = {h->g.nx, h->g.ny, h->g.nz};
+    for (int d = 0; d < 3; ++d)
+        if (b[2 * d] < 0 || b[2 * d + 1] >= ext[d] || b[2 * d] > b[2 * d + 1]) return false;
+    return true;
+}
+
+long long box_cells(const int32_t* b) {
+    return (long long)(b[1] - b[0] + 1) * (b[3] - b[2] + 1) * (b[5] - b[4] + 1);
+}
+
+int plane_blocks(long long cells) {
+    long long b = (cells + 2 * PLANE_THREADS - 1) / (2 * PLANE_THREADS);
+    return (int)std::max(1LL, std::min<long long>(b, PLANE_BLOCKS_MAX));
+}
+
+PlaneJob make_job(const lbdem_handle* h, const int32_t* box, int dim, int dir, double target, int read, int write) {
+    PlaneJob j;
+    j.f = h->f;
+    j.g = h->g;
+    for (int k = 0; k < 6; ++k) j.box[k] = box[k];
+    j.dim = dim;
+    j.dir = dir;
+    j.target = target;
+    j.read = read;
+    j.write = write;
+    return j;
+}
+
+cudaError_t plane_launch(lbdem_handle* h, const PlaneJob* jobs, int njobs, int bpj, int phase, int rescale,
+                         const double* avg_in, double* avg_out) {
+    if (h->prec == LBDEM_PREC_FP64)
+        return launch_plane_pressure<double>(jobs, njobs, bpj, phase, rescale, avg_in, avg_out, h->d_ppart,
+                                             h->d_pcount, h->stream);
+    return launch_plane_pressure<float>(jobs, njobs, bpj, phase, rescale, avg_in, avg_out, h->d_ppart, h->d_pcount,
+                                        h->stream);
 }
 
 }  // namespace
@@ -266,6 +319,13 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     TRY(cudaMallocHost((void**)&h->h_rec, capn * REC_STRIDE * sizeof(double)));
     TRY(cudaMallocHost((void**)&h->h_ft, 6 * capn * sizeof(double)));
     TRY(cudaMallocHost((void**)&h->h_err, sizeof(unsigned)));
+    TRY(dalloc(h, &h->d_jobs, 3 * sizeof(PlaneJob)));
+    TRY(dalloc(h, &h->d_pavg, 8 * sizeof(double)));
+    TRY(dalloc(h, &h->d_ppart, 3 * PLANE_BLOCKS_MAX * sizeof(double)));
+    TRY(dalloc(h, &h->d_pcount, 3 * sizeof(unsigned)));
+    TRY(cudaMemset(h->d_pcount, 0, 3 * sizeof(unsigned)));
+    TRY(cudaMemset(h->d_pavg, 0, 8 * sizeof(double)));
+    TRY(cudaMallocHost((void**)&h->h_pavg, sizeof(double)));
 
     // B(n) = sf ooo / ((1 - sf) + ooo), sf = n/125, ooo = 1/omega - 1/2
     // (src/ibCompositeDynamics3D.hh:178-179); n = 125 is the full-solid branch, B = 1.
@@ -327,6 +387,7 @@ lbdem_status lbdem_init_equilibrium(lbdem_handle* h, double rho_bar, const doubl
     if (h->prec == LBDEM_PREC_FP64) CK(h, launch_fill_equilibrium<double>((double*)h->f, rho_bar, u, h->g, h->stream));
     else CK(h, launch_fill_equilibrium<float>((float*)h->f, rho_bar, u, h->g, h->stream));
     h->launches += 1;
+    h->pavg_valid = false;
     return LBDEM_OK;
 }
 
@@ -346,6 +407,7 @@ lbdem_status lbdem_set_populations(lbdem_handle* h, const void* host_f) {
         h->launches += 1;
     }
     CK(h, cudaStreamSynchronize(h->stream));
+    h->pavg_valid = false;
     return LBDEM_OK;
 }
 
@@ -399,6 +461,12 @@ lbdem_status lbdem_collide_and_stream(lbdem_handle* h) {
     if (n > 0) CK(h, cudaMemsetAsync(h->d_ft, 0, 6 * (size_t)n * sizeof(double), h->stream));
     const bool odd = (h->step & 1) != 0;
     const bool force = h->cfg.body_force[0] != 0.0 || h->cfg.body_force[1] != 0.0 || h->cfg.body_force[2] != 0.0;
+    const int P = odd ? 1 : 0;
+    if (h->pdrop_on && !h->pavg_valid) {
+        // averages of the state before the step (computeAverageDensity before collideAndStream)
+        CK(h, plane_launch(h, h->d_jobs, 2, h->pdrop_bpj, P, 0, nullptr, h->d_pavg + 4 * P));
+        h->launches += 1;
+    }
     if (h->prec == LBDEM_PREC_FP64) {
         CollideArgs<double> a;
         a.g = h->g; a.f = (double*)h->f; a.vox = h->vox; a.up = (const double*)h->up; a.cf = (double*)h->cf;
@@ -415,6 +483,13 @@ lbdem_status lbdem_collide_and_stream(lbdem_handle* h) {
         CK(h, launch_collide_stream<float>(a, odd, force, h->stream));
     }
     h->launches += 1;
+    if (h->pdrop_on) {
+        // rescale of the streamed populations with the pre-step averages; the same
+        // pass leaves the averages of the new state for the next step
+        CK(h, plane_launch(h, h->d_jobs, 2, h->pdrop_bpj, P ^ 1, 1, h->d_pavg + 4 * P, h->d_pavg + 4 * (P ^ 1)));
+        h->launches += 1;
+        h->pavg_valid = true;
+    }
     h->step += 1;
     return LBDEM_OK;
 }
@@ -561,6 +636,98 @@ lbdem_status lbdem_device_bytes(lbdem_handle* h, size_t* bytes) {
 lbdem_status lbdem_get_launch_count(lbdem_handle* h, int64_t* count) {
     if (!h || !count) return LBDEM_ERR_INVALID_ARG;
     *count = h->launches;
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_average_density(lbdem_handle* h, const int32_t box[6], double* rho) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    if (!box || !rho) return fail(h, LBDEM_ERR_INVALID_ARG, "average_density: null argument");
+    if (!box_ok(h, box)) return fail(h, LBDEM_ERR_INVALID_ARG, "average_density: box outside the lattice or empty");
+    DeviceGuard dg(h->device);
+    const PlaneJob j = make_job(h, box, 0, 0, 1.0, 2, 2);
+    CK(h, cudaMemcpyAsync(h->d_jobs + 2, &j, sizeof(j), cudaMemcpyHostToDevice, h->stream));
+    CK(h, plane_launch(h, h->d_jobs + 2, 1, plane_blocks(box_cells(box)), (int)(h->step & 1), 0, nullptr, h->d_pavg));
+    h->launches += 1;
+    CK(h, cudaMemcpyAsync(h->h_pavg, h->d_pavg + 2, sizeof(double), cudaMemcpyDeviceToHost, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    *rho = *h->h_pavg;
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_zhang_rescale(lbdem_handle* h, const int32_t box[6], int32_t dimension, int32_t direction,
+                                 double rho_target, double rho_avg) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    if (!box || !box_ok(h, box)) return fail(h, LBDEM_ERR_INVALID_ARG, "zhang_rescale: box outside the lattice or empty");
+    if (dimension < 0 || dimension > 2 || (direction != 1 && direction != -1))
+        return fail(h, LBDEM_ERR_INVALID_ARG, "zhang_rescale: dimension must be 0..2 and direction +-1");
+    if (!(rho_target > 0.0) || !(rho_avg > 0.0) || !std::isfinite(rho_target) || !std::isfinite(rho_avg))
+        return fail(h, LBDEM_ERR_INVALID_ARG, "zhang_rescale: densities must be positive and finite");
+    DeviceGuard dg(h->device);
+    const PlaneJob j = make_job(h, box, dimension, direction, rho_target, 3, 2);
+    CK(h, cudaMemcpyAsync(h->d_jobs + 2, &j, sizeof(j), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->d_pavg + 3, &rho_avg, sizeof(double), cudaMemcpyHostToDevice, h->stream));
+    CK(h, plane_launch(h, h->d_jobs + 2, 1, plane_blocks(box_cells(box)), (int)(h->step & 1), 1, h->d_pavg,
+                       h->d_pavg));
+    h->launches += 1;
+    CK(h, cudaStreamSynchronize(h->stream));   // the host-side source of the copies is the caller's stack
+    h->pavg_valid = false;
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_set_pressure_drop(lbdem_handle* h, const lbdem_pressure_drop* d) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    if (!d) {
+        h->pdrop_on = false;
+        return LBDEM_OK;
+    }
+    if (d->dimension < 0 || d->dimension > 2) return fail(h, LBDEM_ERR_INVALID_ARG, "pressure_drop: dimension");
+    if (!box_ok(h, d->inlet) || !box_ok(h, d->outlet))
+        return fail(h, LBDEM_ERR_INVALID_ARG, "pressure_drop: box outside the lattice or empty");
+    bool overlap = true;
+    for (int k = 0; k < 3; ++k)
+        if (d->inlet[2 * k + 1] < d->outlet[2 * k] || d->outlet[2 * k + 1] < d->inlet[2 * k]) overlap = false;
+    if (overlap) return fail(h, LBDEM_ERR_INVALID_ARG, "pressure_drop: inlet and outlet boxes overlap");
+    if ((d->in_direction != 1 && d->in_direction != -1) || (d->out_direction != 1 && d->out_direction != -1))
+        return fail(h, LBDEM_ERR_INVALID_ARG, "pressure_drop: directions must be +-1");
+    if (!(d->rho_in > 0.0) || !(d->rho_out > 0.0) || !std::isfinite(d->rho_in) || !std::isfinite(d->rho_out))
+        return fail(h, LBDEM_ERR_INVALID_ARG, "pressure_drop: densities must be positive and finite");
+    DeviceGuard dg(h->device);
+    PlaneJob j[2] = {make_job(h, d->inlet, d->dimension, d->in_direction, d->rho_in, 1, 0),
+                     make_job(h, d->outlet, d->dimension, d->out_direction, d->rho_out, 0, 1)};
+    CK(h, cudaMemcpyAsync(h->d_jobs, j, sizeof(j), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->pdrop_bpj = plane_blocks(std::max(box_cells(d->inlet), box_cells(d->outlet)));
+    h->pdrop_on = true;
+    h->pavg_valid = false;
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_init_profile(lbdem_handle* h, int32_t kind, double rho_hi, double rho_lo, double u_max,
+                                const int32_t n[3], int32_t dimension) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    if (!n || (kind != LBDEM_PROFILE_PRESSURE_GRADIENT && kind != LBDEM_PROFILE_POISEUILLE) || dimension < 0 ||
+        dimension > 2)
+        return fail(h, LBDEM_ERR_INVALID_ARG, "init_profile: kind, dimension or n");
+    if (n[dimension] < 2) return fail(h, LBDEM_ERR_INVALID_ARG, "init_profile: n[dimension] < 2");
+    if (kind == LBDEM_PROFILE_POISEUILLE)
+        for (int d = 0; d < 3; ++d)
+            if (n[d] < 1) return fail(h, LBDEM_ERR_INVALID_ARG, "init_profile: n < 1");
+    if (!std::isfinite(rho_hi) || !std::isfinite(rho_lo) || !std::isfinite(u_max))
+        return fail(h, LBDEM_ERR_INVALID_ARG, "init_profile: non-finite parameter");
+    const int ext[3] = {h->g.nx, h->g.ny, h->g.nz};
+    const double slope = (rho_hi - rho_lo) / (double)(n[dimension] - 1);
+    if (!(rho_hi > 0.0) || !(rho_hi - slope * (ext[dimension] - 1) > 0.0))
+        return fail(h, LBDEM_ERR_INVALID_ARG, "init_profile: density not positive on the lattice");
+    DeviceGuard dg(h->device);
+    const int phase = (int)(h->step & 1);
+    if (h->prec == LBDEM_PREC_FP64)
+        CK(h, launch_init_profile<double>((double*)h->f, phase, kind, rho_hi, rho_lo, u_max, n[0], n[1], n[2],
+                                          dimension, h->g, h->stream));
+    else
+        CK(h, launch_init_profile<float>((float*)h->f, phase, kind, rho_hi, rho_lo, u_max, n[0], n[1], n[2],
+                                         dimension, h->g, h->stream));
+    h->launches += 1;
+    h->pavg_valid = false;
     return LBDEM_OK;
 }
 

@@ -45,6 +45,20 @@ struct Geom {
     size_t N;
 };
 
+// Index of the slot that holds population i of cell (x,y,z) in the AA layout.
+// phase 0 (even number of completed steps): slot (i, x).
+// phase 1: slot (opp i, x - c_i), or (i, x) when x - c_i is beyond a wall.
+__device__ __forceinline__ size_t slot_index(int i, int x, int y, int z, int phase, const Geom& g) {
+    if (phase == 0 || i == 0) return (size_t)i * g.N + ((size_t)x * g.ny + y) * g.nz + z;
+    int X = x - cx(i), Y = y - cy(i), Z = z - cz(i);
+    bool out = false;
+    if (X < 0 || X >= g.nx) { if (g.per[0]) X = X < 0 ? X + g.nx : X - g.nx; else out = true; }
+    if (Y < 0 || Y >= g.ny) { if (g.per[1]) Y = Y < 0 ? Y + g.ny : Y - g.ny; else out = true; }
+    if (Z < 0 || Z >= g.nz) { if (g.per[2]) Z = Z < 0 ? Z + g.nz : Z - g.nz; else out = true; }
+    if (out) return (size_t)i * g.N + ((size_t)x * g.ny + y) * g.nz + z;
+    return (size_t)opp(i) * g.N + ((size_t)X * g.ny + Y) * g.nz + Z;
+}
+
 // Arguments of one collide-stream launch.
 template <typename T>
 struct CollideArgs {
@@ -113,5 +127,32 @@ template <typename T>
 cudaError_t launch_mass(const T* f, double* out, Geom g, cudaStream_t s);
 cudaError_t launch_vox_fields(const uint32_t* vox, double* sf, int32_t* id, uint8_t* nsub, Geom g,
                               cudaStream_t s);
+
+// One plane (box) of the periodic pressure drop: average density of the box and,
+// optionally, the Zhang rescale of the populations entering it.
+struct PlaneJob {
+    void* f;                 // populations of the domain the box lies in
+    Geom g;
+    int box[6];              // x0, x1, y0, y1, z0, z1 (inclusive)
+    int dim, dir;            // rescaled populations: c_i[dim] == dir
+    double target;           // target density of the box
+    int read;                // average slot giving rhoAvg of the rescale
+    int write;               // average slot receiving this box's average
+};
+constexpr int PLANE_BLOCKS_MAX = 64;    // blocks per job (partial sums per job)
+constexpr int PLANE_THREADS = 256;
+
+// jobs: device table; partial: [njobs][PLANE_BLOCKS_MAX]; count: [njobs], zero on
+// entry and left zero; avg_in / avg_out: average slots before / after.  rescale = 0
+// only computes the averages (into avg_out).
+template <typename T>
+cudaError_t launch_plane_pressure(const PlaneJob* jobs, int njobs, int blocks_per_job, int phase, int rescale,
+                                  const double* avg_in, double* avg_out, double* partial, unsigned* count,
+                                  cudaStream_t s);
+// Equilibrium initial profiles, src/periodicPressureFunctionals3D.hh:242-298:
+// kind 0 pressure gradient, kind 1 Poiseuille profile plus pressure gradient.
+template <typename T>
+cudaError_t launch_init_profile(T* f, int phase, int kind, double p_hi, double p_lo, double u_max, int n0, int n1,
+                                int n2, int dim, Geom g, cudaStream_t s);
 
 }  // namespace lbdem

@@ -57,6 +57,15 @@ class Config(C.Structure):
                 ("reserved", C.c_int32)]
 
 
+class PressureDrop(C.Structure):
+    _fields_ = [("dimension", C.c_int32), ("inlet", C.c_int32 * 6), ("outlet", C.c_int32 * 6),
+                ("in_direction", C.c_int32), ("out_direction", C.c_int32),
+                ("rho_in", C.c_double), ("rho_out", C.c_double)]
+
+
+PROFILE_PRESSURE_GRADIENT = 0
+PROFILE_POISEUILLE = 1
+
 SIGNATURES = {
     "lbdem_config_default": (None, [C.POINTER(Config)]),
     "lbdem_create": (C.c_int, [C.POINTER(Config), C.POINTER(_P)]),
@@ -81,6 +90,10 @@ SIGNATURES = {
     "lbdem_device_bytes": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
     "lbdem_get_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
     "lbdem_voxelize_static": (C.c_int, [_I, _I, _I, _I, _I, _P, _P, _P, _P, _P]),
+    "lbdem_average_density": (C.c_int, [_P, C.POINTER(_I), _D]),
+    "lbdem_zhang_rescale": (C.c_int, [_P, C.POINTER(_I), _I, _I, C.c_double, C.c_double]),
+    "lbdem_set_pressure_drop": (C.c_int, [_P, C.POINTER(PressureDrop)]),
+    "lbdem_init_profile": (C.c_int, [_P, _I, C.c_double, C.c_double, C.c_double, C.POINTER(_I), _I]),
 }
 
 # Limits of lbdem_voxelize_static (include/lbdem_gpu.h).
@@ -293,6 +306,38 @@ class Lattice:
 
     def set_stream(self, stream_ptr: int | None):
         self._check(self.lib.lbdem_set_stream(self.h, _P(stream_ptr) if stream_ptr else None))
+
+    # -- periodic pressure drop and initial profiles -----------------------
+    def average_density(self, box) -> float:
+        b = (_I * 6)(*[int(v) for v in box])
+        out = C.c_double()
+        self._check(self.lib.lbdem_average_density(self.h, b, C.byref(out)))
+        return float(out.value)
+
+    def zhang_rescale(self, box, dimension, direction, rho_target, rho_avg):
+        b = (_I * 6)(*[int(v) for v in box])
+        self._check(self.lib.lbdem_zhang_rescale(self.h, b, int(dimension), int(direction), float(rho_target),
+                                                 float(rho_avg)))
+
+    def set_pressure_drop(self, dimension=None, inlet=None, outlet=None, rho_in=1.0, rho_out=1.0,
+                          in_direction=1, out_direction=-1):
+        """Fused Zhang pressure drop in every collide_and_stream; dimension None switches it off."""
+        if dimension is None:
+            self._check(self.lib.lbdem_set_pressure_drop(self.h, None))
+            return
+        d = PressureDrop()
+        d.dimension = int(dimension)
+        for k in range(6):
+            d.inlet[k] = int(inlet[k])
+            d.outlet[k] = int(outlet[k])
+        d.in_direction, d.out_direction = int(in_direction), int(out_direction)
+        d.rho_in, d.rho_out = float(rho_in), float(rho_out)
+        self._check(self.lib.lbdem_set_pressure_drop(self.h, C.byref(d)))
+
+    def init_profile(self, kind, rho_hi, rho_lo, u_max, n, dimension):
+        nn = (_I * 3)(*[int(v) for v in n])
+        self._check(self.lib.lbdem_init_profile(self.h, int(kind), float(rho_hi), float(rho_lo), float(u_max), nn,
+                                                int(dimension)))
 
 
 def pack_records(x, v, w, r, tag) -> np.ndarray:

@@ -383,6 +383,73 @@ long sum_force_torque(const Lattice<T>& L, int n, const double* x, const int32_t
     return unmapped;
 }
 
+// ---- periodic pressure drop and initial profiles (src/periodicPressureFunctionals3D.hh) ----
+//
+// box = {x0, x1, y0, y1, z0, z1}, inclusive, as Palabos' Box3D.
+
+// Palabos computeAverageDensity(lattice, box): fullRho(sum rhoBar / nCells), with
+// fullRho(rhoBar) = 1 + rhoBar for D3Q19; the sum runs in the reference's cell
+// order (x outer, z inner), rhoBar of a cell summed over i = 0..18.
+template <class T>
+double average_density(const Lattice<T>& L, const int32_t b[6]) {
+    double s = 0;
+    for (int x = b[0]; x <= b[1]; ++x)
+        for (int y = b[2]; y <= b[3]; ++y)
+            for (int z = b[4]; z <= b[5]; ++z) {
+                double rb = 0;
+                for (int i = 0; i < Q; ++i) rb += (double)L.f[i * L.N + L.idx(x, y, z)];
+                s += rb;
+            }
+    const double n = (double)(b[1] - b[0] + 1) * (double)(b[3] - b[2] + 1) * (double)(b[5] - b[4] + 1);
+    return 1.0 + s / n;
+}
+
+// ZhangPeriodicPressureFunctional3D (src/periodicPressureFunctionals3D.hh:121-159):
+// the populations with c_i[dimension] == direction are rescaled as
+// f_i + t_i <- (f_i + t_i) * rhoTarget / rhoAvg.  The float lattice evaluates the
+// same expression in double and rounds once.
+template <class T>
+void zhang_rescale(Lattice<T>& L, const int32_t b[6], int dim, int dir, double rhoTarget, double rhoAvg) {
+    const double k = rhoTarget / rhoAvg;                              // :140
+    for (int x = b[0]; x <= b[1]; ++x)
+        for (int y = b[2]; y <= b[3]; ++y)
+            for (int z = b[4]; z <= b[5]; ++z)
+                for (int i = 0; i < Q; ++i) {
+                    if (C[i][dim] != dir) continue;                   // rescalePop, :126-130
+                    T& f = L.f[i * L.N + L.idx(x, y, z)];
+                    double t = (double)f + W[i];                       // :151-153
+                    t *= k;
+                    f = (T)(t - W[i]);
+                }
+}
+
+// PressureGradient (kind 0, :242-256) and PoiseuilleProfileAndPressureGradient
+// (kind 1, :267-298) applied through Palabos initializeAtEquilibrium: every cell
+// gets feq(rhoBar = density - 1, j = density u).  n[3] are the functor's grid
+// sizes (PressureGradient uses n[dimension]).
+template <class T>
+void init_profile(Lattice<T>& L, int kind, double pHi, double pLo, double uMax, const int32_t n[3], int dim) {
+    auto pv = [](double i, double nn) {                              // poiseuilleVelocity, :293-298
+        double nHalf = nn / 2.;
+        double x = (i - nHalf) / nHalf;
+        return 1. - x * x;
+    };
+    for (int x = 0; x < L.nx; ++x)
+        for (int y = 0; y < L.ny; ++y)
+            for (int z = 0; z < L.nz; ++z) {
+                const int ii[3] = {x, y, z};
+                double density = pHi - (pHi - pLo) * (double)ii[dim] / (double)(n[dim] - 1);
+                double u[3] = {0, 0, 0};
+                if (kind == 1) {
+                    const int a = dim == 0 ? 1 : 0, c = dim == 2 ? 1 : 2;
+                    u[dim] = uMax * pv((double)ii[a], (double)n[a]) * pv((double)ii[c], (double)n[c]);
+                }
+                T e[Q];
+                equilibrium_pops<T>(e, density - 1.0, u);
+                for (int i = 0; i < Q; ++i) L.f[i * L.N + L.idx(x, y, z)] = e[i];
+            }
+}
+
 template <class T>
 Lattice<T>* make(int nx, int ny, int nz, const int per[3], double omega, const double g[3], int nth) {
     auto* L = new Lattice<T>();
@@ -457,6 +524,20 @@ long orc_sum_force_torque(void* h, int n, const double* x, const int32_t* tag, d
     long r = 0;
     DISPATCH(h, r = sum_force_torque(L, n, x, tag, F, Tq));
     return r;
+}
+
+double orc_average_density(void* h, const int32_t* box) {
+    double r = 0;
+    DISPATCH(h, r = average_density(L, box));
+    return r;
+}
+
+void orc_zhang_rescale(void* h, const int32_t* box, int dim, int dir, double rhoTarget, double rhoAvg) {
+    DISPATCH(h, zhang_rescale(L, box, dim, dir, rhoTarget, rhoAvg));
+}
+
+void orc_init_profile(void* h, int kind, double pHi, double pLo, double uMax, const int32_t* n, int dim) {
+    DISPATCH(h, init_profile(L, kind, pHi, pLo, uMax, n, dim));
 }
 
 // Per-cell coupling state.  Any pointer may be null.  sf: double[N];

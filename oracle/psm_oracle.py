@@ -42,6 +42,10 @@ def load():
         lib.orc_cycle.restype = C.c_long
         lib.orc_cycle.argtypes = [C.c_void_p, C.c_int, _D, _D, _D, _D, _I, C.c_int, _D, _D]
         lib.orc_has_openmp.restype = C.c_int
+        lib.orc_average_density.restype = C.c_double
+        lib.orc_average_density.argtypes = [C.c_void_p, _I]
+        lib.orc_zhang_rescale.argtypes = [C.c_void_p, _I, C.c_int, C.c_int, C.c_double, C.c_double]
+        lib.orc_init_profile.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, _I, C.c_int]
         _lib = lib
     return _lib
 
@@ -83,6 +87,20 @@ class OracleLattice:
         out = np.empty((19, *self.shape), dtype=self.dtype)
         self.lib.orc_get_pops(self.h, out.ctypes.data_as(C.c_void_p))
         return out
+
+    def average_density(self, box):
+        b = np.ascontiguousarray(box, dtype=np.int32).reshape(6)
+        return self.lib.orc_average_density(self.h, b.ctypes.data_as(_I))
+
+    def zhang_rescale(self, box, dimension, direction, rho_target, rho_avg):
+        b = np.ascontiguousarray(box, dtype=np.int32).reshape(6)
+        self.lib.orc_zhang_rescale(self.h, b.ctypes.data_as(_I), int(dimension), int(direction), float(rho_target),
+                                   float(rho_avg))
+
+    def init_profile(self, kind, rho_hi, rho_lo, u_max, n, dimension):
+        nn = np.ascontiguousarray(n, dtype=np.int32).reshape(3)
+        self.lib.orc_init_profile(self.h, int(kind), float(rho_hi), float(rho_lo), float(u_max),
+                                  nn.ctypes.data_as(_I), int(dimension))
 
     def set_particles(self, x, v, w, r, tag, init_vel=False):
         x = np.ascontiguousarray(x, dtype=np.float64).reshape(-1, 3)
