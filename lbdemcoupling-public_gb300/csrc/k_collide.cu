@@ -15,15 +15,15 @@
 // is replaced by the cell itself with the direction reversed: half-way
 // bounce-back.  Periodic axes wrap.
 //
-// Two kernels implement the step:
-//  * k_collide_staged (nz a multiple of 16 bytes of populations): persistent
-//    CTAs of 128 threads walk 128-cell z-segments.  The 19 population rows of
-//    a segment (plus one 16-byte halo chunk per c_z != 0 direction in the odd
-//    phase, and the voxel words) are copied into shared memory with
-//    cp.async.bulk on an mbarrier, double-buffered, so the next segment's
-//    bytes are in flight while the current one is collided.  The staged
-//    pre-collision values double as fPre of the PSM update.
-//  * k_collide_direct (any nz): one thread per cell, direct global loads.
+// One kernel implements the step: persistent CTAs of 128 threads whose warps
+// walk 64-cell z-segments.  The 19 population rows of a segment (plus, in the
+// odd phase, the halo element of every c_z != 0 direction) and the voxel words
+// are copied into shared memory with cp.async.bulk on an mbarrier,
+// double-buffered, so the next segment's bytes are in flight while the current
+// one is collided.  The staged pre-collision values double as fPre of the PSM
+// update.  Rows that are not 16-byte aligned (nz % 4 != 0) are copied in whole
+// 16-byte chunks around the row.  The same kernel steps many independent
+// domains in one launch (batch mode).
 #include "lbdem_internal.h"
 
 namespace lbdem {
@@ -296,71 +296,6 @@ __device__ __forceinline__ int wrap_plus(int v, int n, int per) { return v < n -
 __device__ __forceinline__ int pick(int c, int m, int v, int p) { return c < 0 ? m : (c > 0 ? p : v); }
 
 // ---------------------------------------------------------------------------
-// Direct kernel: one thread per cell, grid (nx * ny, ceil(nz / 128)).
-template <typename T, bool ODD, bool FORCE>
-__global__ void __launch_bounds__(COLLIDE_BLOCK)
-k_collide_direct(const CollideArgs<T> a) {
-    const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
-    const size_t N = a.g.N;
-    const int row = blockIdx.x;
-    const int x = row / ny;
-    const int y = row - x * ny;
-    const int z = blockIdx.y * COLLIDE_BLOCK + threadIdx.x;
-    const bool valid = z < nz;
-    const size_t c = ((size_t)x * ny + y) * nz + (valid ? z : 0);
-    T* __restrict__ F = a.f;
-
-    int key = -1;
-    T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-    if (valid) {
-        int xm = 0, xp = 0, ym = 0, yp = 0, zm = 0, zp = 0;
-        if (ODD) {
-            xm = wrap_minus(x, nx, a.g.per[0]); xp = wrap_plus(x, nx, a.g.per[0]);
-            ym = wrap_minus(y, ny, a.g.per[1]); yp = wrap_plus(y, ny, a.g.per[1]);
-            zm = wrap_minus(z, nz, a.g.per[2]); zp = wrap_plus(z, nz, a.g.per[2]);
-        }
-        auto nb = [&](int i) -> long long {
-            const int X = pick(cx(i), xm, x, xp), Y = pick(cy(i), ym, y, yp), Z = pick(cz(i), zm, z, zp);
-            if (X < 0 || Y < 0 || Z < 0) return -1;
-            return ((long long)X * ny + Y) * nz + Z;
-        };
-        T f[Q];
-        if (!ODD) {
-#pragma unroll
-            for (int i = 0; i < Q; ++i) f[i] = F[(size_t)i * N + c];
-        } else {
-            f[0] = F[c];
-#pragma unroll
-            for (int i = 1; i < Q; ++i) {
-                const long long s = nb(opp(i));
-                f[i] = s >= 0 ? F[(size_t)opp(i) * N + (size_t)s] : F[(size_t)i * N + c];
-            }
-        }
-        T fPre[Q];
-#pragma unroll
-        for (int i = 0; i < Q; ++i) fPre[i] = f[i];
-        const uint32_t w = __ldg(a.vox + c);
-        T Fx, Fy, Fz;
-        collide_cell<T, FORCE>(a, f, w, c, [&](int i) { return fPre[i]; }, Fx, Fy, Fz);
-        if (!ODD) {
-#pragma unroll
-            for (int i = 0; i < Q; ++i) F[(size_t)opp(i) * N + c] = f[i];
-        } else {
-            F[c] = f[0];
-#pragma unroll
-            for (int i = 1; i < Q; ++i) {
-                const long long d = nb(i);
-                if (d >= 0) F[(size_t)i * N + (size_t)d] = f[i];
-                else F[(size_t)opp(i) * N + c] = f[i];
-            }
-        }
-        if (a.cf) { a.cf[c] = Fx; a.cf[N + c] = Fy; a.cf[2 * N + c] = Fz; }
-        key = cell_force_terms(a, w, x, y, z, Fx, Fy, Fz, v);
-    }
-    reduce_forces(a, key, v);
-}
-
-// ---------------------------------------------------------------------------
 // Staged persistent kernel: every warp runs its own double-buffered pipeline
 // over SEGW-cell z-segments (no block-wide barriers, so a warp with solid
 // cells does not hold up the others).
@@ -371,11 +306,12 @@ constexpr int WAIT_LIMIT = 1 << 22;         // bounded mbarrier wait (iterations
 template <typename T>
 struct WarpStage {
     static constexpr int V = 16 / (int)sizeof(T);   // elements per 16 bytes
-    static constexpr int W = SEGW + 2 * V;          // row: V halo | SEGW core | V halo
+    static constexpr int W = SEGW + 2 * V;          // row: V halo | (lead) SEGW core | V halo
     T f[2][Q][W];
-    uint32_t vox[2][SEGW];
+    uint32_t vox[2][SEGW + 4];
     long long row[2][9];   // element offset of row (x + dx, y + dy) at [3 (dx + 1) + dy + 1]; -1 beyond a wall
-    int geo[2][4];         // x, y, z0, len of the segment held in buffer b
+    int geo[2][8];         // x, y, z0, len, domain of the segment held in buffer b
+    unsigned long long lead[2];   // unaligned rows: lead elements of row i at bits 2i, voxel row at bits 38
     unsigned long long bar[2];
 };
 
@@ -451,13 +387,20 @@ __device__ __forceinline__ long long row_off(const Geom& g, const SegGeo& s, int
 // Issued by one warp for its segment into buffer b:
 //   lanes 0..18:  population rows (even: own row, slot i; odd: row x - c_i,
 //                 slot opp i, or own row slot i when that row is beyond a wall);
-//   lanes 19..28: odd phase, the 16-byte chunk holding the halo element of the
-//                 (lane-19)-th c_z != 0 direction (none beyond a z wall);
+//   lanes 19..28: odd phase, aligned rows: the 16-byte chunk holding the halo
+//                 element of the (lane-19)-th c_z != 0 direction (none beyond a z wall);
 //   lane 29:      voxel words of the segment.
+// MIS (rows not 16-byte aligned, nz % 4 != 0): each row copy starts at the
+// 16-byte boundary below the row and is rounded up to whole chunks (the
+// allocations carry 64 bytes of tail padding); the lead of every row is
+// published in st.lead.  The odd-phase halo elements are then read by lanes
+// 0..9 with plain loads and returned, to be put in place once the copy has
+// landed: the cell that reads and writes such a slot in this step lies in
+// this segment, so no other warp touches it meanwhile.
 // Lanes 0..9 also publish the segment geometry for the compute pass.
-template <typename T, bool ODD>
-__device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, WarpStage<T>& st, int b, long long seg,
-                                              int nzseg) {
+template <typename T, bool ODD, bool MIS>
+__device__ __forceinline__ T issue_segment(const CollideArgs<T>& a, WarpStage<T>& st, int b, long long seg,
+                                           int nzseg, int dom) {
     constexpr int V = WarpStage<T>::V;
     const int lane = threadIdx.x & 31;
     const Geom& g = a.g;
@@ -466,10 +409,14 @@ __device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, WarpStage
     const long long own = ((long long)s.x * g.ny + s.y) * g.nz;
     if (lane < 9) st.row[b][lane] = row_off(g, s, lane / 3 - 1, lane % 3 - 1);
 
-    if (lane == 9) { st.geo[b][0] = s.x; st.geo[b][1] = s.y; st.geo[b][2] = s.z0; st.geo[b][3] = s.len; }
+    if (lane == 9) {
+        st.geo[b][0] = s.x; st.geo[b][1] = s.y; st.geo[b][2] = s.z0; st.geo[b][3] = s.len; st.geo[b][4] = dom;
+    }
     const T* src = nullptr;
     void* dst = nullptr;
     uint32_t bytes = 0;
+    uint32_t lead = 0;
+    T halo = T(0);
     if (lane < Q) {
         const int i = lane;
         size_t off = (size_t)i * N + (size_t)own + s.z0;
@@ -479,8 +426,14 @@ __device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, WarpStage
         }
         src = a.f + off;
         dst = &st.f[b][i][V];
-        bytes = (uint32_t)(s.len * sizeof(T));
-    } else if (ODD && lane < Q + 10) {
+        if (MIS) {
+            lead = (uint32_t)(((uintptr_t)src & 15u) / sizeof(T));
+            src -= lead;
+            bytes = (uint32_t)(((lead + (uint32_t)s.len + V - 1) / V) * 16u);
+        } else {
+            bytes = (uint32_t)(s.len * sizeof(T));
+        }
+    } else if (ODD && !MIS && lane < Q + 10) {
         const int i = zdir(lane - Q);
         const long long r = row_off(g, s, -cx(i), -cy(i));
         if (r >= 0) {
@@ -500,28 +453,58 @@ __device__ __forceinline__ void issue_segment(const CollideArgs<T>& a, WarpStage
             }
         }
     } else if (lane == Q + 10) {
-        src = reinterpret_cast<const T*>(a.vox + own + s.z0);
+        const uint32_t* vs = a.vox + own + s.z0;
+        if (MIS) {
+            lead = (uint32_t)(((uintptr_t)vs & 15u) / 4u);
+            vs -= lead;
+            bytes = ((lead + (uint32_t)s.len + 3u) / 4u) * 16u;
+        } else {
+            bytes = (uint32_t)(s.len * sizeof(uint32_t));
+        }
+        src = reinterpret_cast<const T*>(vs);
         dst = &st.vox[b][0];
-        bytes = (uint32_t)(s.len * sizeof(uint32_t));
+    }
+    if (MIS) {
+        const uint32_t lo = __reduce_or_sync(FULL, lane < 16 ? lead << (2 * lane) : 0u);
+        const uint32_t hi = __reduce_or_sync(
+            FULL, (lane >= 16 && lane < Q) ? lead << (2 * (lane - 16)) : (lane == Q + 10 ? lead << 6 : 0u));
+        if (lane == 0) st.lead[b] = (unsigned long long)lo | ((unsigned long long)hi << 32);
+        if (ODD && lane < 10) {
+            const int i = zdir(lane);
+            const long long r = row_off(g, s, -cx(i), -cy(i));
+            if (r >= 0) {
+                if (cz(i) > 0) {
+                    const int zs = s.z0 > 0 ? s.z0 - 1 : (g.per[2] ? g.nz - 1 : -1);
+                    halo = zs >= 0 ? a.f[(size_t)opp(i) * N + (size_t)r + zs] : a.f[(size_t)i * N + (size_t)own];
+                } else {
+                    const int ze = s.z0 + s.len;
+                    const int zs = ze < g.nz ? ze : (g.per[2] ? 0 : -1);
+                    halo = zs >= 0 ? a.f[(size_t)opp(i) * N + (size_t)r + zs]
+                                   : a.f[(size_t)i * N + (size_t)own + g.nz - 1];
+                }
+            }
+        }
     }
     const uint32_t total = __reduce_add_sync(FULL, bytes);
     if (lane == 0) mbar_arrive_expect_tx(&st.bar[b], total);
     __syncwarp();
     if (bytes) bulk_g2s(dst, src, bytes, &st.bar[b]);
+    return halo;
 }
 
 // PER: every axis periodic (no wall cases; shifts and neighbour rows are fixed).
-template <typename T, bool ODD, bool FORCE, bool PER>
-__global__ void __launch_bounds__(COLLIDE_BLOCK)
-k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
+// MIS: rows not 16-byte aligned (see issue_segment).
+// BATCH: segments of many domains, numbered domain after domain (seg0[d] is
+// the first segment of domain d); every domain has its own CollideArgs.
+template <typename T, bool ODD, bool FORCE, bool PER, bool MIS, bool BATCH>
+__global__ void __launch_bounds__(COLLIDE_BLOCK, sizeof(T) == 4 ? 4 : 2)
+k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const CollideArgs<T>* __restrict__ dargs,
+                 const int* __restrict__ seg0, int ndom) {
     constexpr int V = WarpStage<T>::V;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     WarpStage<T>& st = reinterpret_cast<WarpStage<T>*>(smem_raw)[warp];
-    const Geom& g = a.g;
-    const size_t N = g.N;
-    T* __restrict__ F = a.f;
     if (lane == 0) {
         mbar_init(&st.bar[0], 1);
         mbar_init(&st.bar[1], 1);
@@ -531,25 +514,50 @@ k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
     const long long stride = (long long)gridDim.x * WARPS;
     long long seg = (long long)blockIdx.x * WARPS + warp;
     if (seg >= nseg) return;
-    issue_segment<T, ODD>(a, st, 0, seg, nzseg);
+    auto issue = [&](int buf, long long sg) -> T {
+        if (BATCH) {
+            const int d = find_domain(seg0, ndom, (int)sg);
+            const CollideArgs<T>& A = dargs[d];
+            return issue_segment<T, ODD, MIS>(A, st, buf, sg - __ldg(seg0 + d), (A.g.nz + SEGW - 1) / SEGW, d);
+        }
+        return issue_segment<T, ODD, MIS>(a1, st, buf, sg, nzseg1, 0);
+    };
+    T hcur = issue(0, seg);
     uint32_t phase = 0;   // bit b: parity expected next on buffer b
     int b = 0;
     for (; seg < nseg; seg += stride, b ^= 1) {
         const long long next = seg + stride;
-        if (next < nseg) issue_segment<T, ODD>(a, st, b ^ 1, next, nzseg);
+        T hnext = T(0);
+        if (next < nseg) hnext = issue(b ^ 1, next);
         const bool ok = mbar_wait(&st.bar[b], (phase >> b) & 1u);
         phase ^= 1u << b;
         if (__any_sync(FULL, !ok)) {
             // a copy did not land: report, let in-flight copies finish, leave
-            if (lane == 0) atomicOr(a.err, 0x20u);   // LBDEM_DEVERR_TIMEOUT
+            if (lane == 0) atomicOr(BATCH ? dargs[0].err : a1.err, 0x20u);   // LBDEM_DEVERR_TIMEOUT
             if (next < nseg) mbar_wait(&st.bar[b ^ 1], (phase >> (b ^ 1)) & 1u);
             return;
         }
         const int sx = st.geo[b][0], sy = st.geo[b][1], z0 = st.geo[b][2], len = st.geo[b][3];
+        const CollideArgs<T>& a = BATCH ? dargs[st.geo[b][4]] : a1;
+        const Geom& g = a.g;
+        const size_t N = g.N;
+        T* __restrict__ F = a.f;
         const size_t own = (size_t)st.row[b][row_slot(0, 0)];
-        // Odd phase with walls along z: the halo element of an edge cell is its
-        // own slot i (half-way bounce-back).
-        if (ODD && !PER && !g.per[2] && (z0 == 0 || z0 + len == g.nz)) {
+        const unsigned long long lead = MIS ? st.lead[b] : 0ull;
+        if (MIS && ODD) {
+            if (lane < 10) {
+                const int i = zdir(lane);
+                if (st.row[b][row_slot(-cx(i), -cy(i))] >= 0) {
+                    const int m = (int)((lead >> (2 * i)) & 3u);
+                    if (cz(i) > 0) st.f[b][i][V + m - 1] = hcur;
+                    else st.f[b][i][V + m + len] = hcur;
+                }
+            }
+            __syncwarp();
+        }
+        // Odd phase with walls along z, aligned rows: the halo element of an edge
+        // cell is its own slot i (half-way bounce-back).
+        if (!MIS && ODD && !PER && !g.per[2] && (z0 == 0 || z0 + len == g.nz)) {
             if (lane < 10) {
                 const int i = zdir(lane);
                 if (st.row[b][row_slot(-cx(i), -cy(i))] >= 0) {
@@ -565,6 +573,7 @@ k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
             for (int i = 1; i < Q; ++i)
                 if (cz(i) != 0 && st.row[b][row_slot(-cx(i), -cy(i))] >= 0) srcrow |= 1u << i;
         }
+        const int vlead = MIS ? (int)((lead >> 38) & 3u) : 0;
 #pragma unroll 1
         for (int j = lane; j < SEGW; j += 32) {
             int key = -1;
@@ -572,16 +581,17 @@ k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
             if (j < len) {
                 const int z = z0 + j;
                 const size_t c = own + z;
-                // smem index of direction i: V + j - shift_i, shift_i = c_z,i when
-                // the source row x - c_i exists (odd phase)
+                // smem index of direction i: V + lead_i + j - shift_i, shift_i = c_z,i
+                // when the source row x - c_i exists (odd phase)
                 auto at = [&](int i) -> const T& {
                     const int shift = (ODD && cz(i) != 0 && (PER || ((srcrow >> i) & 1u))) ? cz(i) : 0;
-                    return st.f[b][i][V + j - shift];
+                    const int m = MIS ? (int)((lead >> (2 * i)) & 3u) : 0;
+                    return st.f[b][i][V + m + j - shift];
                 };
                 T f[Q];
 #pragma unroll
                 for (int i = 0; i < Q; ++i) f[i] = at(i);
-                const uint32_t w = st.vox[b][j];
+                const uint32_t w = st.vox[b][vlead + j];
                 T Fx, Fy, Fz;
                 collide_cell<T, FORCE>(a, f, w, c, [&](int i) { return at(i); }, Fx, Fy, Fz);
                 if (!ODD) {
@@ -605,18 +615,13 @@ k_collide_staged(const CollideArgs<T> a, int nzseg, long long nseg) {
             reduce_forces(a, key, v);
         }
         __syncwarp();   // buffer b is free for the segment after next
+        hcur = hnext;
     }
 }
 
-template <typename T, bool ODD, bool FORCE>
-cudaError_t launch_direct(const CollideArgs<T>& a, cudaStream_t s) {
-    dim3 grid((unsigned)((size_t)a.g.nx * a.g.ny), (unsigned)((a.g.nz + COLLIDE_BLOCK - 1) / COLLIDE_BLOCK));
-    k_collide_direct<T, ODD, FORCE><<<grid, COLLIDE_BLOCK, 0, s>>>(a);
-    return cudaGetLastError();
-}
-
-template <typename T, bool ODD, bool FORCE, bool PER>
-cudaError_t launch_staged(const CollideArgs<T>& a, cudaStream_t s) {
+template <typename T, bool ODD, bool FORCE, bool PER, bool MIS, bool BATCH>
+cudaError_t launch_staged(const CollideArgs<T>& a, int nzseg, long long nseg, const CollideArgs<T>* dargs,
+                          const int* seg0, int ndom, int blocks_per_sm, cudaStream_t s) {
     constexpr size_t smem = WARPS * sizeof(WarpStage<T>);
     static int per_sm = 0, sms = 0;
     if (per_sm == 0) {
@@ -624,32 +629,42 @@ cudaError_t launch_staged(const CollideArgs<T>& a, cudaStream_t s) {
         cudaError_t e = cudaGetDevice(&dev);
         if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_collide_staged<T, ODD, FORCE, PER>,
+            e = cudaFuncSetAttribute(k_collide_staged<T, ODD, FORCE, PER, MIS, BATCH>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collide_staged<T, ODD, FORCE, PER>,
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_collide_staged<T, ODD, FORCE, PER, MIS, BATCH>,
                                                               COLLIDE_BLOCK, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
     }
-    const int nzseg = (a.g.nz + SEGW - 1) / SEGW;
-    const long long nseg = (long long)a.g.nx * a.g.ny * nzseg;
-    const long long want = (long long)sms * per_sm;
+    if (nseg <= 0) return cudaSuccess;
+    const int use = (blocks_per_sm > 0 && blocks_per_sm < per_sm) ? blocks_per_sm : per_sm;
+    const long long want = (long long)sms * use;
     const long long blocks = (nseg + WARPS - 1) / WARPS;
     const unsigned grid = (unsigned)(blocks < want ? blocks : want);
-    k_collide_staged<T, ODD, FORCE, PER><<<grid, COLLIDE_BLOCK, smem, s>>>(a, nzseg, nseg);
+    k_collide_staged<T, ODD, FORCE, PER, MIS, BATCH><<<grid, COLLIDE_BLOCK, smem, s>>>(a, nzseg, nseg, dargs, seg0, ndom);
     return cudaGetLastError();
 }
 
 template <typename T, bool ODD, bool FORCE>
 cudaError_t launch_one(const CollideArgs<T>& a, cudaStream_t s) {
-    // The staged bulk copies need every row start and length 16-byte aligned:
+    const int nzseg = (a.g.nz + SEGW - 1) / SEGW;
+    const long long nseg = (long long)a.g.nx * a.g.ny * nzseg;
+    // Aligned bulk copies need every row start and length 16-byte aligned:
     // population rows (nz * sizeof(T)) and voxel-word rows (nz * 4), i.e. nz % 4 == 0.
     if (a.g.nz % 4 == 0) {
-        if (a.g.per[0] && a.g.per[1] && a.g.per[2]) return launch_staged<T, ODD, FORCE, true>(a, s);
-        return launch_staged<T, ODD, FORCE, false>(a, s);
+        if (a.g.per[0] && a.g.per[1] && a.g.per[2])
+            return launch_staged<T, ODD, FORCE, true, false, false>(a, nzseg, nseg, nullptr, nullptr, 0, 0, s);
+        return launch_staged<T, ODD, FORCE, false, false, false>(a, nzseg, nseg, nullptr, nullptr, 0, 0, s);
     }
-    return launch_direct<T, ODD, FORCE>(a, s);
+    return launch_staged<T, ODD, FORCE, false, true, false>(a, nzseg, nseg, nullptr, nullptr, 0, 0, s);
+}
+
+template <typename T, bool ODD, bool FORCE>
+cudaError_t launch_batch(const CollideArgs<T>* dargs, const int* seg0, int ndom, long long nseg, int blocks_per_sm,
+                         cudaStream_t s) {
+    CollideArgs<T> none{};
+    return launch_staged<T, ODD, FORCE, false, true, true>(none, 1, nseg, dargs, seg0, ndom, blocks_per_sm, s);
 }
 
 }  // namespace
@@ -660,7 +675,21 @@ cudaError_t launch_collide_stream(const CollideArgs<T>& a, bool odd, bool force,
     return force ? launch_one<T, false, true>(a, s) : launch_one<T, false, false>(a, s);
 }
 
+template <typename T>
+cudaError_t launch_collide_batch(const CollideArgs<T>* dargs, const int* seg0, int ndom, long long nseg, bool odd,
+                                 bool force, int blocks_per_sm, cudaStream_t s) {
+    if (odd)
+        return force ? launch_batch<T, true, true>(dargs, seg0, ndom, nseg, blocks_per_sm, s)
+                     : launch_batch<T, true, false>(dargs, seg0, ndom, nseg, blocks_per_sm, s);
+    return force ? launch_batch<T, false, true>(dargs, seg0, ndom, nseg, blocks_per_sm, s)
+                 : launch_batch<T, false, false>(dargs, seg0, ndom, nseg, blocks_per_sm, s);
+}
+
 template cudaError_t launch_collide_stream<float>(const CollideArgs<float>&, bool, bool, cudaStream_t);
 template cudaError_t launch_collide_stream<double>(const CollideArgs<double>&, bool, bool, cudaStream_t);
+template cudaError_t launch_collide_batch<float>(const CollideArgs<float>*, const int*, int, long long, bool, bool,
+                                                 int, cudaStream_t);
+template cudaError_t launch_collide_batch<double>(const CollideArgs<double>*, const int*, int, long long, bool, bool,
+                                                  int, cudaStream_t);
 
 }  // namespace lbdem

@@ -252,7 +252,7 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     if (!std::isfinite(c.body_force[0]) || !std::isfinite(c.body_force[1]) || !std::isfinite(c.body_force[2]))
         return LBDEM_ERR_INVALID_ARG;
     const size_t N = (size_t)c.nx * c.ny * c.nz;
-    if ((size_t)c.nx * c.ny > 0x7fffffffu || c.nz > 65535 * COLLIDE_BLOCK) return LBDEM_ERR_INVALID_ARG;
+    if ((size_t)c.nx * c.ny > 0x7fffffffu) return LBDEM_ERR_INVALID_ARG;
     // cell coordinates must be exact in float (voxelization filter, float torque arm)
     if (c.nx >= (1 << 24) || c.ny >= (1 << 24) || c.nz >= (1 << 24)) return LBDEM_ERR_INVALID_ARG;
 
@@ -298,8 +298,8 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     TRY(cudaStreamCreateWithFlags(&h->own_stream, cudaStreamNonBlocking));
     h->stream = h->own_stream;
     TRY(cudaEventCreateWithFlags(&h->ev_staged, cudaEventDisableTiming));
-    TRY(dalloc(h, &h->f, (size_t)Q * N * h->esz));
-    TRY(dalloc(h, &h->vox, N * sizeof(uint32_t)));
+    TRY(dalloc(h, &h->f, (size_t)Q * N * h->esz + ALLOC_TAIL));
+    TRY(dalloc(h, &h->vox, N * sizeof(uint32_t) + ALLOC_TAIL));
     TRY(dalloc(h, &h->up, 3 * N * h->esz));
     if (c.flags & LBDEM_FLAG_CELL_FORCE) TRY(dalloc(h, &h->cf, 3 * N * h->esz));
     TRY(dalloc(h, &h->btab, 126 * sizeof(double)));

@@ -100,9 +100,30 @@ struct SphereFast {
 };
 static_assert(sizeof(SphereFast) == 96, "SphereFast is staged as 24 words");
 
+// Largest d in [0, n) with off[d] <= idx (off ascending, off[0] <= idx).
+__device__ __forceinline__ int find_domain(const int* __restrict__ off, int n, int idx) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (__ldg(off + mid) <= idx) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// Population and voxel-word allocations carry this many bytes past their end:
+// the staged collide kernel copies whole 16-byte chunks around unaligned rows.
+constexpr size_t ALLOC_TAIL = 64;
+
 // Launchers (return cudaGetLastError() of the launch).
 template <typename T>
 cudaError_t launch_collide_stream(const CollideArgs<T>& a, bool odd, bool force, cudaStream_t s);
+// Many domains in one persistent launch: dargs[d] describes domain d, its
+// segments (rows of nz cells cut into 64-cell pieces, x-major) are numbered
+// from seg0[d]; nseg segments in all.  blocks_per_sm <= 0: as many as fit.
+template <typename T>
+cudaError_t launch_collide_batch(const CollideArgs<T>* dargs, const int* seg0, int ndom, long long nseg, bool odd,
+                                 bool force, int blocks_per_sm, cudaStream_t s);
 
 cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
                                    int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,

@@ -22,9 +22,12 @@ CASES = {
     "channel_force": ((20, 24, 18), (1, 0, 1), 1 / 0.55, 4, 2.5, 4.5, False, (1e-5, 0.0, 2e-6)),
     "closed_box": ((16, 18, 40), (0, 0, 0), 1 / 0.6, 2, 4.0, 5.0, False, (0.0, 0.0, 0.0)),
     "tiny_radius": ((13, 11, 9), (1, 1, 1), 1.7, 5, 0.6, 1.6, True, (0.0, 0.0, 0.0)),
-    # z-rows longer than one 128-cell staged segment, last segment partial
+    # z-rows longer than one 64-cell staged segment, last segment partial
     "long_z_walls": ((6, 7, 200), (0, 1, 0), 1 / 0.6, 6, 1.5, 2.5, True, (0.0, 0.0, 1e-5)),
     "long_z_periodic": ((5, 6, 264), (1, 1, 1), 1 / 0.55, 6, 1.5, 2.4, True, (0.0, 0.0, 0.0)),
+    # rows not 16-byte aligned (nz % 4 != 0): z walls, and rows of several segments
+    "odd_z_walls": ((12, 10, 37), (1, 1, 0), 1 / 0.6, 4, 2.0, 3.5, True, (0.0, 0.0, 0.0)),
+    "odd_long_z": ((5, 6, 133), (0, 1, 1), 1 / 0.55, 6, 1.5, 2.4, True, (2e-6, 0.0, 0.0)),
 }
 
 
