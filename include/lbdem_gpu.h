@@ -257,6 +257,85 @@ lbdem_status lbdem_voxelize_static(int32_t nx, int32_t ny, int32_t nz, int32_t p
                                    const double* dev_rec, uint32_t* dev_vox, void* dev_up, uint32_t* dev_err,
                                    void* cuda_stream);
 
+/* ---- Batched independent domains ------------------------------------------
+ * No counterpart in the reference, which couples one lattice per process.
+ * Many independent lattices of uneven size -- each with its own extent,
+ * periodicity, omega, body force, particle list and optional periodic pressure
+ * drop -- step together: each voxelization stage, the collide-stream pass and
+ * the pressure-drop planes are one launch over all domains.  The device part of
+ * a cycle (upload of the staged particle table, voxelization, collide-stream,
+ * planes, download of the forces) is captured once per streaming phase into a
+ * CUDA graph and replayed.  Every domain behaves exactly as an lbdem_handle
+ * with the same configuration fed the same calls. */
+typedef struct lbdem_batch lbdem_batch;
+
+typedef struct {
+    int32_t nx, ny, nz;
+    int32_t periodic[3];
+    double omega;
+    double body_force[3];
+    int32_t max_particles;          /* list capacity of this domain, ghost images included */
+    int32_t has_pressure_drop;      /* 1: `drop` is applied in every step */
+    lbdem_pressure_drop drop;
+} lbdem_domain;
+
+typedef struct {
+    int32_t precision;              /* lbdem_precision, shared by all domains */
+    int32_t device;
+    int32_t max_tag;                /* tags 1..max_tag within every domain */
+    double max_radius;
+    int32_t use_graph;              /* 1: replay the device part of a cycle as a CUDA graph */
+    int32_t autotune;               /* 1: time the collide-stream grid shapes on the first step */
+    int32_t reserved[2];
+} lbdem_batch_config;
+
+void lbdem_batch_config_default(lbdem_batch_config* cfg);
+lbdem_status lbdem_batch_create(const lbdem_batch_config* cfg, int32_t ndomains, const lbdem_domain* domains,
+                                lbdem_batch** out);
+lbdem_status lbdem_batch_destroy(lbdem_batch* b);
+const char* lbdem_batch_last_error(const lbdem_batch* b);
+
+/* Uniform equilibrium in every domain (as lbdem_init_equilibrium). */
+lbdem_status lbdem_batch_init_equilibrium(lbdem_batch* b, double rho_bar, const double u[3]);
+/* lbdem_init_profile on one domain. */
+lbdem_status lbdem_batch_init_profile(lbdem_batch* b, int32_t domain, int32_t kind, double rho_hi, double rho_lo,
+                                      double u_max, const int32_t n[3], int32_t dimension);
+
+/* Stages the particles of every domain: counts[d] records for domain d, the
+ * records of all domains back to back in domain order, [sum counts][12] doubles
+ * as for lbdem_set_particles_device (host memory).  init_vel as for
+ * lbdem_set_particles.  The table is uploaded by the next lbdem_batch_step. */
+lbdem_status lbdem_batch_set_particles(lbdem_batch* b, const int32_t* counts, const double* rec, int32_t init_vel);
+
+/* One coupling step of every domain: voxelization of the staged particles,
+ * collide-stream with the force/torque sums, pressure-drop planes.  Queued,
+ * not synchronized. */
+lbdem_status lbdem_batch_step(lbdem_batch* b);
+
+/* Forces and torques of the last step, [sum counts][3] each, indexed like the
+ * staged records (per domain as lbdem_get_forces).  Synchronizes; returns
+ * LBDEM_ERR_DEVICE if the device error word is set. */
+lbdem_status lbdem_batch_get_forces(lbdem_batch* b, double* force, double* torque);
+
+/* set_particles + step + get_forces. */
+lbdem_status lbdem_batch_cycle(lbdem_batch* b, const int32_t* counts, const double* rec, int32_t init_vel,
+                               double* force, double* torque);
+
+/* Field of one domain (lbdem_field), host memory. */
+lbdem_status lbdem_batch_get_field(lbdem_batch* b, int32_t domain, int32_t which, void* host_buf);
+
+lbdem_status lbdem_batch_synchronize(lbdem_batch* b);
+lbdem_status lbdem_batch_get_step(lbdem_batch* b, int64_t* step);
+lbdem_status lbdem_batch_get_launch_count(lbdem_batch* b, int64_t* count);
+lbdem_status lbdem_batch_device_bytes(lbdem_batch* b, size_t* bytes);
+/* Total cells of all domains. */
+lbdem_status lbdem_batch_cells(lbdem_batch* b, int64_t* cells);
+
+/* Launch shape of the collide-stream pass: CTAs per SM of the persistent grid
+ * (0: as many as fit).  Set by the autotuner or by hand. */
+lbdem_status lbdem_batch_get_tuning(lbdem_batch* b, int32_t* collide_blocks_per_sm, float* collide_ms);
+lbdem_status lbdem_batch_set_tuning(lbdem_batch* b, int32_t collide_blocks_per_sm);
+
 #ifdef __cplusplus
 }
 #endif

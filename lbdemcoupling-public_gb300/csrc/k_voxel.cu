@@ -59,12 +59,24 @@ __device__ __forceinline__ int tiles_along(int n) { return (n + TILE - 1) / TILE
 // (src/ibDataExchangeWrappers3D.hh:127-133), thresholds, the float split of
 // the centre, and the tag -> lowest list index map (LAMMPS atom->map keeps the
 // owned atom, which precedes its ghost images).
+// BATCH: slot i belongs to the domain d with soff[d] <= i; slots past the
+// domain's particle count are skipped; the map stores domain-local slots.
+template <bool BATCH>
 __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereDev* __restrict__ sph,
                                   SphereFast* __restrict__ fast, float* __restrict__ xpf,
                                   int* __restrict__ tag2slot, unsigned* __restrict__ err, Geom g, int max_tag,
-                                  double max_radius) {
+                                  double max_radius, const DomView* __restrict__ doms, const int* __restrict__ soff,
+                                  int ndom, const int* __restrict__ ncur) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    int il = i;
+    if (BATCH) {
+        const int d = find_domain(soff, ndom, i);
+        il = i - __ldg(soff + d);
+        if (il >= __ldg(ncur + d)) return;
+        g = doms[d].g;
+        tag2slot += doms[d].tag0;
+    }
     const double* p = rec + (size_t)i * REC_STRIDE;
     SphereDev s;
     SphereFast q;
@@ -122,17 +134,29 @@ __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereD
     float* xp = xpf + (size_t)i * 8;
     xp[0] = q.xh[0]; xp[1] = q.xh[1]; xp[2] = q.xh[2]; xp[3] = q.xl[0];
     xp[4] = q.xl[1]; xp[5] = q.xl[2]; xp[6] = 0.f; xp[7] = 0.f;
-    if (s.tag >= 1) atomicMin(tag2slot + s.tag, i);
+    if (s.tag >= 1) atomicMin(tag2slot + s.tag, il);
 }
 
 // One warp per sphere, lanes stride over the tiles its box overlaps and
 // append the sphere to each tile's bin (entries past TILE_BIN are dropped; the
-// voxelization of such a tile re-collects its spheres).
+// voxelization of such a tile re-collects its spheres).  The first sphere of a
+// tile also appends the tile to the work list.
+template <bool BATCH>
 __global__ void k_bin_spheres(const SphereFast* __restrict__ fast, int n, int* __restrict__ tile_cnt,
-                              int* __restrict__ bins, Geom g) {
+                              int* __restrict__ bins, int* __restrict__ work, int* __restrict__ work_n, Geom g,
+                              const DomView* __restrict__ doms, const int* __restrict__ soff, int ndom,
+                              const int* __restrict__ ncur) {
     const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
     if (i >= n) return;
+    int il = i, t0 = 0;
+    if (BATCH) {
+        const int d = find_domain(soff, ndom, i);
+        il = i - __ldg(soff + d);
+        if (il >= __ldg(ncur + d)) return;
+        g = doms[d].g;
+        t0 = doms[d].t0;
+    }
     const SphereFast& q = fast[i];
     if (q.lo[0] > q.hi[0] || q.lo[1] > q.hi[1] || q.lo[2] > q.hi[2]) return;
     const int tx0 = q.lo[0] / TILE, ty0 = q.lo[1] / TILE, tz0 = q.lo[2] / TILE;
@@ -142,9 +166,10 @@ __global__ void k_bin_spheres(const SphereFast* __restrict__ fast, int n, int* _
     for (int k = lane; k < total; k += 32) {
         const int kz = k % ez, kr = k / ez;
         const int ky = kr % ey, kx = kr / ey;
-        const size_t t = ((size_t)(tx0 + kx) * tny + (ty0 + ky)) * tnz + (tz0 + kz);
+        const size_t t = (size_t)t0 + ((size_t)(tx0 + kx) * tny + (ty0 + ky)) * tnz + (tz0 + kz);
         const int pos = atomicAdd(tile_cnt + t, 1);
-        if (pos < TILE_BIN) bins[t * TILE_BIN + pos] = i;
+        if (pos == 0) work[atomicAdd(work_n, 1)] = (int)t;
+        if (pos < TILE_BIN) bins[t * TILE_BIN + pos] = il;
     }
 }
 
@@ -280,14 +305,12 @@ __device__ __forceinline__ void set_n(uint32_t* row, int l, uint32_t n) {
 // (src/ibProcessors3D.hh:107-108); it depends only on that uPart, so the last
 // such sphere decides the populations written.
 template <typename T, bool INIT_VEL>
-__global__ void __launch_bounds__(VOX_THREADS, 4)   // 4 blocks per SM (measured best; a few spills)
-k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fast, int nsph,
-           int* __restrict__ tile_cnt, const int* __restrict__ bins, uint32_t* __restrict__ vox, T* __restrict__ up,
-           T* __restrict__ f, int phase, Geom g, unsigned* __restrict__ err) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    VoxSmem<T, INIT_VEL>& S = *reinterpret_cast<VoxSmem<T, INIT_VEL>*>(smem_raw);
+__device__ __forceinline__ void voxelize_tile(VoxSmem<T, INIT_VEL>& S, int t, const SphereDev* __restrict__ sph,
+                                              const SphereFast* __restrict__ fast, int nsph,
+                                              int* __restrict__ tile_cnt, const int* __restrict__ bins,
+                                              uint32_t* __restrict__ vox, T* __restrict__ up, T* __restrict__ f,
+                                              int phase, const Geom& g, unsigned* __restrict__ err) {
     const int tid = threadIdx.x;
-    const int t = blockIdx.x;
     const int tny = tiles_along(g.ny), tnz = tiles_along(g.nz);
     const int tx = t / (tny * tnz);
     const int rem = t - tx * tny * tnz;
@@ -493,50 +516,150 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
     }
 }
 
+// Persistent voxelization: blocks claim tiles of the work list one at a time
+// (work_n[0] tiles listed, work_n[1] claim counter, work_n[2] finished blocks;
+// the last block to finish zeroes all three for the next voxelization).
+// BATCH: a listed tile belongs to the domain d with toff[d] <= tile.
+template <typename T, bool INIT_VEL, bool BATCH>
+__global__ void __launch_bounds__(VOX_THREADS, 4)   // 4 blocks per SM (measured best; a few spills)
+k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fast, int nsph,
+           int* __restrict__ tile_cnt, const int* __restrict__ bins, const int* __restrict__ work,
+           int* __restrict__ work_n, uint32_t* __restrict__ vox, T* __restrict__ up, T* __restrict__ f, int phase,
+           Geom g, unsigned* __restrict__ err, const DomView* __restrict__ doms, const int* __restrict__ toff,
+           int ndom, const int* __restrict__ ncur) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    VoxSmem<T, INIT_VEL>& S = *reinterpret_cast<VoxSmem<T, INIT_VEL>*>(smem_raw);
+    __shared__ int s_item;
+    const int nwork = *(volatile int*)work_n;
+    for (;;) {
+        __syncthreads();   // previous tile done with S
+        if (threadIdx.x == 0) s_item = atomicAdd(work_n + 1, 1);
+        __syncthreads();
+        const int w = s_item;
+        if (w >= nwork) break;
+        const int tg = work[w];
+        if (BATCH) {
+            const int d = find_domain(toff, ndom, tg);
+            const DomView& D = doms[d];
+            voxelize_tile<T, INIT_VEL>(S, tg - D.t0, sph + D.s0, fast + D.s0, __ldg(ncur + d), tile_cnt + D.t0,
+                                       bins + (size_t)D.t0 * TILE_BIN, vox + D.cell0, up + D.up0, f ? f + D.f0 : f,
+                                       phase, D.g, err);
+        } else {
+            voxelize_tile<T, INIT_VEL>(S, tg, sph, fast, nsph, tile_cnt, bins, vox, up, f, phase, g, err);
+        }
+    }
+    if (threadIdx.x == 0) {
+        __threadfence();
+        if (atomicAdd(work_n + 2, 1) == (int)gridDim.x - 1) {
+            work_n[0] = 0;
+            work_n[1] = 0;
+            work_n[2] = 0;
+        }
+    }
+}
+
 }  // namespace
 
 cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
                                    int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
                                    cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_prepare_spheres<<<(n + 127) / 128, 128, 0, s>>>(rec, n, sph, fast, xpf, tag2slot, err, g, max_tag,
-                                                     max_radius);
+    k_prepare_spheres<false><<<(n + 127) / 128, 128, 0, s>>>(rec, n, sph, fast, xpf, tag2slot, err, g, max_tag,
+                                                            max_radius, nullptr, nullptr, 0, nullptr);
     return cudaGetLastError();
 }
 
-cudaError_t launch_bin_spheres(const SphereFast* fast, int n, int* tile_cnt, int* bins, Geom g, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    k_bin_spheres<<<(n + 7) / 8, 256, 0, s>>>(fast, n, tile_cnt, bins, g);
+cudaError_t launch_prepare_spheres_batch(const double* rec, int nslots, SphereDev* sph, SphereFast* fast, float* xpf,
+                                         int* tag2slot, unsigned* err, int max_tag, double max_radius,
+                                         const DomView* doms, const int* soff, int ndom, const int* ncur,
+                                         cudaStream_t s) {
+    if (nslots <= 0) return cudaSuccess;
+    k_prepare_spheres<true><<<(nslots + 127) / 128, 128, 0, s>>>(rec, nslots, sph, fast, xpf, tag2slot, err, Geom{},
+                                                                max_tag, max_radius, doms, soff, ndom, ncur);
     return cudaGetLastError();
 }
+
+cudaError_t launch_bin_spheres(const SphereFast* fast, int n, int* tile_cnt, int* bins, int* work, int* work_n,
+                               Geom g, cudaStream_t s) {
+    if (n <= 0) return cudaSuccess;
+    k_bin_spheres<false><<<(n + 7) / 8, 256, 0, s>>>(fast, n, tile_cnt, bins, work, work_n, g, nullptr, nullptr, 0,
+                                                     nullptr);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_bin_spheres_batch(const SphereFast* fast, int nslots, int* tile_cnt, int* bins, int* work,
+                                     int* work_n, const DomView* doms, const int* soff, int ndom, const int* ncur,
+                                     cudaStream_t s) {
+    if (nslots <= 0) return cudaSuccess;
+    k_bin_spheres<true><<<(nslots + 7) / 8, 256, 0, s>>>(fast, nslots, tile_cnt, bins, work, work_n, Geom{}, doms,
+                                                         soff, ndom, ncur);
+    return cudaGetLastError();
+}
+
+namespace {
+
+template <typename T, bool INIT_VEL, bool BATCH>
+cudaError_t launch_vox(const SphereDev* sph, const SphereFast* fast, int n, int* tile_cnt, const int* bins,
+                       const int* work, int* work_n, int ntiles, uint32_t* vox, T* up, T* f, int phase, Geom g,
+                       unsigned* err, const DomView* doms, const int* toff, int ndom, const int* ncur,
+                       cudaStream_t s) {
+    constexpr size_t smem = sizeof(VoxSmem<T, INIT_VEL>);
+    static int blocks = 0;
+    if (blocks == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaFuncSetAttribute(k_voxelize<T, INIT_VEL, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)smem);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_voxelize<T, INIT_VEL, BATCH>, VOX_THREADS,
+                                                              smem);
+        if (e != cudaSuccess) return e;
+        blocks = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    const int grid = ntiles < blocks ? ntiles : blocks;
+    k_voxelize<T, INIT_VEL, BATCH><<<grid, VOX_THREADS, smem, s>>>(sph, fast, n, tile_cnt, bins, work, work_n, vox, up,
+                                                                  f, phase, g, err, doms, toff, ndom, ncur);
+    return cudaGetLastError();
+}
+
+}  // namespace
 
 template <typename T>
 cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, int n, int* tile_cnt, const int* bins,
-                            int ntiles, uint32_t* vox, T* up, T* f, int init_vel, int odd_phase, Geom g,
-                            unsigned* err, cudaStream_t s) {
+                            const int* work, int* work_n, int ntiles, uint32_t* vox, T* up, T* f, int init_vel,
+                            int odd_phase, Geom g, unsigned* err, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
-    constexpr size_t smem_iv = sizeof(VoxSmem<T, true>), smem = sizeof(VoxSmem<T, false>);
-    static bool attr = false;
-    if (!attr) {
-        cudaError_t e =
-            cudaFuncSetAttribute(k_voxelize<T, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem_iv);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(k_voxelize<T, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-        if (e != cudaSuccess) return e;
-        attr = true;
-    }
     if (init_vel)
-        k_voxelize<T, true><<<ntiles, VOX_THREADS, smem_iv, s>>>(sph, fast, n, tile_cnt, bins, vox, up, f, odd_phase,
-                                                                 g, err);
-    else
-        k_voxelize<T, false><<<ntiles, VOX_THREADS, smem, s>>>(sph, fast, n, tile_cnt, bins, vox, up, f, odd_phase, g,
-                                                               err);
-    return cudaGetLastError();
+        return launch_vox<T, true, false>(sph, fast, n, tile_cnt, bins, work, work_n, ntiles, vox, up, f, odd_phase, g,
+                                          err, nullptr, nullptr, 0, nullptr, s);
+    return launch_vox<T, false, false>(sph, fast, n, tile_cnt, bins, work, work_n, ntiles, vox, up, f, odd_phase, g,
+                                       err, nullptr, nullptr, 0, nullptr, s);
 }
 
-template cudaError_t launch_voxelize<float>(const SphereDev*, const SphereFast*, int, int*, const int*, int,
-                                            uint32_t*, float*, float*, int, int, Geom, unsigned*, cudaStream_t);
-template cudaError_t launch_voxelize<double>(const SphereDev*, const SphereFast*, int, int*, const int*, int,
-                                             uint32_t*, double*, double*, int, int, Geom, unsigned*, cudaStream_t);
+template <typename T>
+cudaError_t launch_voxelize_batch(const SphereDev* sph, const SphereFast* fast, int* tile_cnt, const int* bins,
+                                  const int* work, int* work_n, int ntiles, uint32_t* vox, T* up, T* f, int init_vel,
+                                  int odd_phase, const DomView* doms, const int* toff, int ndom, const int* ncur,
+                                  unsigned* err, cudaStream_t s) {
+    if (ntiles <= 0) return cudaSuccess;
+    if (init_vel)
+        return launch_vox<T, true, true>(sph, fast, 0, tile_cnt, bins, work, work_n, ntiles, vox, up, f, odd_phase,
+                                         Geom{}, err, doms, toff, ndom, ncur, s);
+    return launch_vox<T, false, true>(sph, fast, 0, tile_cnt, bins, work, work_n, ntiles, vox, up, f, odd_phase,
+                                      Geom{}, err, doms, toff, ndom, ncur, s);
+}
+
+#define INST(T)                                                                                                    \
+    template cudaError_t launch_voxelize<T>(const SphereDev*, const SphereFast*, int, int*, const int*, const int*, \
+                                            int*, int, uint32_t*, T*, T*, int, int, Geom, unsigned*, cudaStream_t); \
+    template cudaError_t launch_voxelize_batch<T>(const SphereDev*, const SphereFast*, int*, const int*,          \
+                                                  const int*, int*, int, uint32_t*, T*, T*, int, int,              \
+                                                  const DomView*, const int*, int, const int*, unsigned*,          \
+                                                  cudaStream_t);
+INST(float)
+INST(double)
+#undef INST
 
 }  // namespace lbdem

@@ -37,6 +37,8 @@ struct lbdem_handle {
     int ntiles = 0;
     int* d_tile_cnt = nullptr;  // [ntiles] spheres binned per tile (zero between calls)
     int* d_bins = nullptr;      // [ntiles][TILE_BIN]
+    int* d_work = nullptr;      // [ntiles] tiles with spheres (voxelization work list)
+    int* d_work_n = nullptr;    // [4] work-list counters (zero between calls)
     double* d_ft = nullptr;     // [6][cap]
     unsigned* d_err = nullptr;
     double* d_mass = nullptr;
@@ -113,7 +115,7 @@ cudaError_t dalloc(lbdem_handle* h, P** p, size_t bytes) {
 
 void release(lbdem_handle* h) {
     void* dev[] = {h->f, h->vox, h->up, h->cf, h->btab, h->btabf, h->d_rec, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot,
-                   h->d_tile_cnt, h->d_bins, h->d_ft, h->d_err, h->d_mass, h->scratch, h->d_jobs, h->d_pavg,
+                   h->d_tile_cnt, h->d_bins, h->d_work, h->d_work_n, h->d_ft, h->d_err, h->d_mass, h->scratch, h->d_jobs, h->d_pavg,
                    h->d_ppart, h->d_pcount};
     for (void* p : dev)
         if (p) cudaFree(p);
@@ -152,13 +154,15 @@ lbdem_status voxelize(lbdem_handle* h, int n, int init_vel) {
     if (n > 0) {
         CK(h, launch_prepare_spheres(h->d_rec, n, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot, h->d_err, h->g,
                                      h->cfg.max_tag, h->cfg.max_radius, s));
-        CK(h, launch_bin_spheres(h->d_fast, n, h->d_tile_cnt, h->d_bins, h->g, s));
+        CK(h, launch_bin_spheres(h->d_fast, n, h->d_tile_cnt, h->d_bins, h->d_work, h->d_work_n, h->g, s));
         const int phase = (int)(h->step & 1);
         if (h->prec == LBDEM_PREC_FP64)
-            CK(h, launch_voxelize<double>(h->d_sph, h->d_fast, n, h->d_tile_cnt, h->d_bins, h->ntiles, h->vox,
+            CK(h, launch_voxelize<double>(h->d_sph, h->d_fast, n, h->d_tile_cnt, h->d_bins, h->d_work, h->d_work_n,
+                                          h->ntiles, h->vox,
                                           (double*)h->up, (double*)h->f, init_vel, phase, h->g, h->d_err, s));
         else
-            CK(h, launch_voxelize<float>(h->d_sph, h->d_fast, n, h->d_tile_cnt, h->d_bins, h->ntiles, h->vox,
+            CK(h, launch_voxelize<float>(h->d_sph, h->d_fast, n, h->d_tile_cnt, h->d_bins, h->d_work, h->d_work_n,
+                                         h->ntiles, h->vox,
                                          (float*)h->up, (float*)h->f, init_vel, phase, h->g, h->d_err, s));
         h->launches += 3;
         if (init_vel) h->pavg_valid = false;
@@ -313,6 +317,9 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     TRY(dalloc(h, &h->d_tile_cnt, (size_t)h->ntiles * sizeof(int)));
     TRY(dalloc(h, &h->d_bins, (size_t)h->ntiles * TILE_BIN * sizeof(int)));
     TRY(cudaMemset(h->d_tile_cnt, 0, (size_t)h->ntiles * sizeof(int)));
+    TRY(dalloc(h, &h->d_work, (size_t)h->ntiles * sizeof(int)));
+    TRY(dalloc(h, &h->d_work_n, 4 * sizeof(int)));
+    TRY(cudaMemset(h->d_work_n, 0, 4 * sizeof(int)));
     TRY(dalloc(h, &h->d_ft, 6 * capn * sizeof(double)));
     TRY(dalloc(h, &h->d_err, sizeof(unsigned)));
     TRY(dalloc(h, &h->d_mass, sizeof(double)));

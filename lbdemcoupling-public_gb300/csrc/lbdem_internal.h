@@ -100,6 +100,18 @@ struct SphereFast {
 };
 static_assert(sizeof(SphereFast) == 96, "SphereFast is staged as 24 words");
 
+// One domain of a batch as the voxelization kernels see it: its geometry and
+// where its data starts in the batch arenas.
+struct DomView {
+    Geom g;
+    int s0;          // first particle slot (slots s0 .. s0 + capacity - 1)
+    int t0;          // first voxelization tile
+    size_t cell0;    // first cell in the voxel-word arena
+    size_t up0;      // first element of the domain's [3][N] particle-velocity block
+    size_t f0;       // first element of the domain's [19][N] population block
+    size_t tag0;     // first entry of the domain's tag -> slot map
+};
+
 // Largest d in [0, n) with off[d] <= idx (off ascending, off[0] <= idx).
 __device__ __forceinline__ int find_domain(const int* __restrict__ off, int n, int idx) {
     int lo = 0, hi = n - 1;
@@ -128,12 +140,32 @@ cudaError_t launch_collide_batch(const CollideArgs<T>* dargs, const int* seg0, i
 cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
                                    int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
                                    cudaStream_t s);
-// tile_cnt must be zero on entry; launch_voxelize leaves it zero again.
-cudaError_t launch_bin_spheres(const SphereFast* fast, int n, int* tile_cnt, int* bins, Geom g, cudaStream_t s);
+// tile_cnt must be zero on entry; launch_voxelize leaves it zero again.  Every
+// tile that receives a sphere is appended to work[] (work_n counts them; zero
+// on entry, left zero by launch_voxelize).
+cudaError_t launch_bin_spheres(const SphereFast* fast, int n, int* tile_cnt, int* bins, int* work, int* work_n,
+                               Geom g, cudaStream_t s);
 template <typename T>
 cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, int n, int* tile_cnt, const int* bins,
-                            int ntiles, uint32_t* vox, T* up, T* f, int init_vel, int odd_phase, Geom g,
-                            unsigned* err, cudaStream_t s);
+                            const int* work, int* work_n, int ntiles, uint32_t* vox, T* up, T* f, int init_vel,
+                            int odd_phase, Geom g, unsigned* err, cudaStream_t s);
+
+// Batch forms: particle slots and tiles of all domains in one index space;
+// soff[d] = doms[d].s0, toff[d] = doms[d].t0 (ascending); ncur[d] particles of
+// domain d are in use (slots s0 .. s0 + ncur[d] - 1); tag2slot holds a
+// (max_tag + 1)-entry map per domain, with domain-local slots.
+cudaError_t launch_prepare_spheres_batch(const double* rec, int nslots, SphereDev* sph, SphereFast* fast, float* xpf,
+                                         int* tag2slot, unsigned* err, int max_tag, double max_radius,
+                                         const DomView* doms, const int* soff, int ndom, const int* ncur,
+                                         cudaStream_t s);
+cudaError_t launch_bin_spheres_batch(const SphereFast* fast, int nslots, int* tile_cnt, int* bins, int* work,
+                                     int* work_n, const DomView* doms, const int* soff, int ndom, const int* ncur,
+                                     cudaStream_t s);
+template <typename T>
+cudaError_t launch_voxelize_batch(const SphereDev* sph, const SphereFast* fast, int* tile_cnt, const int* bins,
+                                  const int* work, int* work_n, int ntiles, uint32_t* vox, T* up, T* f, int init_vel,
+                                  int odd_phase, const DomView* doms, const int* toff, int ndom, const int* ncur,
+                                  unsigned* err, cudaStream_t s);
 
 // Field helpers.  phase: number of completed steps mod 2 (storage layout).
 template <typename T>

@@ -33,7 +33,9 @@ constexpr size_t OFF_XPF = OFF_FAST + up_align(sizeof(SphereFast) * LBDEM_STATIC
 constexpr size_t OFF_TAG = OFF_XPF + up_align(sizeof(float) * 8 * LBDEM_STATIC_MAX_SPHERES);
 constexpr size_t OFF_CNT = OFF_TAG + up_align(sizeof(int) * ((size_t)LBDEM_STATIC_MAX_TAG + 1));
 constexpr size_t OFF_BINS = OFF_CNT + up_align(sizeof(int) * LBDEM_STATIC_MAX_TILES);
-constexpr size_t SCRATCH_BYTES = OFF_BINS + up_align(sizeof(int) * TILE_BIN * (size_t)LBDEM_STATIC_MAX_TILES);
+constexpr size_t OFF_WORK = OFF_BINS + up_align(sizeof(int) * TILE_BIN * (size_t)LBDEM_STATIC_MAX_TILES);
+constexpr size_t OFF_WORKN = OFF_WORK + up_align(sizeof(int) * LBDEM_STATIC_MAX_TILES);
+constexpr size_t SCRATCH_BYTES = OFF_WORKN + up_align(sizeof(int) * 4);
 
 static_assert(SCRATCH_BYTES <= LBDEM_STATIC_SCRATCH_BYTES, "static scratch regions exceed the stated size");
 
@@ -80,6 +82,8 @@ extern "C" lbdem_status lbdem_voxelize_static(int32_t nx, int32_t ny, int32_t nz
     int* tag2slot = reinterpret_cast<int*>(base + OFF_TAG);
     int* tile_cnt = reinterpret_cast<int*>(base + OFF_CNT);
     int* bins = reinterpret_cast<int*>(base + OFF_BINS);
+    int* work = reinterpret_cast<int*>(base + OFF_WORK);
+    int* work_n = reinterpret_cast<int*>(base + OFF_WORKN);
 
     cudaStream_t s = static_cast<cudaStream_t>(cuda_stream);
     Geom g;
@@ -87,20 +91,22 @@ extern "C" lbdem_status lbdem_voxelize_static(int32_t nx, int32_t ny, int32_t nz
     g.per[0] = g.per[1] = g.per[2] = 1;   // used only when populations are initialised
     g.N = (size_t)nx * ny * nz;
 
-    // what must start from zero (the tile counters) or from "no particle" (the tag map)
+    // what must start from zero (the tile counters, the work-list counters) or
+    // from "no particle" (the tag map)
     if (cudaMemsetAsync(tile_cnt, 0, sizeof(int) * (size_t)ntiles, s) != cudaSuccess ||
+        cudaMemsetAsync(work_n, 0, sizeof(int) * 4, s) != cudaSuccess ||
         cudaMemsetAsync(tag2slot, 0x7F, sizeof(int) * ((size_t)LBDEM_STATIC_MAX_TAG + 1), s) != cudaSuccess)
         return LBDEM_ERR_CUDA;
     if (n == 0) return LBDEM_OK;   // no sphere touches a cell (as in the reference)
     cudaError_t e = launch_prepare_spheres(dev_rec, n, sph, fast, xpf, tag2slot, dev_err, g,
                                            LBDEM_STATIC_MAX_TAG, 1024.0, s);
-    if (e == cudaSuccess) e = launch_bin_spheres(fast, n, tile_cnt, bins, g, s);
+    if (e == cudaSuccess) e = launch_bin_spheres(fast, n, tile_cnt, bins, work, work_n, g, s);
     if (e == cudaSuccess) {
         if (precision == LBDEM_PREC_FP64)
-            e = launch_voxelize<double>(sph, fast, n, tile_cnt, bins, (int)ntiles, dev_vox,
+            e = launch_voxelize<double>(sph, fast, n, tile_cnt, bins, work, work_n, (int)ntiles, dev_vox,
                                         static_cast<double*>(dev_up), nullptr, 0, 0, g, dev_err, s);
         else
-            e = launch_voxelize<float>(sph, fast, n, tile_cnt, bins, (int)ntiles, dev_vox,
+            e = launch_voxelize<float>(sph, fast, n, tile_cnt, bins, work, work_n, (int)ntiles, dev_vox,
                                        static_cast<float*>(dev_up), nullptr, 0, 0, g, dev_err, s);
     }
     return e == cudaSuccess ? LBDEM_OK : LBDEM_ERR_CUDA;

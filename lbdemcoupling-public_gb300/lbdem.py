@@ -63,6 +63,18 @@ class PressureDrop(C.Structure):
                 ("rho_in", C.c_double), ("rho_out", C.c_double)]
 
 
+class Domain(C.Structure):
+    _fields_ = [("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32), ("periodic", C.c_int32 * 3),
+                ("omega", C.c_double), ("body_force", C.c_double * 3), ("max_particles", C.c_int32),
+                ("has_pressure_drop", C.c_int32), ("drop", PressureDrop)]
+
+
+class BatchConfig(C.Structure):
+    _fields_ = [("precision", C.c_int32), ("device", C.c_int32), ("max_tag", C.c_int32),
+                ("max_radius", C.c_double), ("use_graph", C.c_int32), ("autotune", C.c_int32),
+                ("reserved", C.c_int32 * 2)]
+
+
 PROFILE_PRESSURE_GRADIENT = 0
 PROFILE_POISEUILLE = 1
 
@@ -94,6 +106,24 @@ SIGNATURES = {
     "lbdem_zhang_rescale": (C.c_int, [_P, C.POINTER(_I), _I, _I, C.c_double, C.c_double]),
     "lbdem_set_pressure_drop": (C.c_int, [_P, C.POINTER(PressureDrop)]),
     "lbdem_init_profile": (C.c_int, [_P, _I, C.c_double, C.c_double, C.c_double, C.POINTER(_I), _I]),
+    "lbdem_batch_config_default": (None, [C.POINTER(BatchConfig)]),
+    "lbdem_batch_create": (C.c_int, [C.POINTER(BatchConfig), _I, C.POINTER(Domain), C.POINTER(_P)]),
+    "lbdem_batch_destroy": (C.c_int, [_P]),
+    "lbdem_batch_last_error": (C.c_char_p, [_P]),
+    "lbdem_batch_init_equilibrium": (C.c_int, [_P, C.c_double, _D]),
+    "lbdem_batch_init_profile": (C.c_int, [_P, _I, _I, C.c_double, C.c_double, C.c_double, C.POINTER(_I), _I]),
+    "lbdem_batch_set_particles": (C.c_int, [_P, C.POINTER(_I), _D, _I]),
+    "lbdem_batch_step": (C.c_int, [_P]),
+    "lbdem_batch_get_forces": (C.c_int, [_P, _D, _D]),
+    "lbdem_batch_cycle": (C.c_int, [_P, C.POINTER(_I), _D, _I, _D, _D]),
+    "lbdem_batch_get_field": (C.c_int, [_P, _I, _I, _P]),
+    "lbdem_batch_synchronize": (C.c_int, [_P]),
+    "lbdem_batch_get_step": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "lbdem_batch_get_launch_count": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "lbdem_batch_device_bytes": (C.c_int, [_P, C.POINTER(C.c_size_t)]),
+    "lbdem_batch_cells": (C.c_int, [_P, C.POINTER(C.c_int64)]),
+    "lbdem_batch_get_tuning": (C.c_int, [_P, C.POINTER(_I), C.POINTER(C.c_float)]),
+    "lbdem_batch_set_tuning": (C.c_int, [_P, _I]),
 }
 
 # Limits of lbdem_voxelize_static (include/lbdem_gpu.h).
@@ -351,3 +381,149 @@ def pack_records(x, v, w, r, tag) -> np.ndarray:
     rec[:, 9] = np.asarray(r, dtype=np.float64).reshape(n)
     rec[:, 10] = np.asarray(tag).reshape(n)
     return rec
+
+
+class Batch:
+    """Many independent lattices stepped together (lbdem_batch_* of the C ABI).
+
+    domains: list of dicts with keys shape, periodic, omega, body_force (optional),
+    max_particles, drop (optional dict: dimension, inlet, outlet, rho_in, rho_out,
+    in_direction=1, out_direction=-1)."""
+
+    def __init__(self, domains, precision=PREC_FP32_DEV, max_tag=1024, max_radius=16.0, use_graph=True,
+                 autotune=True, device=0):
+        self.lib = load()
+        cfg = BatchConfig()
+        self.lib.lbdem_batch_config_default(C.byref(cfg))
+        cfg.precision, cfg.device, cfg.max_tag = int(precision), int(device), int(max_tag)
+        cfg.max_radius = float(max_radius)
+        cfg.use_graph, cfg.autotune = int(bool(use_graph)), int(bool(autotune))
+        arr = (Domain * len(domains))()
+        for k, d in enumerate(domains):
+            D = arr[k]
+            D.nx, D.ny, D.nz = (int(v) for v in d["shape"])
+            for a in range(3):
+                D.periodic[a] = int(d.get("periodic", (1, 1, 1))[a])
+                D.body_force[a] = float(d.get("body_force", (0, 0, 0))[a])
+            D.omega = float(d["omega"])
+            D.max_particles = int(d.get("max_particles", 0))
+            drop = d.get("drop")
+            D.has_pressure_drop = int(drop is not None)
+            if drop is not None:
+                D.drop.dimension = int(drop["dimension"])
+                for q in range(6):
+                    D.drop.inlet[q] = int(drop["inlet"][q])
+                    D.drop.outlet[q] = int(drop["outlet"][q])
+                D.drop.in_direction = int(drop.get("in_direction", 1))
+                D.drop.out_direction = int(drop.get("out_direction", -1))
+                D.drop.rho_in, D.drop.rho_out = float(drop["rho_in"]), float(drop["rho_out"])
+        self.shapes = [tuple(int(v) for v in d["shape"]) for d in domains]
+        self.dtype = np.float64 if precision == PREC_FP64 else np.float32
+        h = _P()
+        st = self.lib.lbdem_batch_create(C.byref(cfg), len(domains), arr, C.byref(h))
+        if st != 0:
+            raise LbdemError(st, self.lib.lbdem_status_string(st).decode())
+        self.h = h
+        self.counts = np.zeros(len(domains), dtype=np.int32)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.lbdem_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st: int):
+        if st != 0:
+            raise LbdemError(st, self.lib.lbdem_batch_last_error(self.h).decode())
+
+    def init_equilibrium(self, rho_bar=0.0, u=(0.0, 0.0, 0.0)):
+        uu = _c64(u)
+        self._check(self.lib.lbdem_batch_init_equilibrium(self.h, float(rho_bar), _dptr(uu)))
+
+    def init_profile(self, domain, kind, rho_hi, rho_lo, u_max, n, dimension):
+        nn = (_I * 3)(*[int(v) for v in n])
+        self._check(self.lib.lbdem_batch_init_profile(self.h, int(domain), int(kind), float(rho_hi), float(rho_lo),
+                                                      float(u_max), nn, int(dimension)))
+
+    def set_particles(self, counts, rec, init_vel=False):
+        """counts[d] records of domain d, rec: [sum counts][12] (pack_records layout)."""
+        self.counts = np.ascontiguousarray(counts, dtype=np.int32)
+        rec = np.ascontiguousarray(rec, dtype=np.float64).reshape(-1, 12)
+        self._check(self.lib.lbdem_batch_set_particles(self.h, self.counts.ctypes.data_as(C.POINTER(_I)),
+                                                       _dptr(rec), int(bool(init_vel))))
+
+    def step(self):
+        self._check(self.lib.lbdem_batch_step(self.h))
+
+    def get_forces(self):
+        n = int(self.counts.sum())
+        F = np.zeros((max(n, 1), 3))
+        T = np.zeros((max(n, 1), 3))
+        self._check(self.lib.lbdem_batch_get_forces(self.h, _dptr(F), _dptr(T)))
+        return F[:n], T[:n]
+
+    def cycle(self, counts, rec, init_vel=False):
+        self.set_particles(counts, rec, init_vel)
+        self.step()
+        return self.get_forces()
+
+    def get_field(self, domain, which):
+        shape = self.shapes[domain]
+        shapes = {
+            FIELD_POPULATIONS: ((19, *shape), self.dtype),
+            FIELD_SOLID_FRACTION: (shape, np.float64),
+            FIELD_PARTICLE_ID: (shape, np.int32),
+            FIELD_PARTICLE_VELOCITY: ((3, *shape), self.dtype),
+            FIELD_DENSITY: (shape, np.float64),
+            FIELD_VELOCITY: ((3, *shape), np.float64),
+            FIELD_SUBCELL_COUNT: (shape, np.uint8),
+        }
+        shp, dt = shapes[which]
+        out = np.empty(shp, dtype=dt)
+        self._check(self.lib.lbdem_batch_get_field(self.h, int(domain), int(which), out.ctypes.data_as(_P)))
+        return out
+
+    def get_populations(self, domain):
+        return self.get_field(domain, FIELD_POPULATIONS)
+
+    def synchronize(self):
+        self._check(self.lib.lbdem_batch_synchronize(self.h))
+
+    def _i64(self, fn) -> int:
+        v = C.c_int64()
+        self._check(fn(self.h, C.byref(v)))
+        return int(v.value)
+
+    def step_count(self) -> int:
+        return self._i64(self.lib.lbdem_batch_get_step)
+
+    def launch_count(self) -> int:
+        return self._i64(self.lib.lbdem_batch_get_launch_count)
+
+    def cells(self) -> int:
+        return self._i64(self.lib.lbdem_batch_cells)
+
+    def device_bytes(self) -> int:
+        v = C.c_size_t()
+        self._check(self.lib.lbdem_batch_device_bytes(self.h, C.byref(v)))
+        return int(v.value)
+
+    def tuning(self):
+        bps = _I()
+        ms = C.c_float()
+        self._check(self.lib.lbdem_batch_get_tuning(self.h, C.byref(bps), C.byref(ms)))
+        return int(bps.value), float(ms.value)
+
+    def set_tuning(self, collide_blocks_per_sm: int):
+        self._check(self.lib.lbdem_batch_set_tuning(self.h, int(collide_blocks_per_sm)))

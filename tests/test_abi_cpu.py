@@ -41,22 +41,25 @@ def test_config_struct_matches_header(lbdem_lib):
     assert cfg.max_radius == 16.0
 
 
-def test_config_layout_matches_c_compiler(lbdem_lib, tmp_path):
-    """ctypes field offsets equal the C compiler's offsetof for lbdem_config."""
+@pytest.mark.parametrize("cname,pyname", [("lbdem_config", "Config"), ("lbdem_pressure_drop", "PressureDrop"),
+                                           ("lbdem_domain", "Domain"), ("lbdem_batch_config", "BatchConfig")])
+def test_struct_layout_matches_c_compiler(lbdem_lib, tmp_path, cname, pyname):
+    """ctypes field offsets and sizes equal the C compiler's offsetof/sizeof."""
     import shutil
     import subprocess
     cc = shutil.which("gcc") or shutil.which("cc")
     if not cc:
         pytest.skip("no C compiler")
-    fields = [f[0] for f in lbdem_lib.Config._fields_]
+    st = getattr(lbdem_lib, pyname)
+    fields = [f[0] for f in st._fields_]
     src = tmp_path / "probe.c"
-    body = "".join(f'printf("%zu\\n", offsetof(lbdem_config, {f}));' for f in fields)
+    body = "".join(f'printf("%zu\\n", offsetof({cname}, {f}));' for f in fields)
     src.write_text('#include <stddef.h>\n#include <stdio.h>\n#include "lbdem_gpu.h"\n'
-                   f'int main(void){{{body} printf("%zu\\n", sizeof(lbdem_config)); return 0;}}\n')
+                   f'int main(void){{{body} printf("%zu\\n", sizeof({cname})); return 0;}}\n')
     exe = tmp_path / "probe"
     subprocess.run([cc, "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
     got = [int(v) for v in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
-    want = [getattr(lbdem_lib.Config, f).offset for f in fields] + [C.sizeof(lbdem_lib.Config)]
+    want = [getattr(st, f).offset for f in fields] + [C.sizeof(st)]
     assert got == want
 
 
