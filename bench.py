@@ -233,6 +233,108 @@ def cpu_oracle_mlups(host_tables, budget_s: float, max_cycles: int, threads: int
     return N * done / dt / 1e6, done, dt
 
 
+def run_batched(steps: int, warmup: int, single_steps: int, device: int):
+    """Batched pressure-driven channels (workloads.channels: 512 domains, FP32
+    deviation form): aggregate MLUPS of the batch -- graph replay of one launch
+    per stage over all domains -- through the host-buffer cycle call, of the
+    replayed step alone, and of the same domains stepped one handle at a time
+    (every stage launched per domain, one synchronization per cycle)."""
+    import ctypes as C
+
+    import lbdem
+    import workloads as W
+    ch = W.channels()
+    doms = [d for d, _ in ch]
+    cells = sum(int(np.prod(d["shape"])) for d in doms)
+    nt = min(warmup + max(steps, single_steps), 16)
+    per_step, per_dom = [], []
+    q = [p for _, p in ch]
+    for _ in range(nt):
+        g = [W.with_ghosts(p, d["shape"], d["periodic"]) for d, p in zip(doms, q)]
+        counts = np.array([x.n for x in g], dtype=np.int32)
+        rec = np.concatenate([lbdem.pack_records(x.x, x.v, x.w, x.r, x.tag) for x in g])
+        per_step.append((counts, rec))
+        per_dom.append(g)
+        q = [W.advance(p, d["shape"], d["periodic"]) for d, p in zip(doms, q)]
+
+    B = lbdem.Batch(doms, precision=lbdem.PREC_FP32_DEV, max_tag=64, max_radius=8.0, device=device)
+    for s in range(warmup):
+        B.cycle(*per_step[s % nt], init_vel=False)
+    B.synchronize()
+    t0 = time.perf_counter()
+    for s in range(steps):
+        B.cycle(*per_step[(warmup + s) % nt])
+    t_e2e = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    for s in range(steps):
+        B.step()
+    B.synchronize()
+    t_dev = time.perf_counter() - t0
+    n0 = B.launch_count()
+    B.step()
+    B.synchronize()
+    launches = B.launch_count() - n0
+    bps, k1_ms = B.tuning()
+    B.close()
+
+    lib = lbdem.load()
+    Ls = []
+    for d in doms:
+        L = lbdem.Lattice(*d["shape"], d["omega"], periodic=d["periodic"], precision=lbdem.PREC_FP32_DEV,
+                          max_particles=d["max_particles"], max_tag=64, max_radius=8.0, device=device)
+        dr = d["drop"]
+        L.set_pressure_drop(dr["dimension"], dr["inlet"], dr["outlet"], dr["rho_in"], dr["rho_out"])
+        Ls.append(L)
+    D = C.POINTER(C.c_double)
+    calls = []   # per table: per domain the pointer arguments of lbdem_set_particles
+    keep = []
+    for g in per_dom:
+        row = []
+        for x in g:
+            arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (x.x, x.v, x.w, x.r)]
+            tag = np.ascontiguousarray(x.tag, dtype=np.int32)
+            keep.append((arrs, tag))
+            row.append((x.n, *[a.ctypes.data_as(D) for a in arrs], tag.ctypes.data_as(C.POINTER(C.c_int32))))
+        calls.append(row)
+    Fbuf = [np.zeros((max(L.cfg.max_particles, 1), 3)) for L in Ls]
+    Tbuf = [np.zeros((max(L.cfg.max_particles, 1), 3)) for L in Ls]
+
+    def cycle_all(s):
+        row = calls[s % nt]
+        for L, a in zip(Ls, row):
+            lib.lbdem_set_particles(L.h, a[0], a[1], a[2], a[3], a[4], a[5], 0)
+            lib.lbdem_collide_and_stream(L.h)
+        for L, a, F, T in zip(Ls, row, Fbuf, Tbuf):
+            lib.lbdem_get_forces(L.h, a[0], F.ctypes.data_as(D), T.ctypes.data_as(D))
+
+    for s in range(2):
+        cycle_all(s)
+    t0 = time.perf_counter()
+    for s in range(single_steps):
+        cycle_all(2 + s)
+    t_one = time.perf_counter() - t0
+    for L in Ls:
+        L.close()
+    peak, _ = peaks()
+    ach = BYTES_PER_CELL["fp32"] * cells / (k1_ms * 1e-3) / 1e9 if k1_ms > 0 else None
+    return {
+        "workload": f"{len(doms)} pressure-driven channels, Lx U[64,160], Ly=Lz U[24,48], walls in y and z, "
+                    f"1-40 spheres r U[3,6] each, tau 0.6, fp32 deviation form",
+        "cells": cells, "particles_local": int(sum(p.n for _, p in ch)),
+        "value": cells * steps / t_e2e / 1e6, "unit": "MLUPS",
+        "note": "value: lbdem_batch_cycle with host buffers (upload of the particle table and download of the "
+                "forces inside the replayed graph), wall clock over the timed cycles",
+        "device_value": cells * steps / t_dev / 1e6,
+        "one_at_a_time": cells * single_steps / t_one / 1e6,
+        "one_at_a_time_steps": single_steps,
+        "speedup_vs_one_at_a_time": (cells * steps / t_e2e) / (cells * single_steps / t_one),
+        "launches_per_step": launches, "launches_per_step_one_at_a_time": 5 * len(doms),
+        "collide_blocks_per_sm": bps, "k1_ms": k1_ms,
+        "k1_roofline": None if ach is None else {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
+                                                   "bytes_per_cell": BYTES_PER_CELL["fp32"]},
+    }
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -243,6 +345,8 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--forms", default="fp32,fp64", help="population forms to time (fp32 is the headline)")
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI leg (profiling runs)")
+    ap.add_argument("--no-batched", action="store_true", help="skip the batched-channels leg")
+    ap.add_argument("--batched-steps", type=int, default=60)
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -334,6 +438,10 @@ def main():
         F32, F64 = r32["F"], r64["F"]
         ferr = float(np.max(np.abs(F32 - F64)) / np.max(np.abs(F64)))
 
+    batched = None
+    if not args.no_batched and world == 1:
+        batched = run_batched(args.batched_steps, args.warmup, 8, device)
+
     cpu = None
     if not args.no_cpu_baseline:
         mlups, cycles, secs = cpu_oracle_mlups(host, args.cpu_budget, 1000, threads)
@@ -349,16 +457,17 @@ def main():
                    "l2": "inputs larger than L2 (populations 1.27 GB fp32 / 2.55 GB fp64)",
                    "parallelism": "replicas" if world > 1 else "single GPU"},
         "roofline": {"bound": "hbm", "achieved": ach32, "peak": peak, "unit": "GB/s", "frac": ach32 / peak,
-                     "traffic": traffic.get("fp32"), "kernel": "k_collide_stream<float>",
+                     "traffic": traffic.get("fp32"), "kernel": "k_collide_staged<float> (all axes periodic)",
                      "bytes_per_cell": BYTES_PER_CELL["fp32"], "peak_source": peak_kind,
                      "k1_ms": r32["k1_ms"], "k2_voxelize_ms": r32["k2_ms"]},
         "fp64": None if r64 is None else {
             "value": v64, "unit": "MLUPS", "ms_per_step": t64 / args.steps,
             "roofline": {"bound": "hbm", "achieved": ach64, "peak": peak, "unit": "GB/s", "frac": ach64 / peak,
-                         "traffic": traffic.get("fp64"), "kernel": "k_collide_stream<double>",
+                         "traffic": traffic.get("fp64"), "kernel": "k_collide_staged<double> (all axes periodic)",
                          "bytes_per_cell": BYTES_PER_CELL["fp64"], "k1_ms": r64["k1_ms"],
                          "k2_voxelize_ms": r64["k2_ms"]}},
         "force_rel_err_fp32_vs_fp64": ferr,
+        "batched": batched,
         "e2e": None if args.no_e2e else {"value": world * N * args.steps / e2e_s / 1e6, "unit": "MLUPS",
                                          "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "cpu_baseline": cpu,

@@ -10,7 +10,9 @@ Without LIGGGHTS, this module produces the same kind of list:
 * ``with_ghosts``: appends the periodic images whose bounding box reaches the
   lattice, axis by axis (x, then y, then z, images of earlier images included),
   the order in which LAMMPS builds ghost atoms;
-* ``advance``: prescribed kinematics, x += v per step with periodic wrap.
+* ``advance``: prescribed kinematics, x += v per step with periodic wrap;
+* ``channels``: many pressure-driven rectangular channels of uneven size, the
+  domains of a batch.
 """
 from __future__ import annotations
 
@@ -155,3 +157,27 @@ def polydisperse_512(seed: int = 2025) -> tuple[tuple[int, int, int], Particles]
     """Periodic 512x256x256, r ~ U[4, 10] until solid fraction 0.30."""
     shape = (512, 256, 256)
     return shape, suspension(shape, rmin=4.0, rmax=10.0, phi_target=0.30, seed=seed)
+
+
+def channels(n_domains: int = 512, seed: int = 2026, tau: float = 0.6, rho_in: float = 1.0,
+             rho_out: float = 0.999) -> list[tuple[dict, Particles]]:
+    """Independent channels: Lx ~ U{64..160}, Ly = Lz ~ U{24..48}, walls in y and z,
+    x periodic and driven by the Zhang pressure drop between the planes x = 0 and
+    x = Lx - 1 (interior rows, as examples/showcaseRectChannel); 1..40 spheres
+    of radius U[3, 6] per channel (fewer where random sequential addition does not
+    fit them), v ~ N(0, 0.01), omega ~ N(0, 1e-3).  Returns (domain, locals) pairs;
+    a domain's max_particles leaves room for the periodic images."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_domains):
+        lx = int(rng.integers(64, 161))
+        l = int(rng.integers(24, 49))
+        shape = (lx, l, l)
+        want = int(rng.integers(1, 41))
+        p = suspension(shape, n_max=want, rmin=3.0, rmax=6.0, seed=seed * 100003 + k, periodic=(1, 0, 0),
+                       max_trials=20000)
+        dom = {"shape": shape, "periodic": (1, 0, 0), "omega": 1.0 / tau, "max_particles": 2 * max(p.n, 1),
+               "drop": {"dimension": 0, "inlet": [0, 0, 1, l - 2, 1, l - 2],
+                        "outlet": [lx - 1, lx - 1, 1, l - 2, 1, l - 2], "rho_in": rho_in, "rho_out": rho_out}}
+        out.append((dom, p))
+    return out
