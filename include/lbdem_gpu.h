@@ -257,6 +257,38 @@ lbdem_status lbdem_voxelize_static(int32_t nx, int32_t ny, int32_t nz, int32_t p
                                    const double* dev_rec, uint32_t* dev_vox, void* dev_up, uint32_t* dev_err,
                                    void* cuda_stream);
 
+/* ---- Adjoint ---------------------------------------------------------------
+ * No counterpart in the reference.  Reverse-mode gradients of a loss built
+ * from the per-particle forces and torques of a window of steps,
+ *     L = sum_t sum_p weights[t][p] . (F_p(t), T_p(t)),
+ * with respect to the per-step particle velocities and angular velocities,
+ * the body force and tau.  Every cell's solid fraction and owner are held
+ * fixed over the window and are not differentiated.  The call runs the window
+ * forward from the handle's state exactly as nsteps calls of
+ * lbdem_set_particles_device + lbdem_collide_and_stream would, keeps the
+ * populations every checkpoint_every steps, then sweeps back segment by
+ * segment, recomputing each segment once into a tape and applying the
+ * hand-written reverse of collide-stream (transposed streaming, reverse
+ * B-weighted PSM collision, reverse BGK with Guo forcing) step by step.
+ *   rec        [nsteps][n][12] particle tables (host) as for
+ *              lbdem_set_particles_device; positions, radii and tags must be
+ *              identical in every step, velocities may change
+ *   weights    [nsteps][n][6] dL/dF_p and dL/dT_p of every step (host)
+ *   loss       out: L
+ *   grad_vel   out [nsteps][n][6]: dL/dv_p(t), dL/domega_p(t), at the first
+ *              list index of each tag (ghost-image entries zero)
+ *   grad_body_force out [3], grad_tau out [1]
+ *   grad_f0    optional out [19][N] of the lattice type, natural order: dL/d
+ *              populations before the window
+ * On return the handle holds the state after the window and the forces of its
+ * last step.  Not available with a pressure drop set (not differentiated). */
+lbdem_status lbdem_adjoint_window(lbdem_handle* h, int32_t nsteps, int32_t checkpoint_every, int32_t n,
+                                  const double* rec, const double* weights, double* loss, double* grad_vel,
+                                  double* grad_body_force, double* grad_tau, void* grad_f0);
+/* Device time of the last lbdem_adjoint_window: forward pass and backward
+ * pass (segment recomputation + adjoint steps), CUDA events. */
+lbdem_status lbdem_adjoint_timing(lbdem_handle* h, float* forward_ms, float* backward_ms);
+
 /* ---- Batched independent domains ------------------------------------------
  * No counterpart in the reference, which couples one lattice per process.
  * Many independent lattices of uneven size -- each with its own extent,

@@ -1,0 +1,395 @@
+// Reverse-mode (adjoint) step of the PSM lattice: gradients of a loss built
+// from the per-particle forces and torques of a window of steps, with respect
+// to the populations, the per-step particle velocities and angular velocities,
+// the body force and the relaxation time tau.  The solid fraction and owner of
+// every cell are held fixed over the window and are not differentiated.
+//
+// Forward map of one cell (what K1 computes, src/ibCompositeDynamics3D.hh:130-203,
+// written as one function of the pre-collision populations f):
+//   BGK with Guo forcing (n < 125):
+//     rhoBar = sum f, j = sum c f, rho = 1 + rhoBar, r = 1/rho,
+//     J = j + rho g / 2, u = J r, pre = (1 - omega/2) rho,
+//     feq_k = t_k [rhoBar + 3 c_k.J + r (4.5 (c_k.J)^2 - 1.5 J.J)],
+//     src_k = t_k pre [3 (c_k.g - u.g) + 9 (c_k.u)(c_k.g)],
+//     f*_k = (1 - omega) f_k + omega feq_k + src_k          (f* = f when n = 125)
+//   PSM (n > 0), moments rhoBar*, j* of f*, P = (1 + rhoBar*) uP:
+//     out_k = (1 - B) f*_k + B (f_opp(k) - feq_opp(k)(j*) + feq_k(P))   k != 0
+//     out_0 = (1 - B) f*_0 + B (f_0 + feq_0(j*) - feq_0(P))
+//     F = -sum_{k=1..9} c_k (bb_k - bbOpp_k) = B (2 j - j* - P)
+//   (feq(.) at rhoBar*, 1/(1 + rhoBar*)), and push streaming with half-way
+//   bounce-back.  With uP = v + w x d (d: cell minus particle centre, minimum
+//   image), tau entering through omega = 1/tau and B = sf ooo / ((1 - sf) + ooo),
+//   ooo = tau - 1/2.
+//
+// The adjoint step, per cell x, given lambda_{t+1} (natural layout):
+//   mu_k   = lambda_{t+1,k}(x + c_k), or lambda_{t+1,opp k}(x) beyond a wall
+//            (transpose of push streaming),
+//   a      = dL/dF of the owner particle at this step (+ w_T x arm for torques),
+//   lambda_t(x) = (d out / d f)^T mu + (dF/df)^T a, and the parameter
+//   gradients (d out / d theta)^T mu + (dF/d theta)^T a,
+// evaluated by hand-written reverse differentiation of the formulas above.
+#include "lbdem_internal.h"
+
+namespace lbdem {
+namespace {
+
+constexpr unsigned FULLMASK = 0xffffffffu;
+constexpr int ADJ_THREADS = 256;
+
+template <typename T>
+__device__ __forceinline__ T cdotT(int k, T a, T b, T c) {
+    const int X = cx(k), Y = cy(k), Z = cz(k);
+    T r = T(0);
+    if (X) r = X > 0 ? a : -a;
+    if (Y) r = Y > 0 ? r + b : r - b;
+    if (Z) r = Z > 0 ? r + c : r - c;
+    return r;
+}
+
+template <typename T>
+__device__ __forceinline__ T feqT(int k, T rb, T r, T c_dot, T sq) {
+    return T(wt(k)) * (rb + T(3) * c_dot + r * (T(4.5) * c_dot * c_dot - T(1.5) * sq));
+}
+
+// Reverse of one cell.  f: pre-collision populations; mu: adjoint of the
+// post-collision populations; a: adjoint of the cell force.  Returns lambda
+// (adjoint of f) and accumulates d/duP, d/dtau, d/dg.
+template <typename T>
+__device__ __forceinline__ void adjoint_cell(const T (&f)[Q], const T (&mu)[Q], int n, T B, double dBdtau,
+                                             const T (&uP)[3], const T (&a)[3], T omega, const T (&g)[3],
+                                             T (&lam)[Q], T (&guP)[3], double& gtau, double (&gg)[3]) {
+    // pre-collision moments
+    T rb = T(0), j0 = T(0), j1 = T(0), j2 = T(0);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        rb += f[k];
+        if (cx(k)) j0 += cx(k) > 0 ? f[k] : -f[k];
+        if (cy(k)) j1 += cy(k) > 0 ? f[k] : -f[k];
+        if (cz(k)) j2 += cz(k) > 0 ? f[k] : -f[k];
+    }
+    const T rho = T(1) + rb, r = T(1) / rho;
+    const T J0 = j0 + T(0.5) * rho * g[0], J1 = j1 + T(0.5) * rho * g[1], J2v = j2 + T(0.5) * rho * g[2];
+    const T u0 = J0 * r, u1 = J1 * r, u2 = J2v * r;
+    const T JJ = J0 * J0 + J1 * J1 + J2v * J2v;
+    const T pre = (T(1) - T(0.5) * omega) * rho;
+    const T ug = u0 * g[0] + u1 * g[1] + u2 * g[2];
+
+    // moments of f* and S1 = sum mu_k f*_k
+    T rbs = T(0), js0 = T(0), js1 = T(0), js2 = T(0), S1 = T(0);
+    if (n == 125) {
+        rbs = rb; js0 = j0; js1 = j1; js2 = j2;
+#pragma unroll
+        for (int k = 0; k < Q; ++k) S1 += mu[k] * f[k];
+    } else {
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const T cJ = cdotT<T>(k, J0, J1, J2v);
+            const T cu = cdotT<T>(k, u0, u1, u2), cg = cdotT<T>(k, g[0], g[1], g[2]);
+            const T src = T(wt(k)) * pre * (T(3) * (cg - ug) + T(9) * cu * cg);
+            const T fs = (T(1) - omega) * f[k] + omega * feqT<T>(k, rb, r, cJ, JJ) + src;
+            rbs += fs;
+            if (cx(k)) js0 += cx(k) > 0 ? fs : -fs;
+            if (cy(k)) js1 += cy(k) > 0 ? fs : -fs;
+            if (cz(k)) js2 += cz(k) > 0 ? fs : -fs;
+            S1 += mu[k] * fs;
+        }
+    }
+
+    // adjoint of f* (gfs_k = sB mu_k + grbs + c_k . gjs) and the PSM part of lambda
+    T sB = T(1), grbs = T(0), gjs0 = T(0), gjs1 = T(0), gjs2 = T(0);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) lam[k] = T(0);
+    guP[0] = guP[1] = guP[2] = T(0);
+    if (n > 0) {
+        sB = T(1) - B;
+        const T rhos = T(1) + rbs, rs = T(1) / rhos;
+        const T Jq = js0 * js0 + js1 * js1 + js2 * js2;
+        const T P0 = rhos * uP[0], P1 = rhos * uP[1], P2v = rhos * uP[2];
+        const T PP = P0 * P0 + P1 * P1 + P2v * P2v;
+        T gB = -S1;
+        T grs = T(0), gP0 = T(0), gP1 = T(0), gP2 = T(0);
+        // F = B (2 j - j* - P)
+        gB += a[0] * (T(2) * j0 - js0 - P0) + a[1] * (T(2) * j1 - js1 - P1) + a[2] * (T(2) * j2 - js2 - P2v);
+        gjs0 -= B * a[0]; gjs1 -= B * a[1]; gjs2 -= B * a[2];
+        gP0 -= B * a[0]; gP1 -= B * a[1]; gP2 -= B * a[2];
+        // seeds of feq(j*) (e_k) and feq(P) (E_k), the B-weighted terms of out
+        T e[Q], E[Q];
+        {
+            const T q0 = feqT<T>(0, rbs, rs, T(0), Jq), s0 = feqT<T>(0, rbs, rs, T(0), PP);
+            gB += mu[0] * (f[0] + q0 - s0);
+            e[0] = B * mu[0];
+            E[0] = -B * mu[0];
+            lam[0] = B * mu[0];
+        }
+#pragma unroll
+        for (int i = 1; i <= 9; ++i) {
+            const int o = i + 9;
+            const T ci = cdotT<T>(i, js0, js1, js2), co = -ci;
+            const T pi = cdotT<T>(i, P0, P1, P2v), po = -pi;
+            const T qi = feqT<T>(i, rbs, rs, ci, Jq), qo = feqT<T>(o, rbs, rs, co, Jq);
+            const T si = feqT<T>(i, rbs, rs, pi, PP), so = feqT<T>(o, rbs, rs, po, PP);
+            gB += mu[i] * (f[o] - qo + si) + mu[o] * (f[i] - qi + so);
+            e[o] = -B * mu[i];
+            e[i] = -B * mu[o];
+            E[i] = B * mu[i];
+            E[o] = B * mu[o];
+            lam[o] = B * mu[i];
+            lam[i] = B * mu[o];
+        }
+        // reverse of the two equilibria
+#pragma unroll
+        for (int k = 0; k < Q; ++k) {
+            const T w = T(wt(k));
+            const T cj = cdotT<T>(k, js0, js1, js2);
+            const T cp = cdotT<T>(k, P0, P1, P2v);
+            grbs += w * (e[k] + E[k]);
+            grs += w * (e[k] * (T(4.5) * cj * cj - T(1.5) * Jq) + E[k] * (T(4.5) * cp * cp - T(1.5) * PP));
+            // d/dj* of e_k feq: w e_k (3 c_k + 9 rs (c_k.j*) c_k - 3 rs j*)
+            const T aj = w * e[k] * (T(3) + T(9) * rs * cj);
+            const T ap = w * E[k] * (T(3) + T(9) * rs * cp);
+            if (cx(k)) { gjs0 += cx(k) > 0 ? aj : -aj; gP0 += cx(k) > 0 ? ap : -ap; }
+            if (cy(k)) { gjs1 += cy(k) > 0 ? aj : -aj; gP1 += cy(k) > 0 ? ap : -ap; }
+            if (cz(k)) { gjs2 += cz(k) > 0 ? aj : -aj; gP2 += cz(k) > 0 ? ap : -ap; }
+            const T bj = T(3) * rs * w * e[k], bp = T(3) * rs * w * E[k];
+            gjs0 -= bj * js0; gjs1 -= bj * js1; gjs2 -= bj * js2;
+            gP0 -= bp * P0; gP1 -= bp * P1; gP2 -= bp * P2v;
+        }
+        // P = rho* uP, rs = 1/rho*, rho* = 1 + rbs
+        T grhos = gP0 * uP[0] + gP1 * uP[1] + gP2 * uP[2];
+        guP[0] = rhos * gP0; guP[1] = rhos * gP1; guP[2] = rhos * gP2;
+        grhos -= rs * rs * grs;
+        grbs += grhos;
+        // F's 2 B j term: d/df_k = 2 B (a . c_k)
+#pragma unroll
+        for (int k = 0; k < Q; ++k) lam[k] += T(2) * B * cdotT<T>(k, a[0], a[1], a[2]);
+        gtau += (double)gB * dBdtau;
+    }
+
+    if (n == 125) {
+        // f* = f
+#pragma unroll
+        for (int k = 0; k < Q; ++k) lam[k] += sB * mu[k] + grbs + cdotT<T>(k, gjs0, gjs1, gjs2);
+        return;
+    }
+    // BGK reverse with phi_k = sB mu_k + grbs + c_k . gjs
+    T gom = T(0), grb = T(0), gr = T(0), gJ0 = T(0), gJ1 = T(0), gJ2 = T(0), gpre = T(0);
+    T gu0 = T(0), gu1 = T(0), gu2 = T(0);
+    T gg0 = T(0), gg1 = T(0), gg2 = T(0);
+#pragma unroll
+    for (int k = 0; k < Q; ++k) {
+        const T phi = sB * mu[k] + grbs + cdotT<T>(k, gjs0, gjs1, gjs2);
+        const T w = T(wt(k));
+        const T cJ = cdotT<T>(k, J0, J1, J2v);
+        const T cu = cdotT<T>(k, u0, u1, u2), cg = cdotT<T>(k, g[0], g[1], g[2]);
+        const T fe = feqT<T>(k, rb, r, cJ, JJ);
+        lam[k] += (T(1) - omega) * phi;
+        gom += phi * (fe - f[k]);
+        const T h = omega * phi;
+        grb += w * h;
+        gr += w * h * (T(4.5) * cJ * cJ - T(1.5) * JJ);
+        const T aJ = w * h * (T(3) + T(9) * r * cJ);
+        const T bJ = T(3) * r * w * h;
+        gJ0 -= bJ * J0; gJ1 -= bJ * J1; gJ2 -= bJ * J2v;
+        gpre += w * phi * (T(3) * (cg - ug) + T(9) * cu * cg);
+        const T wp = w * pre * phi;
+        // d src / du = w pre (-3 g + 9 (c.g) c);  d src / dg = w pre (3 c - 3 u + 9 (c.u) c)
+        gu0 -= T(3) * wp * g[0]; gu1 -= T(3) * wp * g[1]; gu2 -= T(3) * wp * g[2];
+        gg0 -= T(3) * wp * u0; gg1 -= T(3) * wp * u1; gg2 -= T(3) * wp * u2;
+        const T au = T(9) * wp * cg, ag = wp * (T(3) + T(9) * cu);
+        if (cx(k)) { const T s = cx(k) > 0 ? T(1) : T(-1); gJ0 += s * aJ; gu0 += s * au; gg0 += s * ag; }
+        if (cy(k)) { const T s = cy(k) > 0 ? T(1) : T(-1); gJ1 += s * aJ; gu1 += s * au; gg1 += s * ag; }
+        if (cz(k)) { const T s = cz(k) > 0 ? T(1) : T(-1); gJ2 += s * aJ; gu2 += s * au; gg2 += s * ag; }
+    }
+    // pre = (1 - omega/2) rho
+    gom -= T(0.5) * rho * gpre;
+    T grho = (T(1) - T(0.5) * omega) * gpre;
+    // u = J r
+    gJ0 += r * gu0; gJ1 += r * gu1; gJ2 += r * gu2;
+    gr += J0 * gu0 + J1 * gu1 + J2v * gu2;
+    // J = j + rho g / 2
+    grho += T(0.5) * (g[0] * gJ0 + g[1] * gJ1 + g[2] * gJ2);
+    gg0 += T(0.5) * rho * gJ0; gg1 += T(0.5) * rho * gJ1; gg2 += T(0.5) * rho * gJ2;
+    grho -= r * r * gr;
+    grb += grho;
+#pragma unroll
+    for (int k = 0; k < Q; ++k) lam[k] += grb + cdotT<T>(k, gJ0, gJ1, gJ2);
+    gtau -= (double)gom * (double)omega * (double)omega;   // omega = 1/tau
+    gg[0] += (double)gg0; gg[1] += (double)gg1; gg[2] += (double)gg2;
+}
+
+// Warp-segmented sum of six values per particle slot into out[key][6]
+// (consecutive cells mostly share the owner).  All 32 lanes must call.
+__device__ __forceinline__ void reduce6(int key, double (&v)[6], double* __restrict__ out) {
+    const unsigned solid = __ballot_sync(FULLMASK, key >= 0);
+    if (solid == 0u) return;
+    const int lane = threadIdx.x & 31;
+    const int prevKey = __shfl_up_sync(FULLMASK, key, 1);
+    const bool head = (lane == 0) || (prevKey != key);
+    const unsigned heads = __ballot_sync(FULLMASK, head);
+    const int segStart = 31 - __clz(heads & (FULLMASK >> (31 - lane)));
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const double o = __shfl_up_sync(FULLMASK, v[q], d);
+            if (lane - d >= segStart) v[q] += o;
+        }
+    }
+    const int nextKey = __shfl_down_sync(FULLMASK, key, 1);
+    const bool tail = (lane == 31) || (nextKey != key);
+    if (tail && key >= 0)
+#pragma unroll
+        for (int q = 0; q < 6; ++q) atomicAdd(out + 6 * (size_t)key + q, v[q]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_step(const AdjointArgs<T> A) {
+    __shared__ double s_red[ADJ_THREADS / 32][4];
+    const Geom g = A.g;
+    const size_t N = g.N;
+    double gtau = 0.0, gg[3] = {0.0, 0.0, 0.0};
+    const size_t stride = (size_t)gridDim.x * blockDim.x;
+    const size_t total = (N + 31) / 32 * 32;   // whole warps for the shuffles
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < total; c += stride) {
+        int key = -1;
+        double pv[6] = {0, 0, 0, 0, 0, 0};
+        if (c < N) {
+            const int z = (int)(c % g.nz);
+            const size_t rr = c / g.nz;
+            const int y = (int)(rr % g.ny);
+            const int x = (int)(rr / g.ny);
+            T f[Q], mu[Q];
+#pragma unroll
+            for (int k = 0; k < Q; ++k) f[k] = A.f[slot_index(k, x, y, z, A.phase, g)];
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                int X = x + cx(k), Y = y + cy(k), Z = z + cz(k);
+                bool out = false;
+                if (X < 0 || X >= g.nx) { if (g.per[0]) X = X < 0 ? X + g.nx : X - g.nx; else out = true; }
+                if (Y < 0 || Y >= g.ny) { if (g.per[1]) Y = Y < 0 ? Y + g.ny : Y - g.ny; else out = true; }
+                if (Z < 0 || Z >= g.nz) { if (g.per[2]) Z = Z < 0 ? Z + g.nz : Z - g.nz; else out = true; }
+                mu[k] = out ? A.lam_in[(size_t)opp(k) * N + c]
+                            : A.lam_in[(size_t)k * N + ((size_t)X * g.ny + Y) * g.nz + Z];
+            }
+            const uint32_t w = A.vox[c];
+            int n = min((int)(w & VOX_NMASK), 125);
+            T uP[3] = {T(0), T(0), T(0)}, a[3] = {T(0), T(0), T(0)};
+            double d[3] = {0, 0, 0};
+            T B = T(0);
+            double dBdtau = 0.0;
+            int slot = -1;
+            if (n > 0) {
+                const int tag = (int)(w >> VOX_NBITS);
+                slot = tag <= A.max_tag ? A.tag2slot[tag] : -1;
+                if (slot < 0 || slot >= A.nslot) {
+                    atomicOr(A.err, 0x8u);   // LBDEM_DEVERR_UNMAPPED_TAG
+                    slot = -1;
+                } else {
+                    const double* p = A.rec + (size_t)slot * REC_STRIDE;
+                    const int pos[3] = {x, y, z}, ext[3] = {g.nx, g.ny, g.nz};
+#pragma unroll
+                    for (int q = 0; q < 3; ++q) {
+                        // minimum image as in the force arm (src/ibProcessors3D.hh:230-243)
+                        double dq = (double)pos[q] - p[q];
+                        const int h = ext[q] / 2;
+                        if (dq > (double)h) dq -= (double)ext[q];
+                        else if (dq < (double)(-h)) dq += (double)ext[q];
+                        d[q] = dq;
+                    }
+                    // uP = v + w x d (setValues, src/ibProcessors3D.hh:163-174)
+                    uP[0] = T(p[3] + (p[7] * d[2] - p[8] * d[1]));
+                    uP[1] = T(p[4] + (-p[6] * d[2] + p[8] * d[0]));
+                    uP[2] = T(p[5] + (p[6] * d[1] - p[7] * d[0]));
+                    const double* wgt = A.w + (size_t)slot * 6;
+                    // dL/dF_cell = w_F + w_T x d
+                    a[0] = T(wgt[0] + (wgt[4] * d[2] - wgt[5] * d[1]));
+                    a[1] = T(wgt[1] + (wgt[5] * d[0] - wgt[3] * d[2]));
+                    a[2] = T(wgt[2] + (wgt[3] * d[1] - wgt[4] * d[0]));
+                    B = A.btab[n];
+                    const double sf = (1. / 125.) * (double)n, ooo = A.tau - 0.5, den = (1. - sf) + ooo;
+                    dBdtau = n < 125 ? sf * (1. - sf) / (den * den) : 0.0;
+                }
+            }
+            if (n > 0 && slot < 0) n = 0;
+            T lam[Q], guP[3];
+            const T gvec[3] = {A.g3[0], A.g3[1], A.g3[2]};
+            adjoint_cell<T>(f, mu, n, B, dBdtau, uP, a, A.omega, gvec, lam, guP, gtau, gg);
+#pragma unroll
+            for (int k = 0; k < Q; ++k) A.lam_out[(size_t)k * N + c] = lam[k];
+            if (slot >= 0) {
+                key = slot;
+                const double u0 = (double)guP[0], u1 = (double)guP[1], u2 = (double)guP[2];
+                pv[0] = u0; pv[1] = u1; pv[2] = u2;
+                // d/dw of w x d: d x guP
+                pv[3] = d[1] * u2 - d[2] * u1;
+                pv[4] = d[2] * u0 - d[0] * u2;
+                pv[5] = d[0] * u1 - d[1] * u0;
+            }
+        }
+        reduce6(key, pv, A.gvel);
+    }
+    // block sums of d/dg and d/dtau, one atomic per block and value
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    double v4[4] = {gg[0], gg[1], gg[2], gtau};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+        for (int o = 16; o > 0; o >>= 1) v4[q] += __shfl_down_sync(FULLMASK, v4[q], o);
+    if (lane == 0)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) s_red[warp][q] = v4[q];
+    __syncthreads();
+    if (threadIdx.x < 4) {
+        double s = 0;
+        for (int k = 0; k < ADJ_THREADS / 32; ++k) s += s_red[k][threadIdx.x];
+        atomicAdd(A.gglob + threadIdx.x, s);
+    }
+}
+
+// loss += sum_p w[p] . (F_p, T_p) for one step (ft: F (3 nslot) then T (3 nslot)).
+__global__ void k_loss_step(const double* __restrict__ ft, const double* __restrict__ w, int n, int nslot,
+                            double* __restrict__ loss) {
+    double s = 0.0;
+    for (int p = threadIdx.x; p < n; p += blockDim.x)
+#pragma unroll
+        for (int q = 0; q < 3; ++q)
+            s += w[6 * (size_t)p + q] * ft[3 * (size_t)p + q] + w[6 * (size_t)p + 3 + q] * ft[3 * (size_t)nslot + 3 * (size_t)p + q];
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(FULLMASK, s, o);
+    __shared__ double part[32];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double t = 0;
+        for (int k = 0; k < (int)(blockDim.x >> 5); ++k) t += part[k];
+        *loss += t;
+    }
+}
+
+}  // namespace
+
+template <typename T>
+cudaError_t launch_adjoint_step(const AdjointArgs<T>& a, cudaStream_t s) {
+    static int blocks = 0;
+    if (blocks == 0) {
+        int dev = 0, sms = 0, per_sm = 0;
+        cudaError_t e = cudaGetDevice(&dev);
+        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (e == cudaSuccess)
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adjoint_step<T>, ADJ_THREADS, 0);
+        if (e != cudaSuccess) return e;
+        blocks = sms * (per_sm > 0 ? per_sm : 1);
+    }
+    const size_t need = (a.g.N + ADJ_THREADS - 1) / ADJ_THREADS;
+    const unsigned grid = (unsigned)(need < (size_t)blocks ? (need > 0 ? need : 1) : (size_t)blocks);
+    k_adjoint_step<T><<<grid, ADJ_THREADS, 0, s>>>(a);
+    return cudaGetLastError();
+}
+
+cudaError_t launch_loss_step(const double* ft, const double* w, int n, int nslot, double* loss, cudaStream_t s) {
+    k_loss_step<<<1, 256, 0, s>>>(ft, w, n, nslot, loss);
+    return cudaGetLastError();
+}
+
+template cudaError_t launch_adjoint_step<float>(const AdjointArgs<float>&, cudaStream_t);
+template cudaError_t launch_adjoint_step<double>(const AdjointArgs<double>&, cudaStream_t);
+
+}  // namespace lbdem

@@ -9,6 +9,8 @@
 #include <cstring>
 #include <new>
 #include <string>
+#include <utility>
+#include <vector>
 
 using namespace lbdem;
 
@@ -64,6 +66,8 @@ struct lbdem_handle {
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
     size_t dev_bytes = 0;
+
+    float adj_fwd_ms = 0.f, adj_bwd_ms = 0.f;
 
     int n_cur = 0;
     int64_t step = 0;
@@ -735,6 +739,202 @@ lbdem_status lbdem_init_profile(lbdem_handle* h, int32_t kind, double rho_hi, do
                                          dimension, h->g, h->stream));
     h->launches += 1;
     h->pavg_valid = false;
+    return LBDEM_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Device buffers of one adjoint window, released on every exit path.
+struct AdjointBuffers {
+    std::vector<void*> ptrs;
+    ~AdjointBuffers() {
+        for (void* p : ptrs)
+            if (p) cudaFree(p);
+    }
+    template <typename P>
+    cudaError_t get(P** p, size_t bytes) {
+        void* q = nullptr;
+        cudaError_t e = cudaMalloc(&q, bytes == 0 ? 16 : bytes);
+        if (e == cudaSuccess) {
+            ptrs.push_back(q);
+            *p = (P*)q;
+        }
+        return e;
+    }
+};
+
+struct EventPair {
+    cudaEvent_t e[3] = {nullptr, nullptr, nullptr};
+    ~EventPair() {
+        for (auto& x : e)
+            if (x) cudaEventDestroy(x);
+    }
+};
+
+template <typename T>
+cudaError_t adjoint_launch(lbdem_handle* h, const T* f, int phase, const T* lam_in, T* lam_out, const double* rec,
+                           const double* w, double* gvel, double* gglob, int n) {
+    AdjointArgs<T> a;
+    a.g = h->g;
+    a.f = f;
+    a.phase = phase;
+    a.lam_in = lam_in;
+    a.lam_out = lam_out;
+    a.vox = h->vox;
+    a.tag2slot = h->d_tag2slot;
+    a.max_tag = h->cfg.max_tag;
+    a.nslot = n;
+    a.rec = rec;
+    a.w = w;
+    a.gvel = gvel;
+    a.gglob = gglob;
+    a.btab = sizeof(T) == 8 ? (const T*)h->btab : (const T*)h->btabf;
+    a.omega = (T)h->cfg.omega;
+    a.tau = 1.0 / h->cfg.omega;
+    for (int d = 0; d < 3; ++d) a.g3[d] = (T)h->cfg.body_force[d];
+    a.err = h->d_err;
+    return launch_adjoint_step<T>(a, h->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+lbdem_status lbdem_adjoint_window(lbdem_handle* h, int32_t nsteps, int32_t K, int32_t n, const double* rec,
+                                  const double* weights, double* loss, double* grad_vel, double* grad_body_force,
+                                  double* grad_tau, void* grad_f0) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    if (nsteps < 1 || K < 1 || K > nsteps) return fail(h, LBDEM_ERR_INVALID_ARG, "adjoint: need 1 <= checkpoint_every <= nsteps");
+    if (n < 0) return fail(h, LBDEM_ERR_INVALID_ARG, "adjoint: n < 0");
+    if (n > h->cap) return fail(h, LBDEM_ERR_CAPACITY, "adjoint: n exceeds max_particles");
+    if (!loss || !grad_body_force || !grad_tau || (n > 0 && (!rec || !weights || !grad_vel)))
+        return fail(h, LBDEM_ERR_INVALID_ARG, "adjoint: null argument");
+    if (h->pdrop_on) return fail(h, LBDEM_ERR_INVALID_ARG, "adjoint: the pressure drop is not differentiated");
+    for (int t = 1; t < nsteps; ++t)
+        for (int k = 0; k < n; ++k) {
+            const double* a = rec + ((size_t)t * n + k) * REC_STRIDE;
+            const double* b = rec + (size_t)k * REC_STRIDE;
+            if (std::memcmp(a, b, 3 * sizeof(double)) != 0 || std::memcmp(a + 9, b + 9, 2 * sizeof(double)) != 0)
+                return fail(h, LBDEM_ERR_INVALID_ARG, "adjoint: positions, radii and tags must stay fixed");
+        }
+    DeviceGuard dg(h->device);
+    cudaStream_t s = h->stream;
+    const size_t N = h->g.N;
+    const size_t pop = (size_t)Q * N * h->esz;
+    const int nseg = (nsteps + K - 1) / K;
+    const size_t nrec = (size_t)nsteps * n;
+    AdjointBuffers buf;
+    double *d_recs = nullptr, *d_w = nullptr, *d_gv = nullptr, *d_glob = nullptr, *d_loss = nullptr, *d_ft = nullptr;
+    unsigned char *ckpt = nullptr, *tape = nullptr, *lam = nullptr, *work = nullptr;
+    CK(h, buf.get(&d_recs, nrec * REC_STRIDE * sizeof(double)));
+    CK(h, buf.get(&d_w, nrec * 6 * sizeof(double)));
+    CK(h, buf.get(&d_gv, nrec * 6 * sizeof(double)));
+    CK(h, buf.get(&d_glob, 4 * sizeof(double)));
+    CK(h, buf.get(&d_loss, sizeof(double)));
+    CK(h, buf.get(&d_ft, 6 * (size_t)std::max(n, 1) * sizeof(double)));
+    CK(h, buf.get(&ckpt, (size_t)nseg * pop));
+    CK(h, buf.get(&tape, (size_t)K * pop));
+    CK(h, buf.get(&lam, 2 * pop));
+    CK(h, buf.get(&work, pop + ALLOC_TAIL));
+    EventPair ev;
+    for (auto& e : ev.e) CK(h, cudaEventCreate(&e));
+    if (n > 0) {
+        CK(h, cudaMemcpyAsync(d_recs, rec, nrec * REC_STRIDE * sizeof(double), cudaMemcpyHostToDevice, s));
+        CK(h, cudaMemcpyAsync(d_w, weights, nrec * 6 * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    CK(h, cudaMemsetAsync(d_gv, 0, nrec * 6 * sizeof(double) + 0, s));
+    CK(h, cudaMemsetAsync(d_glob, 0, 4 * sizeof(double), s));
+    CK(h, cudaMemsetAsync(d_loss, 0, sizeof(double), s));
+    CK(h, cudaMemsetAsync(lam, 0, pop, s));        // lambda after the window = 0
+    CK(h, cudaMemsetAsync(work + pop, 0, ALLOC_TAIL, s));
+    const int64_t step0 = h->step;
+    lbdem_status st;
+
+    // forward pass with checkpoints
+    CK(h, cudaEventRecord(ev.e[0], s));
+    for (int t = 0; t < nsteps; ++t) {
+        if (t % K == 0) CK(h, cudaMemcpyAsync(ckpt + (size_t)(t / K) * pop, h->f, pop, cudaMemcpyDeviceToDevice, s));
+        if ((st = lbdem_set_particles_device(h, n, d_recs + (size_t)t * n * REC_STRIDE, 0)) != LBDEM_OK) return st;
+        if ((st = lbdem_collide_and_stream(h)) != LBDEM_OK) return st;
+        if (n > 0) {
+            CK(h, launch_loss_step(h->d_ft, d_w + (size_t)t * n * 6, n, n, d_loss, s));
+            h->launches += 1;
+        }
+    }
+    CK(h, cudaEventRecord(ev.e[1], s));
+    if (n > 0) CK(h, cudaMemcpyAsync(d_ft, h->d_ft, 6 * (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+
+    // backward pass: recompute each segment into the tape, then reverse steps
+    void* f_final = h->f;
+    h->f = work;
+    unsigned char* lam_in = lam;
+    unsigned char* lam_out = lam + pop;
+    lbdem_status bst = LBDEM_OK;
+    for (int seg = nseg - 1; seg >= 0 && bst == LBDEM_OK; --seg) {
+        const int t0 = seg * K, t1 = std::min(t0 + K, nsteps);
+        cudaError_t e = cudaMemcpyAsync(work, ckpt + (size_t)seg * pop, pop, cudaMemcpyDeviceToDevice, s);
+        if (e != cudaSuccess) { bst = fail_cuda(h, "adjoint checkpoint restore", e); break; }
+        h->step = step0 + t0;
+        for (int t = t0; t < t1 && bst == LBDEM_OK; ++t) {
+            e = cudaMemcpyAsync(tape + (size_t)(t - t0) * pop, work, pop, cudaMemcpyDeviceToDevice, s);
+            if (e != cudaSuccess) { bst = fail_cuda(h, "adjoint tape", e); break; }
+            if (t + 1 < t1) {   // the state after the segment's last step is not needed
+                if ((bst = lbdem_set_particles_device(h, n, d_recs + (size_t)t * n * REC_STRIDE, 0)) != LBDEM_OK) break;
+                bst = lbdem_collide_and_stream(h);
+            }
+        }
+        for (int t = t1 - 1; t >= t0 && bst == LBDEM_OK; --t) {
+            const int phase = (int)((step0 + t) & 1);
+            const unsigned char* ft = tape + (size_t)(t - t0) * pop;
+            if (h->prec == LBDEM_PREC_FP64)
+                e = adjoint_launch<double>(h, (const double*)ft, phase, (const double*)lam_in, (double*)lam_out,
+                                           d_recs + (size_t)t * n * REC_STRIDE, d_w + (size_t)t * n * 6,
+                                           d_gv + (size_t)t * n * 6, d_glob, n);
+            else
+                e = adjoint_launch<float>(h, (const float*)ft, phase, (const float*)lam_in, (float*)lam_out,
+                                          d_recs + (size_t)t * n * REC_STRIDE, d_w + (size_t)t * n * 6,
+                                          d_gv + (size_t)t * n * 6, d_glob, n);
+            if (e != cudaSuccess) { bst = fail_cuda(h, "adjoint step", e); break; }
+            h->launches += 1;
+            std::swap(lam_in, lam_out);
+        }
+    }
+    h->f = f_final;
+    h->step = step0 + nsteps;
+    if (bst != LBDEM_OK) return bst;
+    CK(h, cudaEventRecord(ev.e[2], s));
+    // the voxel state and the forces of the window's last step
+    if ((st = lbdem_set_particles_device(h, n, d_recs + (size_t)(nsteps - 1) * n * REC_STRIDE, 0)) != LBDEM_OK)
+        return st;
+    if (n > 0) CK(h, cudaMemcpyAsync(h->d_ft, d_ft, 6 * (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+
+    double glob[4];
+    CK(h, cudaMemcpyAsync(loss, d_loss, sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(h, cudaMemcpyAsync(glob, d_glob, 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (n > 0) CK(h, cudaMemcpyAsync(grad_vel, d_gv, nrec * 6 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    if (grad_f0) CK(h, cudaMemcpyAsync(grad_f0, lam_in, pop, cudaMemcpyDeviceToHost, s));
+    CK(h, cudaMemcpyAsync(h->h_err, h->d_err, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    CK(h, cudaStreamSynchronize(s));
+    grad_body_force[0] = glob[0];
+    grad_body_force[1] = glob[1];
+    grad_body_force[2] = glob[2];
+    *grad_tau = glob[3];
+    CK(h, cudaEventElapsedTime(&h->adj_fwd_ms, ev.e[0], ev.e[1]));
+    CK(h, cudaEventElapsedTime(&h->adj_bwd_ms, ev.e[1], ev.e[2]));
+    if (*h->h_err) {
+        char msg[96];
+        std::snprintf(msg, sizeof(msg), "device error word 0x%x", *h->h_err);
+        return fail(h, LBDEM_ERR_DEVICE, msg);
+    }
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_adjoint_timing(lbdem_handle* h, float* forward_ms, float* backward_ms) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    if (forward_ms) *forward_ms = h->adj_fwd_ms;
+    if (backward_ms) *backward_ms = h->adj_bwd_ms;
     return LBDEM_OK;
 }
 

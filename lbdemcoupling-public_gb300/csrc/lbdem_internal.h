@@ -202,6 +202,32 @@ template <typename T>
 cudaError_t launch_plane_pressure(const PlaneJob* jobs, int njobs, int blocks_per_job, int phase, int rescale,
                                   const double* avg_in, double* avg_out, double* partial, unsigned* count,
                                   cudaStream_t s);
+// One adjoint step (k_adjoint.cu).
+template <typename T>
+struct AdjointArgs {
+    Geom g;
+    const T* f;              // pre-collision populations of the step, AA layout of `phase`
+    int phase;
+    const T* lam_in;         // adjoint of the populations after the step, natural [19][N]
+    T* lam_out;              // adjoint of the populations before the step, natural [19][N]
+    const uint32_t* vox;     // voxel words (fixed over the window)
+    const int* tag2slot;
+    int max_tag, nslot;
+    const double* rec;       // [nslot][12] particle records of the step
+    const double* w;         // [nslot][6] dL/dF, dL/dT of the step
+    double* gvel;            // [nslot][6] += dL/dv, dL/domega of the step
+    double* gglob;           // [4] += dL/dg, dL/dtau
+    const T* btab;           // B(n)
+    T omega;
+    double tau;
+    T g3[3];
+    unsigned* err;
+};
+template <typename T>
+cudaError_t launch_adjoint_step(const AdjointArgs<T>& a, cudaStream_t s);
+// loss += sum_p w[p] . (F_p, T_p) of one step
+cudaError_t launch_loss_step(const double* ft, const double* w, int n, int nslot, double* loss, cudaStream_t s);
+
 // Equilibrium initial profiles, src/periodicPressureFunctionals3D.hh:242-298:
 // kind 0 pressure gradient, kind 1 Poiseuille profile plus pressure gradient.
 template <typename T>

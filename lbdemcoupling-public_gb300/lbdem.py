@@ -106,6 +106,8 @@ SIGNATURES = {
     "lbdem_zhang_rescale": (C.c_int, [_P, C.POINTER(_I), _I, _I, C.c_double, C.c_double]),
     "lbdem_set_pressure_drop": (C.c_int, [_P, C.POINTER(PressureDrop)]),
     "lbdem_init_profile": (C.c_int, [_P, _I, C.c_double, C.c_double, C.c_double, C.POINTER(_I), _I]),
+    "lbdem_adjoint_window": (C.c_int, [_P, _I, _I, _I, _D, _D, _D, _D, _D, _D, _P]),
+    "lbdem_adjoint_timing": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "lbdem_batch_config_default": (None, [C.POINTER(BatchConfig)]),
     "lbdem_batch_create": (C.c_int, [C.POINTER(BatchConfig), _I, C.POINTER(Domain), C.POINTER(_P)]),
     "lbdem_batch_destroy": (C.c_int, [_P]),
@@ -336,6 +338,33 @@ class Lattice:
 
     def set_stream(self, stream_ptr: int | None):
         self._check(self.lib.lbdem_set_stream(self.h, _P(stream_ptr) if stream_ptr else None))
+
+    # -- adjoint --------------------------------------------------------------
+    def adjoint_window(self, rec, weights, checkpoint_every, want_f0=False):
+        """lbdem_adjoint_window.  rec: [nsteps][n][12] particle tables (positions fixed),
+        weights: [nsteps][n][6] dL/dF, dL/dT.  Returns a dict with loss, grad_vel
+        [nsteps][n][6], grad_body_force [3], grad_tau and optionally grad_f0."""
+        rec = np.ascontiguousarray(rec, dtype=np.float64)
+        nsteps, n = rec.shape[0], rec.shape[1]
+        w = np.ascontiguousarray(weights, dtype=np.float64).reshape(nsteps, n, 6)
+        loss = C.c_double()
+        gv = np.zeros((nsteps, max(n, 1), 6))
+        gb = np.zeros(3)
+        gt = C.c_double()
+        f0 = np.zeros((19, *self.shape), dtype=self.dtype) if want_f0 else None
+        self._check(self.lib.lbdem_adjoint_window(self.h, nsteps, int(checkpoint_every), n, _dptr(rec), _dptr(w),
+                                                  C.byref(loss), _dptr(gv), _dptr(gb), C.byref(gt),
+                                                  f0.ctypes.data_as(_P) if want_f0 else None))
+        self.n = n   # the handle holds the particle list of the window's last step
+        out = {"loss": float(loss.value), "grad_vel": gv[:, :n], "grad_body_force": gb, "grad_tau": float(gt.value)}
+        if want_f0:
+            out["grad_f0"] = f0
+        return out
+
+    def adjoint_timing(self):
+        a, b = C.c_float(), C.c_float()
+        self._check(self.lib.lbdem_adjoint_timing(self.h, C.byref(a), C.byref(b)))
+        return float(a.value), float(b.value)
 
     # -- periodic pressure drop and initial profiles -----------------------
     def average_density(self, box) -> float:
