@@ -51,13 +51,25 @@ __device__ __forceinline__ T feqT(int k, T rb, T r, T c_dot, T sq) {
     return T(wt(k)) * (rb + T(3) * c_dot + r * (T(4.5) * c_dot * c_dot - T(1.5) * sq));
 }
 
-// Reverse of one cell.  f: pre-collision populations; mu: adjoint of the
-// post-collision populations; a: adjoint of the cell force.  Returns lambda
-// (adjoint of f) and accumulates d/duP, d/dtau, d/dg.
+// Scalars of one cell's reverse pass; with them lambda_k (the adjoint of f_k) is
+//   psm_k + (n == 125 ? phi_k : (1 - omega) phi_k + grb + c_k . gJ),
+//   psm_k = B mu_opp(k) + 2 B (a . c_k),  phi_k = sB mu_k + grbs + c_k . gjs
+// (n == 0: B = 0, sB = 1, grbs = gjs = 0), so the 19 values are formed while
+// they are stored and never held together.
 template <typename T>
-__device__ __forceinline__ void adjoint_cell(const T (&f)[Q], const T (&mu)[Q], int n, T B, double dBdtau,
-                                             const T (&uP)[3], const T (&a)[3], T omega, const T (&g)[3],
-                                             T (&lam)[Q], T (&guP)[3], double& gtau, double (&gg)[3]) {
+struct CellAdj {
+    T B, sB, grbs, gjs0, gjs1, gjs2;   // PSM part: adjoint of f* = sB mu + grbs + c . gjs
+    T grb, gJ0, gJ1, gJ2;              // BGK part
+};
+
+// Reverse of one cell.  f: pre-collision populations; mu: adjoint of the
+// post-collision populations; a: adjoint of the cell force.  Accumulates
+// d/duP, d/dtau, d/dg and returns the scalars lambda is built from.
+template <typename T>
+__device__ __forceinline__ CellAdj<T> adjoint_cell(const T (&f)[Q], const T (&mu)[Q], int n, T B, double dBdtau,
+                                                   const T (&uP)[3], const T (&a)[3], T omega, const T (&g)[3],
+                                                   T (&guP)[3], double& gtau, double (&gg)[3]) {
+    CellAdj<T> R;
     // pre-collision moments
     T rb = T(0), j0 = T(0), j1 = T(0), j2 = T(0);
 #pragma unroll
@@ -74,132 +86,114 @@ __device__ __forceinline__ void adjoint_cell(const T (&f)[Q], const T (&mu)[Q], 
     const T pre = (T(1) - T(0.5) * omega) * rho;
     const T ug = u0 * g[0] + u1 * g[1] + u2 * g[2];
 
-    // moments of f* and S1 = sum mu_k f*_k
-    T rbs = T(0), js0 = T(0), js1 = T(0), js2 = T(0), S1 = T(0);
-    if (n == 125) {
-        rbs = rb; js0 = j0; js1 = j1; js2 = j2;
-#pragma unroll
-        for (int k = 0; k < Q; ++k) S1 += mu[k] * f[k];
-    } else {
-#pragma unroll
-        for (int k = 0; k < Q; ++k) {
-            const T cJ = cdotT<T>(k, J0, J1, J2v);
-            const T cu = cdotT<T>(k, u0, u1, u2), cg = cdotT<T>(k, g[0], g[1], g[2]);
-            const T src = T(wt(k)) * pre * (T(3) * (cg - ug) + T(9) * cu * cg);
-            const T fs = (T(1) - omega) * f[k] + omega * feqT<T>(k, rb, r, cJ, JJ) + src;
-            rbs += fs;
-            if (cx(k)) js0 += cx(k) > 0 ? fs : -fs;
-            if (cy(k)) js1 += cy(k) > 0 ? fs : -fs;
-            if (cz(k)) js2 += cz(k) > 0 ? fs : -fs;
-            S1 += mu[k] * fs;
-        }
-    }
-
-    // adjoint of f* (gfs_k = sB mu_k + grbs + c_k . gjs) and the PSM part of lambda
-    T sB = T(1), grbs = T(0), gjs0 = T(0), gjs1 = T(0), gjs2 = T(0);
-#pragma unroll
-    for (int k = 0; k < Q; ++k) lam[k] = T(0);
+    R.B = T(0); R.sB = T(1); R.grbs = T(0); R.gjs0 = T(0); R.gjs1 = T(0); R.gjs2 = T(0);
     guP[0] = guP[1] = guP[2] = T(0);
     if (n > 0) {
-        sB = T(1) - B;
+        // moments of f* and S1 = sum mu_k f*_k
+        T rbs = T(0), js0 = T(0), js1 = T(0), js2 = T(0), S1 = T(0);
+        if (n == 125) {
+            rbs = rb; js0 = j0; js1 = j1; js2 = j2;
+#pragma unroll
+            for (int k = 0; k < Q; ++k) S1 += mu[k] * f[k];
+        } else {
+#pragma unroll
+            for (int k = 0; k < Q; ++k) {
+                const T cJ = cdotT<T>(k, J0, J1, J2v);
+                const T cu = cdotT<T>(k, u0, u1, u2), cg = cdotT<T>(k, g[0], g[1], g[2]);
+                const T src = T(wt(k)) * pre * (T(3) * (cg - ug) + T(9) * cu * cg);
+                const T fs = (T(1) - omega) * f[k] + omega * feqT<T>(k, rb, r, cJ, JJ) + src;
+                rbs += fs;
+                if (cx(k)) js0 += cx(k) > 0 ? fs : -fs;
+                if (cy(k)) js1 += cy(k) > 0 ? fs : -fs;
+                if (cz(k)) js2 += cz(k) > 0 ? fs : -fs;
+                S1 += mu[k] * fs;
+            }
+        }
+        R.B = B;
+        R.sB = T(1) - B;
         const T rhos = T(1) + rbs, rs = T(1) / rhos;
         const T Jq = js0 * js0 + js1 * js1 + js2 * js2;
         const T P0 = rhos * uP[0], P1 = rhos * uP[1], P2v = rhos * uP[2];
         const T PP = P0 * P0 + P1 * P1 + P2v * P2v;
-        T gB = -S1;
-        T grs = T(0), gP0 = T(0), gP1 = T(0), gP2 = T(0);
         // F = B (2 j - j* - P)
-        gB += a[0] * (T(2) * j0 - js0 - P0) + a[1] * (T(2) * j1 - js1 - P1) + a[2] * (T(2) * j2 - js2 - P2v);
-        gjs0 -= B * a[0]; gjs1 -= B * a[1]; gjs2 -= B * a[2];
-        gP0 -= B * a[0]; gP1 -= B * a[1]; gP2 -= B * a[2];
-        // seeds of feq(j*) (e_k) and feq(P) (E_k), the B-weighted terms of out
-        T e[Q], E[Q];
+        T gB = -S1 + a[0] * (T(2) * j0 - js0 - P0) + a[1] * (T(2) * j1 - js1 - P1) + a[2] * (T(2) * j2 - js2 - P2v);
+        T gjs0 = -B * a[0], gjs1 = -B * a[1], gjs2 = -B * a[2];
+        T gP0 = -B * a[0], gP1 = -B * a[1], gP2 = -B * a[2];
+        // seeds e (of feq at j*) and E (of feq at P) of the B-weighted terms of out,
+        // folded into the equilibria's reverse as they are formed
+        T se = T(0), sE = T(0), grs = T(0);
         {
             const T q0 = feqT<T>(0, rbs, rs, T(0), Jq), s0 = feqT<T>(0, rbs, rs, T(0), PP);
             gB += mu[0] * (f[0] + q0 - s0);
-            e[0] = B * mu[0];
-            E[0] = -B * mu[0];
-            lam[0] = B * mu[0];
+            const T w = T(wt(0)), e0 = B * mu[0], E0 = -B * mu[0];
+            se += w * e0;
+            sE += w * E0;
+            grs += w * (e0 * (-T(1.5) * Jq) + E0 * (-T(1.5) * PP));
         }
 #pragma unroll
         for (int i = 1; i <= 9; ++i) {
             const int o = i + 9;
-            const T ci = cdotT<T>(i, js0, js1, js2), co = -ci;
-            const T pi = cdotT<T>(i, P0, P1, P2v), po = -pi;
-            const T qi = feqT<T>(i, rbs, rs, ci, Jq), qo = feqT<T>(o, rbs, rs, co, Jq);
-            const T si = feqT<T>(i, rbs, rs, pi, PP), so = feqT<T>(o, rbs, rs, po, PP);
+            const T w = T(wt(i));
+            const T ci = cdotT<T>(i, js0, js1, js2);
+            const T pi = cdotT<T>(i, P0, P1, P2v);
+            const T qi = feqT<T>(i, rbs, rs, ci, Jq), qo = feqT<T>(o, rbs, rs, -ci, Jq);
+            const T si = feqT<T>(i, rbs, rs, pi, PP), so = feqT<T>(o, rbs, rs, -pi, PP);
             gB += mu[i] * (f[o] - qo + si) + mu[o] * (f[i] - qi + so);
-            e[o] = -B * mu[i];
-            e[i] = -B * mu[o];
-            E[i] = B * mu[i];
-            E[o] = B * mu[o];
-            lam[o] = B * mu[i];
-            lam[i] = B * mu[o];
+            const T ei = -B * mu[o], eo = -B * mu[i], Ei = B * mu[i], Eo = B * mu[o];
+            se += w * (ei + eo);
+            sE += w * (Ei + Eo);
+            const T cq = T(4.5) * ci * ci - T(1.5) * Jq, pq = T(4.5) * pi * pi - T(1.5) * PP;
+            grs += w * ((ei + eo) * cq + (Ei + Eo) * pq);
+            // c_i w (e_i (3 + 9 rs c_i.j*) - e_o (3 - 9 rs c_i.j*)), c_o = -c_i
+            const T aj = w * (ei * (T(3) + T(9) * rs * ci) - eo * (T(3) - T(9) * rs * ci));
+            const T ap = w * (Ei * (T(3) + T(9) * rs * pi) - Eo * (T(3) - T(9) * rs * pi));
+            if (cx(i)) { gjs0 += cx(i) > 0 ? aj : -aj; gP0 += cx(i) > 0 ? ap : -ap; }
+            if (cy(i)) { gjs1 += cy(i) > 0 ? aj : -aj; gP1 += cy(i) > 0 ? ap : -ap; }
+            if (cz(i)) { gjs2 += cz(i) > 0 ? aj : -aj; gP2 += cz(i) > 0 ? ap : -ap; }
         }
-        // reverse of the two equilibria
-#pragma unroll
-        for (int k = 0; k < Q; ++k) {
-            const T w = T(wt(k));
-            const T cj = cdotT<T>(k, js0, js1, js2);
-            const T cp = cdotT<T>(k, P0, P1, P2v);
-            grbs += w * (e[k] + E[k]);
-            grs += w * (e[k] * (T(4.5) * cj * cj - T(1.5) * Jq) + E[k] * (T(4.5) * cp * cp - T(1.5) * PP));
-            // d/dj* of e_k feq: w e_k (3 c_k + 9 rs (c_k.j*) c_k - 3 rs j*)
-            const T aj = w * e[k] * (T(3) + T(9) * rs * cj);
-            const T ap = w * E[k] * (T(3) + T(9) * rs * cp);
-            if (cx(k)) { gjs0 += cx(k) > 0 ? aj : -aj; gP0 += cx(k) > 0 ? ap : -ap; }
-            if (cy(k)) { gjs1 += cy(k) > 0 ? aj : -aj; gP1 += cy(k) > 0 ? ap : -ap; }
-            if (cz(k)) { gjs2 += cz(k) > 0 ? aj : -aj; gP2 += cz(k) > 0 ? ap : -ap; }
-            const T bj = T(3) * rs * w * e[k], bp = T(3) * rs * w * E[k];
-            gjs0 -= bj * js0; gjs1 -= bj * js1; gjs2 -= bj * js2;
-            gP0 -= bp * P0; gP1 -= bp * P1; gP2 -= bp * P2v;
-        }
+        // the -3 rs j* (resp. P) part of d feq / d j*, summed over k
+        gjs0 -= T(3) * rs * se * js0; gjs1 -= T(3) * rs * se * js1; gjs2 -= T(3) * rs * se * js2;
+        gP0 -= T(3) * rs * sE * P0; gP1 -= T(3) * rs * sE * P1; gP2 -= T(3) * rs * sE * P2v;
         // P = rho* uP, rs = 1/rho*, rho* = 1 + rbs
         T grhos = gP0 * uP[0] + gP1 * uP[1] + gP2 * uP[2];
         guP[0] = rhos * gP0; guP[1] = rhos * gP1; guP[2] = rhos * gP2;
         grhos -= rs * rs * grs;
-        grbs += grhos;
-        // F's 2 B j term: d/df_k = 2 B (a . c_k)
-#pragma unroll
-        for (int k = 0; k < Q; ++k) lam[k] += T(2) * B * cdotT<T>(k, a[0], a[1], a[2]);
+        R.grbs = se + sE + grhos;
+        R.gjs0 = gjs0; R.gjs1 = gjs1; R.gjs2 = gjs2;
         gtau += (double)gB * dBdtau;
     }
 
-    if (n == 125) {
-        // f* = f
-#pragma unroll
-        for (int k = 0; k < Q; ++k) lam[k] += sB * mu[k] + grbs + cdotT<T>(k, gjs0, gjs1, gjs2);
-        return;
-    }
+    R.grb = T(0); R.gJ0 = T(0); R.gJ1 = T(0); R.gJ2 = T(0);
+    if (n == 125) return R;   // no BGK: f* = f
     // BGK reverse with phi_k = sB mu_k + grbs + c_k . gjs
-    T gom = T(0), grb = T(0), gr = T(0), gJ0 = T(0), gJ1 = T(0), gJ2 = T(0), gpre = T(0);
+    T gom = T(0), sh = T(0), gr = T(0), gJ0 = T(0), gJ1 = T(0), gJ2 = T(0), gpre = T(0);
     T gu0 = T(0), gu1 = T(0), gu2 = T(0);
-    T gg0 = T(0), gg1 = T(0), gg2 = T(0);
+    T gg0 = T(0), gg1 = T(0), gg2 = T(0), swp = T(0);
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
-        const T phi = sB * mu[k] + grbs + cdotT<T>(k, gjs0, gjs1, gjs2);
+        const T phi = R.sB * mu[k] + R.grbs + cdotT<T>(k, R.gjs0, R.gjs1, R.gjs2);
         const T w = T(wt(k));
         const T cJ = cdotT<T>(k, J0, J1, J2v);
         const T cu = cdotT<T>(k, u0, u1, u2), cg = cdotT<T>(k, g[0], g[1], g[2]);
         const T fe = feqT<T>(k, rb, r, cJ, JJ);
-        lam[k] += (T(1) - omega) * phi;
         gom += phi * (fe - f[k]);
         const T h = omega * phi;
-        grb += w * h;
+        sh += w * h;
         gr += w * h * (T(4.5) * cJ * cJ - T(1.5) * JJ);
         const T aJ = w * h * (T(3) + T(9) * r * cJ);
-        const T bJ = T(3) * r * w * h;
-        gJ0 -= bJ * J0; gJ1 -= bJ * J1; gJ2 -= bJ * J2v;
         gpre += w * phi * (T(3) * (cg - ug) + T(9) * cu * cg);
         const T wp = w * pre * phi;
+        swp += wp;
         // d src / du = w pre (-3 g + 9 (c.g) c);  d src / dg = w pre (3 c - 3 u + 9 (c.u) c)
-        gu0 -= T(3) * wp * g[0]; gu1 -= T(3) * wp * g[1]; gu2 -= T(3) * wp * g[2];
-        gg0 -= T(3) * wp * u0; gg1 -= T(3) * wp * u1; gg2 -= T(3) * wp * u2;
         const T au = T(9) * wp * cg, ag = wp * (T(3) + T(9) * cu);
-        if (cx(k)) { const T s = cx(k) > 0 ? T(1) : T(-1); gJ0 += s * aJ; gu0 += s * au; gg0 += s * ag; }
-        if (cy(k)) { const T s = cy(k) > 0 ? T(1) : T(-1); gJ1 += s * aJ; gu1 += s * au; gg1 += s * ag; }
-        if (cz(k)) { const T s = cz(k) > 0 ? T(1) : T(-1); gJ2 += s * aJ; gu2 += s * au; gg2 += s * ag; }
+        if (cx(k)) { const T sg = cx(k) > 0 ? T(1) : T(-1); gJ0 += sg * aJ; gu0 += sg * au; gg0 += sg * ag; }
+        if (cy(k)) { const T sg = cy(k) > 0 ? T(1) : T(-1); gJ1 += sg * aJ; gu1 += sg * au; gg1 += sg * ag; }
+        if (cz(k)) { const T sg = cz(k) > 0 ? T(1) : T(-1); gJ2 += sg * aJ; gu2 += sg * au; gg2 += sg * ag; }
     }
+    // the k-independent parts summed once: -3 r J (sum w h), -3 g (sum w pre phi), -3 u (sum w pre phi)
+    gJ0 -= T(3) * r * sh * J0; gJ1 -= T(3) * r * sh * J1; gJ2 -= T(3) * r * sh * J2v;
+    gu0 -= T(3) * swp * g[0]; gu1 -= T(3) * swp * g[1]; gu2 -= T(3) * swp * g[2];
+    gg0 -= T(3) * swp * u0; gg1 -= T(3) * swp * u1; gg2 -= T(3) * swp * u2;
     // pre = (1 - omega/2) rho
     gom -= T(0.5) * rho * gpre;
     T grho = (T(1) - T(0.5) * omega) * gpre;
@@ -210,11 +204,11 @@ __device__ __forceinline__ void adjoint_cell(const T (&f)[Q], const T (&mu)[Q], 
     grho += T(0.5) * (g[0] * gJ0 + g[1] * gJ1 + g[2] * gJ2);
     gg0 += T(0.5) * rho * gJ0; gg1 += T(0.5) * rho * gJ1; gg2 += T(0.5) * rho * gJ2;
     grho -= r * r * gr;
-    grb += grho;
-#pragma unroll
-    for (int k = 0; k < Q; ++k) lam[k] += grb + cdotT<T>(k, gJ0, gJ1, gJ2);
+    R.grb = sh + grho;
+    R.gJ0 = gJ0; R.gJ1 = gJ1; R.gJ2 = gJ2;
     gtau -= (double)gom * (double)omega * (double)omega;   // omega = 1/tau
     gg[0] += (double)gg0; gg[1] += (double)gg1; gg[2] += (double)gg2;
+    return R;
 }
 
 // Warp-segmented sum of six values per particle slot into out[key][6]
@@ -311,11 +305,17 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_step(const AdjointArgs<
                 }
             }
             if (n > 0 && slot < 0) n = 0;
-            T lam[Q], guP[3];
+            T guP[3];
             const T gvec[3] = {A.g3[0], A.g3[1], A.g3[2]};
-            adjoint_cell<T>(f, mu, n, B, dBdtau, uP, a, A.omega, gvec, lam, guP, gtau, gg);
+            const CellAdj<T> R = adjoint_cell<T>(f, mu, n, B, dBdtau, uP, a, A.omega, gvec, guP, gtau, gg);
+            const T om1 = n == 125 ? T(1) : T(1) - A.omega;
 #pragma unroll
-            for (int k = 0; k < Q; ++k) A.lam_out[(size_t)k * N + c] = lam[k];
+            for (int k = 0; k < Q; ++k) {
+                const T phi = R.sB * mu[k] + R.grbs + cdotT<T>(k, R.gjs0, R.gjs1, R.gjs2);
+                T l = om1 * phi + R.grb + cdotT<T>(k, R.gJ0, R.gJ1, R.gJ2);
+                if (n > 0) l += R.B * mu[opp(k)] + T(2) * R.B * cdotT<T>(k, a[0], a[1], a[2]);
+                A.lam_out[(size_t)k * N + c] = l;
+            }
             if (slot >= 0) {
                 key = slot;
                 const double u0 = (double)guP[0], u1 = (double)guP[1], u2 = (double)guP[2];
