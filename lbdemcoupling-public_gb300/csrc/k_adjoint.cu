@@ -66,9 +66,9 @@ struct CellAdj {
 // post-collision populations; a: adjoint of the cell force.  Accumulates
 // d/duP, d/dtau, d/dg and returns the scalars lambda is built from.
 template <typename T>
-__device__ __forceinline__ CellAdj<T> adjoint_cell(const T (&f)[Q], const T (&mu)[Q], int n, T B, double dBdtau,
+__device__ __forceinline__ CellAdj<T> adjoint_cell(const T (&f)[Q], const T (&mu)[Q], int n, T B, T dBdtau,
                                                    const T (&uP)[3], const T (&a)[3], T omega, const T (&g)[3],
-                                                   T (&guP)[3], double& gtau, double (&gg)[3]) {
+                                                   T (&guP)[3], T& gtau, T (&gg)[3]) {
     CellAdj<T> R;
     // pre-collision moments
     T rb = T(0), j0 = T(0), j1 = T(0), j2 = T(0);
@@ -160,37 +160,53 @@ __device__ __forceinline__ CellAdj<T> adjoint_cell(const T (&f)[Q], const T (&mu
         grhos -= rs * rs * grs;
         R.grbs = se + sE + grhos;
         R.gjs0 = gjs0; R.gjs1 = gjs1; R.gjs2 = gjs2;
-        gtau += (double)gB * dBdtau;
+        gtau += gB * dBdtau;
     }
 
     R.grb = T(0); R.gJ0 = T(0); R.gJ1 = T(0); R.gJ2 = T(0);
     if (n == 125) return R;   // no BGK: f* = f
-    // BGK reverse with phi_k = sB mu_k + grbs + c_k . gjs
-    T gom = T(0), sh = T(0), gr = T(0), gJ0 = T(0), gJ1 = T(0), gJ2 = T(0), gpre = T(0);
-    T gu0 = T(0), gu1 = T(0), gu2 = T(0);
-    T gg0 = T(0), gg1 = T(0), gg2 = T(0), swp = T(0);
+    // BGK reverse with phi_k = sB mu_k + grbs + c_k . gjs.  Every term is a
+    // weighted moment of phi of order <= 2 in c_k (feq and src are quadratic in
+    // c_k), so the sums over k reduce to m0 = sum t_k phi_k, m1 = sum t_k phi_k c_k,
+    // m2 = sum t_k phi_k c_k c_k^T, and sum phi_k f_k.
+    T m0 = T(0), m1x = T(0), m1y = T(0), m1z = T(0);
+    T mxx = T(0), myy = T(0), mzz = T(0), mxy = T(0), mxz = T(0), myz = T(0), sphf = T(0);
 #pragma unroll
     for (int k = 0; k < Q; ++k) {
         const T phi = R.sB * mu[k] + R.grbs + cdotT<T>(k, R.gjs0, R.gjs1, R.gjs2);
-        const T w = T(wt(k));
-        const T cJ = cdotT<T>(k, J0, J1, J2v);
-        const T cu = cdotT<T>(k, u0, u1, u2), cg = cdotT<T>(k, g[0], g[1], g[2]);
-        const T fe = feqT<T>(k, rb, r, cJ, JJ);
-        gom += phi * (fe - f[k]);
-        const T h = omega * phi;
-        sh += w * h;
-        gr += w * h * (T(4.5) * cJ * cJ - T(1.5) * JJ);
-        const T aJ = w * h * (T(3) + T(9) * r * cJ);
-        gpre += w * phi * (T(3) * (cg - ug) + T(9) * cu * cg);
-        const T wp = w * pre * phi;
-        swp += wp;
-        // d src / du = w pre (-3 g + 9 (c.g) c);  d src / dg = w pre (3 c - 3 u + 9 (c.u) c)
-        const T au = T(9) * wp * cg, ag = wp * (T(3) + T(9) * cu);
-        if (cx(k)) { const T sg = cx(k) > 0 ? T(1) : T(-1); gJ0 += sg * aJ; gu0 += sg * au; gg0 += sg * ag; }
-        if (cy(k)) { const T sg = cy(k) > 0 ? T(1) : T(-1); gJ1 += sg * aJ; gu1 += sg * au; gg1 += sg * ag; }
-        if (cz(k)) { const T sg = cz(k) > 0 ? T(1) : T(-1); gJ2 += sg * aJ; gu2 += sg * au; gg2 += sg * ag; }
+        sphf += phi * f[k];
+        const T wp = T(wt(k)) * phi;
+        m0 += wp;
+        const int X = cx(k), Y = cy(k), Z = cz(k);
+        if (X) { m1x += X > 0 ? wp : -wp; mxx += wp; }
+        if (Y) { m1y += Y > 0 ? wp : -wp; myy += wp; }
+        if (Z) { m1z += Z > 0 ? wp : -wp; mzz += wp; }
+        if (X && Y) mxy += X * Y > 0 ? wp : -wp;
+        if (X && Z) mxz += X * Z > 0 ? wp : -wp;
+        if (Y && Z) myz += Y * Z > 0 ? wp : -wp;
     }
-    // the k-independent parts summed once: -3 r J (sum w h), -3 g (sum w pre phi), -3 u (sum w pre phi)
+    // m2 applied to J, u, g
+    const T aJ0 = mxx * J0 + mxy * J1 + mxz * J2v, aJ1 = mxy * J0 + myy * J1 + myz * J2v,
+            aJ2 = mxz * J0 + myz * J1 + mzz * J2v;
+    const T ag0 = mxx * g[0] + mxy * g[1] + mxz * g[2], ag1 = mxy * g[0] + myy * g[1] + myz * g[2],
+            ag2 = mxz * g[0] + myz * g[1] + mzz * g[2];
+    const T au0 = mxx * u0 + mxy * u1 + mxz * u2, au1 = mxy * u0 + myy * u1 + myz * u2,
+            au2 = mxz * u0 + myz * u1 + mzz * u2;
+    const T JmJ = J0 * aJ0 + J1 * aJ1 + J2v * aJ2;
+    const T quad = T(4.5) * JmJ - T(1.5) * JJ * m0;            // sum t phi (4.5 (c.J)^2 - 1.5 J.J)
+    // sum phi_k feq_k - sum phi_k f_k
+    T gom = rb * m0 + T(3) * (m1x * J0 + m1y * J1 + m1z * J2v) + r * quad - sphf;
+    const T sh = omega * m0;                                       // sum t_k h_k, h = omega phi
+    T gr = omega * quad;
+    T gJ0 = omega * (T(3) * m1x + T(9) * r * aJ0), gJ1 = omega * (T(3) * m1y + T(9) * r * aJ1),
+      gJ2 = omega * (T(3) * m1z + T(9) * r * aJ2);
+    const T gpre = T(3) * (m1x * g[0] + m1y * g[1] + m1z * g[2]) - T(3) * ug * m0 +
+                   T(9) * (u0 * ag0 + u1 * ag1 + u2 * ag2);
+    const T swp = pre * m0;                                        // sum t_k pre phi_k
+    T gu0 = T(9) * pre * ag0, gu1 = T(9) * pre * ag1, gu2 = T(9) * pre * ag2;
+    T gg0 = pre * (T(3) * m1x + T(9) * au0), gg1 = pre * (T(3) * m1y + T(9) * au1),
+      gg2 = pre * (T(3) * m1z + T(9) * au2);
+    // the k-independent parts: -3 r J (sum t h), -3 g (sum t pre phi), -3 u (sum t pre phi)
     gJ0 -= T(3) * r * sh * J0; gJ1 -= T(3) * r * sh * J1; gJ2 -= T(3) * r * sh * J2v;
     gu0 -= T(3) * swp * g[0]; gu1 -= T(3) * swp * g[1]; gu2 -= T(3) * swp * g[2];
     gg0 -= T(3) * swp * u0; gg1 -= T(3) * swp * u1; gg2 -= T(3) * swp * u2;
@@ -206,14 +222,15 @@ __device__ __forceinline__ CellAdj<T> adjoint_cell(const T (&f)[Q], const T (&mu
     grho -= r * r * gr;
     R.grb = sh + grho;
     R.gJ0 = gJ0; R.gJ1 = gJ1; R.gJ2 = gJ2;
-    gtau -= (double)gom * (double)omega * (double)omega;   // omega = 1/tau
-    gg[0] += (double)gg0; gg[1] += (double)gg1; gg[2] += (double)gg2;
+    gtau -= gom * omega * omega;   // omega = 1/tau
+    gg[0] += gg0; gg[1] += gg1; gg[2] += gg2;
     return R;
 }
 
 // Warp-segmented sum of six values per particle slot into out[key][6]
 // (consecutive cells mostly share the owner).  All 32 lanes must call.
-__device__ __forceinline__ void reduce6(int key, double (&v)[6], double* __restrict__ out) {
+template <typename T>
+__device__ __forceinline__ void reduce6(int key, T (&v)[6], double* __restrict__ out) {
     const unsigned solid = __ballot_sync(FULLMASK, key >= 0);
     if (solid == 0u) return;
     const int lane = threadIdx.x & 31;
@@ -225,7 +242,7 @@ __device__ __forceinline__ void reduce6(int key, double (&v)[6], double* __restr
     for (int d = 1; d < 32; d <<= 1) {
 #pragma unroll
         for (int q = 0; q < 6; ++q) {
-            const double o = __shfl_up_sync(FULLMASK, v[q], d);
+            const T o = __shfl_up_sync(FULLMASK, v[q], d);
             if (lane - d >= segStart) v[q] += o;
         }
     }
@@ -233,7 +250,7 @@ __device__ __forceinline__ void reduce6(int key, double (&v)[6], double* __restr
     const bool tail = (lane == 31) || (nextKey != key);
     if (tail && key >= 0)
 #pragma unroll
-        for (int q = 0; q < 6; ++q) atomicAdd(out + 6 * (size_t)key + q, v[q]);
+        for (int q = 0; q < 6; ++q) atomicAdd(out + 6 * (size_t)key + q, (double)v[q]);
 }
 
 template <typename T>
@@ -241,12 +258,12 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_step(const AdjointArgs<
     __shared__ double s_red[ADJ_THREADS / 32][4];
     const Geom g = A.g;
     const size_t N = g.N;
-    double gtau = 0.0, gg[3] = {0.0, 0.0, 0.0};
+    T gtau = T(0), gg[3] = {T(0), T(0), T(0)};   // per-thread sums, widened once
     const size_t stride = (size_t)gridDim.x * blockDim.x;
     const size_t total = (N + 31) / 32 * 32;   // whole warps for the shuffles
     for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < total; c += stride) {
         int key = -1;
-        double pv[6] = {0, 0, 0, 0, 0, 0};
+        T pv[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
         if (c < N) {
             const int z = (int)(c % g.nz);
             const size_t rr = c / g.nz;
@@ -267,10 +284,8 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_step(const AdjointArgs<
             }
             const uint32_t w = A.vox[c];
             int n = min((int)(w & VOX_NMASK), 125);
-            T uP[3] = {T(0), T(0), T(0)}, a[3] = {T(0), T(0), T(0)};
-            double d[3] = {0, 0, 0};
-            T B = T(0);
-            double dBdtau = 0.0;
+            T uP[3] = {T(0), T(0), T(0)}, a[3] = {T(0), T(0), T(0)}, d[3] = {T(0), T(0), T(0)};
+            T B = T(0), dBdtau = T(0);
             int slot = -1;
             if (n > 0) {
                 const int tag = (int)(w >> VOX_NBITS);
@@ -280,28 +295,41 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_step(const AdjointArgs<
                     slot = -1;
                 } else {
                     const double* p = A.rec + (size_t)slot * REC_STRIDE;
-                    const int pos[3] = {x, y, z}, ext[3] = {g.nx, g.ny, g.nz};
+                    // arm d = cell - centre, minimum image as in the force arm
+                    // (src/ibProcessors3D.hh:230-243); the float form takes the
+                    // centre's hi/lo split as the forward pass does
+                    if (sizeof(T) == 8) {
+                        d[0] = T((double)x - p[0]); d[1] = T((double)y - p[1]); d[2] = T((double)z - p[2]);
+                    } else {
+                        const float4* q4 = reinterpret_cast<const float4*>(A.xpf) + 2 * (size_t)slot;
+                        const float4 hq = q4[0], lq = q4[1];
+                        d[0] = T(((float)x - hq.x) - hq.w);
+                        d[1] = T(((float)y - hq.y) - lq.x);
+                        d[2] = T(((float)z - hq.z) - lq.y);
+                    }
+                    const int ext[3] = {g.nx, g.ny, g.nz};
 #pragma unroll
                     for (int q = 0; q < 3; ++q) {
-                        // minimum image as in the force arm (src/ibProcessors3D.hh:230-243)
-                        double dq = (double)pos[q] - p[q];
                         const int h = ext[q] / 2;
-                        if (dq > (double)h) dq -= (double)ext[q];
-                        else if (dq < (double)(-h)) dq += (double)ext[q];
-                        d[q] = dq;
+                        if (d[q] > T(h)) d[q] -= T(ext[q]);
+                        else if (d[q] < T(-h)) d[q] += T(ext[q]);
                     }
+                    const T v0 = T(p[3]), v1 = T(p[4]), v2 = T(p[5]);
+                    const T w0 = T(p[6]), w1 = T(p[7]), w2 = T(p[8]);
                     // uP = v + w x d (setValues, src/ibProcessors3D.hh:163-174)
-                    uP[0] = T(p[3] + (p[7] * d[2] - p[8] * d[1]));
-                    uP[1] = T(p[4] + (-p[6] * d[2] + p[8] * d[0]));
-                    uP[2] = T(p[5] + (p[6] * d[1] - p[7] * d[0]));
+                    uP[0] = v0 + (w1 * d[2] - w2 * d[1]);
+                    uP[1] = v1 + (-w0 * d[2] + w2 * d[0]);
+                    uP[2] = v2 + (w0 * d[1] - w1 * d[0]);
                     const double* wgt = A.w + (size_t)slot * 6;
+                    const T wf0 = T(wgt[0]), wf1 = T(wgt[1]), wf2 = T(wgt[2]);
+                    const T wt0 = T(wgt[3]), wt1 = T(wgt[4]), wt2 = T(wgt[5]);
                     // dL/dF_cell = w_F + w_T x d
-                    a[0] = T(wgt[0] + (wgt[4] * d[2] - wgt[5] * d[1]));
-                    a[1] = T(wgt[1] + (wgt[5] * d[0] - wgt[3] * d[2]));
-                    a[2] = T(wgt[2] + (wgt[3] * d[1] - wgt[4] * d[0]));
+                    a[0] = wf0 + (wt1 * d[2] - wt2 * d[1]);
+                    a[1] = wf1 + (wt2 * d[0] - wt0 * d[2]);
+                    a[2] = wf2 + (wt0 * d[1] - wt1 * d[0]);
                     B = A.btab[n];
-                    const double sf = (1. / 125.) * (double)n, ooo = A.tau - 0.5, den = (1. - sf) + ooo;
-                    dBdtau = n < 125 ? sf * (1. - sf) / (den * den) : 0.0;
+                    const T sf = T(1.0 / 125.0) * T(n), den = (T(1) - sf) + (A.tauT - T(0.5));
+                    dBdtau = n < 125 ? sf * (T(1) - sf) / (den * den) : T(0);
                 }
             }
             if (n > 0 && slot < 0) n = 0;
@@ -318,19 +346,18 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_step(const AdjointArgs<
             }
             if (slot >= 0) {
                 key = slot;
-                const double u0 = (double)guP[0], u1 = (double)guP[1], u2 = (double)guP[2];
-                pv[0] = u0; pv[1] = u1; pv[2] = u2;
+                pv[0] = guP[0]; pv[1] = guP[1]; pv[2] = guP[2];
                 // d/dw of w x d: d x guP
-                pv[3] = d[1] * u2 - d[2] * u1;
-                pv[4] = d[2] * u0 - d[0] * u2;
-                pv[5] = d[0] * u1 - d[1] * u0;
+                pv[3] = d[1] * guP[2] - d[2] * guP[1];
+                pv[4] = d[2] * guP[0] - d[0] * guP[2];
+                pv[5] = d[0] * guP[1] - d[1] * guP[0];
             }
         }
         reduce6(key, pv, A.gvel);
     }
     // block sums of d/dg and d/dtau, one atomic per block and value
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    double v4[4] = {gg[0], gg[1], gg[2], gtau};
+    double v4[4] = {(double)gg[0], (double)gg[1], (double)gg[2], (double)gtau};
 #pragma unroll
     for (int q = 0; q < 4; ++q)
         for (int o = 16; o > 0; o >>= 1) v4[q] += __shfl_down_sync(FULLMASK, v4[q], o);

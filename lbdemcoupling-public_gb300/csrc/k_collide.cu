@@ -541,7 +541,8 @@ k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const Coll
         const CollideArgs<T>& a = BATCH ? dargs[st.geo[b][4]] : a1;
         const Geom& g = a.g;
         const size_t N = g.N;
-        T* __restrict__ F = a.f;
+        const T* Fin = a.f;   // input populations
+        T* F = a.fo;          // output populations (== a.f in place)
         const size_t own = (size_t)st.row[b][row_slot(0, 0)];
         const unsigned long long lead = MIS ? st.lead[b] : 0ull;
         if (MIS && ODD) {
@@ -561,8 +562,8 @@ k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const Coll
             if (lane < 10) {
                 const int i = zdir(lane);
                 if (st.row[b][row_slot(-cx(i), -cy(i))] >= 0) {
-                    if (cz(i) > 0 && z0 == 0) st.f[b][i][V - 1] = F[(size_t)i * N + own];
-                    if (cz(i) < 0 && z0 + len == g.nz) st.f[b][i][V + len] = F[(size_t)i * N + own + g.nz - 1];
+                    if (cz(i) > 0 && z0 == 0) st.f[b][i][V - 1] = Fin[(size_t)i * N + own];
+                    if (cz(i) < 0 && z0 + len == g.nz) st.f[b][i][V + len] = Fin[(size_t)i * N + own + g.nz - 1];
                 }
             }
             __syncwarp();

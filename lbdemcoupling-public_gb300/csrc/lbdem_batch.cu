@@ -196,6 +196,7 @@ void fill_dargs(lbdem_batch* b, std::vector<CollideArgs<T>>& out, T* f_base, dou
         a = CollideArgs<T>{};
         a.g = v.g;
         a.f = f_base + v.f0;
+        a.fo = a.f;
         a.vox = b->vox + v.cell0;
         a.up = (const T*)b->up + v.up0;
         a.cf = nullptr;

@@ -204,6 +204,30 @@ PlaneJob make_job(const lbdem_handle* h, const int32_t* box, int dim, int dir, d
     return j;
 }
 
+// One collide-stream launch of the handle reading populations fin and writing
+// fout (fin == fout: the in-place step; otherwise an out-of-place step into an
+// array of the same layout).  Particle state, force sums and the step parity
+// are the handle's.
+cudaError_t k1_launch(lbdem_handle* h, void* fin, void* fout) {
+    const bool odd = (h->step & 1) != 0;
+    const bool force = h->cfg.body_force[0] != 0.0 || h->cfg.body_force[1] != 0.0 || h->cfg.body_force[2] != 0.0;
+    const int n = h->n_cur;
+    if (h->prec == LBDEM_PREC_FP64) {
+        CollideArgs<double> a;
+        a.g = h->g; a.f = (double*)fin; a.fo = (double*)fout; a.vox = h->vox; a.up = (const double*)h->up;
+        a.cf = (double*)h->cf; a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.xpf = h->d_xpf; a.nslot = n;
+        a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err; a.btab = h->btab; a.omega = h->cfg.omega;
+        for (int d = 0; d < 3; ++d) a.g3[d] = h->cfg.body_force[d];
+        return launch_collide_stream<double>(a, odd, force, h->stream);
+    }
+    CollideArgs<float> a;
+    a.g = h->g; a.f = (float*)fin; a.fo = (float*)fout; a.vox = h->vox; a.up = (const float*)h->up;
+    a.cf = (float*)h->cf; a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.xpf = h->d_xpf; a.nslot = n;
+    a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err; a.btab = h->btabf; a.omega = (float)h->cfg.omega;
+    for (int d = 0; d < 3; ++d) a.g3[d] = (float)h->cfg.body_force[d];
+    return launch_collide_stream<float>(a, odd, force, h->stream);
+}
+
 cudaError_t plane_launch(lbdem_handle* h, const PlaneJob* jobs, int njobs, int bpj, int phase, int rescale,
                          const double* avg_in, double* avg_out) {
     if (h->prec == LBDEM_PREC_FP64)
@@ -470,29 +494,13 @@ lbdem_status lbdem_collide_and_stream(lbdem_handle* h) {
     DeviceGuard dg(h->device);
     const int n = h->n_cur;
     if (n > 0) CK(h, cudaMemsetAsync(h->d_ft, 0, 6 * (size_t)n * sizeof(double), h->stream));
-    const bool odd = (h->step & 1) != 0;
-    const bool force = h->cfg.body_force[0] != 0.0 || h->cfg.body_force[1] != 0.0 || h->cfg.body_force[2] != 0.0;
-    const int P = odd ? 1 : 0;
+    const int P = (int)(h->step & 1);
     if (h->pdrop_on && !h->pavg_valid) {
         // averages of the state before the step (computeAverageDensity before collideAndStream)
         CK(h, plane_launch(h, h->d_jobs, 2, h->pdrop_bpj, P, 0, nullptr, h->d_pavg + 4 * P));
         h->launches += 1;
     }
-    if (h->prec == LBDEM_PREC_FP64) {
-        CollideArgs<double> a;
-        a.g = h->g; a.f = (double*)h->f; a.vox = h->vox; a.up = (const double*)h->up; a.cf = (double*)h->cf;
-        a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.xpf = h->d_xpf; a.nslot = n; a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err;
-        a.btab = h->btab; a.omega = h->cfg.omega;
-        for (int d = 0; d < 3; ++d) a.g3[d] = h->cfg.body_force[d];
-        CK(h, launch_collide_stream<double>(a, odd, force, h->stream));
-    } else {
-        CollideArgs<float> a;
-        a.g = h->g; a.f = (float*)h->f; a.vox = h->vox; a.up = (const float*)h->up; a.cf = (float*)h->cf;
-        a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.xpf = h->d_xpf; a.nslot = n; a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err;
-        a.btab = h->btabf; a.omega = (float)h->cfg.omega;
-        for (int d = 0; d < 3; ++d) a.g3[d] = (float)h->cfg.body_force[d];
-        CK(h, launch_collide_stream<float>(a, odd, force, h->stream));
-    }
+    CK(h, k1_launch(h, h->f, h->f));
     h->launches += 1;
     if (h->pdrop_on) {
         // rescale of the streamed populations with the pre-step averages; the same
@@ -787,12 +795,13 @@ cudaError_t adjoint_launch(lbdem_handle* h, const T* f, int phase, const T* lam_
     a.max_tag = h->cfg.max_tag;
     a.nslot = n;
     a.rec = rec;
+    a.xpf = h->d_xpf;
     a.w = w;
     a.gvel = gvel;
     a.gglob = gglob;
     a.btab = sizeof(T) == 8 ? (const T*)h->btab : (const T*)h->btabf;
     a.omega = (T)h->cfg.omega;
-    a.tau = 1.0 / h->cfg.omega;
+    a.tauT = (T)(1.0 / h->cfg.omega);
     for (int d = 0; d < 3; ++d) a.g3[d] = (T)h->cfg.body_force[d];
     a.err = h->d_err;
     return launch_adjoint_step<T>(a, h->stream);
@@ -827,7 +836,7 @@ lbdem_status lbdem_adjoint_window(lbdem_handle* h, int32_t nsteps, int32_t K, in
     const size_t nrec = (size_t)nsteps * n;
     AdjointBuffers buf;
     double *d_recs = nullptr, *d_w = nullptr, *d_gv = nullptr, *d_glob = nullptr, *d_loss = nullptr, *d_ft = nullptr;
-    unsigned char *ckpt = nullptr, *tape = nullptr, *lam = nullptr, *work = nullptr;
+    unsigned char *ckpt = nullptr, *tape = nullptr, *lam = nullptr;
     CK(h, buf.get(&d_recs, nrec * REC_STRIDE * sizeof(double)));
     CK(h, buf.get(&d_w, nrec * 6 * sizeof(double)));
     CK(h, buf.get(&d_gv, nrec * 6 * sizeof(double)));
@@ -835,9 +844,8 @@ lbdem_status lbdem_adjoint_window(lbdem_handle* h, int32_t nsteps, int32_t K, in
     CK(h, buf.get(&d_loss, sizeof(double)));
     CK(h, buf.get(&d_ft, 6 * (size_t)std::max(n, 1) * sizeof(double)));
     CK(h, buf.get(&ckpt, (size_t)nseg * pop));
-    CK(h, buf.get(&tape, (size_t)K * pop));
+    CK(h, buf.get(&tape, (size_t)K * pop + ALLOC_TAIL));
     CK(h, buf.get(&lam, 2 * pop));
-    CK(h, buf.get(&work, pop + ALLOC_TAIL));
     EventPair ev;
     for (auto& e : ev.e) CK(h, cudaEventCreate(&e));
     if (n > 0) {
@@ -848,7 +856,7 @@ lbdem_status lbdem_adjoint_window(lbdem_handle* h, int32_t nsteps, int32_t K, in
     CK(h, cudaMemsetAsync(d_glob, 0, 4 * sizeof(double), s));
     CK(h, cudaMemsetAsync(d_loss, 0, sizeof(double), s));
     CK(h, cudaMemsetAsync(lam, 0, pop, s));        // lambda after the window = 0
-    CK(h, cudaMemsetAsync(work + pop, 0, ALLOC_TAIL, s));
+    CK(h, cudaMemsetAsync(tape + (size_t)K * pop, 0, ALLOC_TAIL, s));
     const int64_t step0 = h->step;
     lbdem_status st;
 
@@ -867,23 +875,26 @@ lbdem_status lbdem_adjoint_window(lbdem_handle* h, int32_t nsteps, int32_t K, in
     if (n > 0) CK(h, cudaMemcpyAsync(d_ft, h->d_ft, 6 * (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
 
     // backward pass: recompute each segment into the tape, then reverse steps
-    void* f_final = h->f;
-    h->f = work;
     unsigned char* lam_in = lam;
     unsigned char* lam_out = lam + pop;
     lbdem_status bst = LBDEM_OK;
     for (int seg = nseg - 1; seg >= 0 && bst == LBDEM_OK; --seg) {
         const int t0 = seg * K, t1 = std::min(t0 + K, nsteps);
-        cudaError_t e = cudaMemcpyAsync(work, ckpt + (size_t)seg * pop, pop, cudaMemcpyDeviceToDevice, s);
+        // tape[0] = the segment's checkpoint; every recomputed step writes its
+        // output straight into the next tape slot (out-of-place collide-stream)
+        cudaError_t e = cudaMemcpyAsync(tape, ckpt + (size_t)seg * pop, pop, cudaMemcpyDeviceToDevice, s);
         if (e != cudaSuccess) { bst = fail_cuda(h, "adjoint checkpoint restore", e); break; }
         h->step = step0 + t0;
-        for (int t = t0; t < t1 && bst == LBDEM_OK; ++t) {
-            e = cudaMemcpyAsync(tape + (size_t)(t - t0) * pop, work, pop, cudaMemcpyDeviceToDevice, s);
-            if (e != cudaSuccess) { bst = fail_cuda(h, "adjoint tape", e); break; }
-            if (t + 1 < t1) {   // the state after the segment's last step is not needed
-                if ((bst = lbdem_set_particles_device(h, n, d_recs + (size_t)t * n * REC_STRIDE, 0)) != LBDEM_OK) break;
-                bst = lbdem_collide_and_stream(h);
+        for (int t = t0; t + 1 < t1 && bst == LBDEM_OK; ++t) {
+            if ((bst = lbdem_set_particles_device(h, n, d_recs + (size_t)t * n * REC_STRIDE, 0)) != LBDEM_OK) break;
+            if (n > 0) {
+                e = cudaMemsetAsync(h->d_ft, 0, 6 * (size_t)n * sizeof(double), s);
+                if (e != cudaSuccess) { bst = fail_cuda(h, "adjoint force reset", e); break; }
             }
+            e = k1_launch(h, tape + (size_t)(t - t0) * pop, tape + (size_t)(t - t0 + 1) * pop);
+            if (e != cudaSuccess) { bst = fail_cuda(h, "adjoint recompute", e); break; }
+            h->launches += 1;
+            h->step += 1;
         }
         for (int t = t1 - 1; t >= t0 && bst == LBDEM_OK; --t) {
             const int phase = (int)((step0 + t) & 1);
@@ -901,7 +912,6 @@ lbdem_status lbdem_adjoint_window(lbdem_handle* h, int32_t nsteps, int32_t K, in
             std::swap(lam_in, lam_out);
         }
     }
-    h->f = f_final;
     h->step = step0 + nsteps;
     if (bst != LBDEM_OK) return bst;
     CK(h, cudaEventRecord(ev.e[2], s));

@@ -64,6 +64,8 @@ template <typename T>
 struct CollideArgs {
     Geom g;
     T* f;                    // [19][N] populations, AA in-place layout
+    T* fo;                   // where the step's output goes: f itself (in place) or a second
+                             // array of the same layout (an out-of-place step)
     const uint32_t* vox;     // [N] n | tag << 7
     const T* up;             // [3][N] particle surface velocity
     T* cf;                   // [3][N] per-cell force (nullptr: not kept)
@@ -214,12 +216,13 @@ struct AdjointArgs {
     const int* tag2slot;
     int max_tag, nslot;
     const double* rec;       // [nslot][12] particle records of the step
+    const float* xpf;        // [nslot][8] centres split into float hi/lo (float form's arm)
     const double* w;         // [nslot][6] dL/dF, dL/dT of the step
     double* gvel;            // [nslot][6] += dL/dv, dL/domega of the step
     double* gglob;           // [4] += dL/dg, dL/dtau
     const T* btab;           // B(n)
     T omega;
-    double tau;
+    T tauT;                  // tau = 1 / omega in the lattice type
     T g3[3];
     unsigned* err;
 };
