@@ -46,6 +46,16 @@ __device__ __forceinline__ T cdotT(int k, T a, T b, T c) {
     return r;
 }
 
+// 1/x: IEEE division in float; in double a float reciprocal refined by two
+// Newton-Raphson steps r <- r (2 - x r) (relative error ~2^-23 -> ~2^-46 -> below
+// double rounding), far cheaper than a double division on the narrow FP64 pipe.
+__device__ __forceinline__ float recipT(float x) { return 1.0f / x; }
+__device__ __forceinline__ double recipT(double x) {
+    double r = (double)(1.0f / (float)x);
+    r = r * (2.0 - x * r);
+    return r * (2.0 - x * r);
+}
+
 template <typename T>
 __device__ __forceinline__ T feqT(int k, T rb, T r, T c_dot, T sq) {
     return T(wt(k)) * (rb + T(3) * c_dot + r * (T(4.5) * c_dot * c_dot - T(1.5) * sq));
@@ -79,7 +89,7 @@ __device__ __forceinline__ CellAdj<T> adjoint_cell(const T (&f)[Q], const T (&mu
         if (cy(k)) j1 += cy(k) > 0 ? f[k] : -f[k];
         if (cz(k)) j2 += cz(k) > 0 ? f[k] : -f[k];
     }
-    const T rho = T(1) + rb, r = T(1) / rho;
+    const T rho = T(1) + rb, r = recipT(rho);
     const T J0 = j0 + T(0.5) * rho * g[0], J1 = j1 + T(0.5) * rho * g[1], J2v = j2 + T(0.5) * rho * g[2];
     const T u0 = J0 * r, u1 = J1 * r, u2 = J2v * r;
     const T JJ = J0 * J0 + J1 * J1 + J2v * J2v;
@@ -111,7 +121,7 @@ __device__ __forceinline__ CellAdj<T> adjoint_cell(const T (&f)[Q], const T (&mu
         }
         R.B = B;
         R.sB = T(1) - B;
-        const T rhos = T(1) + rbs, rs = T(1) / rhos;
+        const T rhos = T(1) + rbs, rs = recipT(rhos);
         const T Jq = js0 * js0 + js1 * js1 + js2 * js2;
         const T P0 = rhos * uP[0], P1 = rhos * uP[1], P2v = rhos * uP[2];
         const T PP = P0 * P0 + P1 * P1 + P2v * P2v;
@@ -171,20 +181,24 @@ __device__ __forceinline__ CellAdj<T> adjoint_cell(const T (&f)[Q], const T (&mu
     // m2 = sum t_k phi_k c_k c_k^T, and sum phi_k f_k.
     T m0 = T(0), m1x = T(0), m1y = T(0), m1z = T(0);
     T mxx = T(0), myy = T(0), mzz = T(0), mxy = T(0), mxz = T(0), myz = T(0), sphf = T(0);
+    auto moments = [&](auto phi_of) {
 #pragma unroll
-    for (int k = 0; k < Q; ++k) {
-        const T phi = R.sB * mu[k] + R.grbs + cdotT<T>(k, R.gjs0, R.gjs1, R.gjs2);
-        sphf += phi * f[k];
-        const T wp = T(wt(k)) * phi;
-        m0 += wp;
-        const int X = cx(k), Y = cy(k), Z = cz(k);
-        if (X) { m1x += X > 0 ? wp : -wp; mxx += wp; }
-        if (Y) { m1y += Y > 0 ? wp : -wp; myy += wp; }
-        if (Z) { m1z += Z > 0 ? wp : -wp; mzz += wp; }
-        if (X && Y) mxy += X * Y > 0 ? wp : -wp;
-        if (X && Z) mxz += X * Z > 0 ? wp : -wp;
-        if (Y && Z) myz += Y * Z > 0 ? wp : -wp;
-    }
+        for (int k = 0; k < Q; ++k) {
+            const T phi = phi_of(k);
+            sphf += phi * f[k];
+            const T wp = T(wt(k)) * phi;
+            m0 += wp;
+            const int X = cx(k), Y = cy(k), Z = cz(k);
+            if (X) { m1x += X > 0 ? wp : -wp; mxx += wp; }
+            if (Y) { m1y += Y > 0 ? wp : -wp; myy += wp; }
+            if (Z) { m1z += Z > 0 ? wp : -wp; mzz += wp; }
+            if (X && Y) mxy += X * Y > 0 ? wp : -wp;
+            if (X && Z) mxz += X * Z > 0 ? wp : -wp;
+            if (Y && Z) myz += Y * Z > 0 ? wp : -wp;
+        }
+    };
+    if (n == 0) moments([&](int k) { return mu[k]; });   // fluid cell: phi = mu
+    else moments([&](int k) { return R.sB * mu[k] + R.grbs + cdotT<T>(k, R.gjs0, R.gjs1, R.gjs2); });
     // m2 applied to J, u, g
     const T aJ0 = mxx * J0 + mxy * J1 + mxz * J2v, aJ1 = mxy * J0 + myy * J1 + myz * J2v,
             aJ2 = mxz * J0 + myz * J1 + mzz * J2v;
@@ -259,28 +273,56 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_step(const AdjointArgs<
     const Geom g = A.g;
     const size_t N = g.N;
     T gtau = T(0), gg[3] = {T(0), T(0), T(0)};   // per-thread sums, widened once
-    const size_t stride = (size_t)gridDim.x * blockDim.x;
-    const size_t total = (N + 31) / 32 * 32;   // whole warps for the shuffles
-    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < total; c += stride) {
+    // one warp per 32-cell run of a z-row: rows * runs < 2^31 (nx * ny < 2^31 is
+    // checked at creation), so all index arithmetic stays in 32 bits
+    const int lane = threadIdx.x & 31;
+    const int nzc = (g.nz + 31) >> 5;
+    const long long nchunks = (long long)g.nx * g.ny * nzc;
+    const long long wstride = (long long)gridDim.x * (ADJ_THREADS / 32);
+    for (long long q = (long long)blockIdx.x * (ADJ_THREADS / 32) + (threadIdx.x >> 5); q < nchunks; q += wstride) {
+        const int qi = (int)q;   // runs of 32 cells: < 2^31 for any lattice that fits in memory
+        const int row = qi / nzc;
+        const int z = (qi - row * nzc) * 32 + lane;
         int key = -1;
         T pv[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-        if (c < N) {
-            const int z = (int)(c % g.nz);
-            const size_t rr = c / g.nz;
-            const int y = (int)(rr % g.ny);
-            const int x = (int)(rr / g.ny);
-            T f[Q], mu[Q];
+        if (z < g.nz) {
+            const int x = row / g.ny;
+            const int y = row - x * g.ny;
+            const size_t c = (size_t)row * g.nz + z;
+            // neighbour coordinates (-1 beyond a wall) and the nine row offsets
+            const int xs[3] = {x > 0 ? x - 1 : (g.per[0] ? g.nx - 1 : -1), x, x < g.nx - 1 ? x + 1 : (g.per[0] ? 0 : -1)};
+            const int ys[3] = {y > 0 ? y - 1 : (g.per[1] ? g.ny - 1 : -1), y, y < g.ny - 1 ? y + 1 : (g.per[1] ? 0 : -1)};
+            const int zs[3] = {z > 0 ? z - 1 : (g.per[2] ? g.nz - 1 : -1), z, z < g.nz - 1 ? z + 1 : (g.per[2] ? 0 : -1)};
+            long long rowoff[9];
 #pragma unroll
-            for (int k = 0; k < Q; ++k) f[k] = A.f[slot_index(k, x, y, z, A.phase, g)];
+            for (int a = 0; a < 3; ++a)
+#pragma unroll
+                for (int b = 0; b < 3; ++b)
+                    rowoff[3 * a + b] = (xs[a] >= 0 && ys[b] >= 0) ? ((long long)xs[a] * g.ny + ys[b]) * g.nz : -1;
+            // cell x + (dx, dy, dz) as a linear index, or -1 beyond a wall
+            auto nb = [&](int dx, int dy, int dz) -> long long {
+                const long long r = rowoff[3 * (dx + 1) + dy + 1];
+                const int zz = zs[dz + 1];
+                return (r >= 0 && zz >= 0) ? r + zz : -1;
+            };
+            T f[Q], mu[Q];
+            if (A.phase == 0) {
+#pragma unroll
+                for (int k = 0; k < Q; ++k) f[k] = A.f[(size_t)k * N + c];
+            } else {
+                // odd layout: f_k(x) in slot (opp k, x - c_k), or (k, x) when x - c_k is beyond a wall
+                f[0] = A.f[c];
+#pragma unroll
+                for (int k = 1; k < Q; ++k) {
+                    const long long s2 = nb(-cx(k), -cy(k), -cz(k));
+                    f[k] = s2 >= 0 ? A.f[(size_t)opp(k) * N + (size_t)s2] : A.f[(size_t)k * N + c];
+                }
+            }
+            // transpose of push streaming: mu_k = lambda_k(x + c_k), or lambda_opp k(x) beyond a wall
 #pragma unroll
             for (int k = 0; k < Q; ++k) {
-                int X = x + cx(k), Y = y + cy(k), Z = z + cz(k);
-                bool out = false;
-                if (X < 0 || X >= g.nx) { if (g.per[0]) X = X < 0 ? X + g.nx : X - g.nx; else out = true; }
-                if (Y < 0 || Y >= g.ny) { if (g.per[1]) Y = Y < 0 ? Y + g.ny : Y - g.ny; else out = true; }
-                if (Z < 0 || Z >= g.nz) { if (g.per[2]) Z = Z < 0 ? Z + g.nz : Z - g.nz; else out = true; }
-                mu[k] = out ? A.lam_in[(size_t)opp(k) * N + c]
-                            : A.lam_in[(size_t)k * N + ((size_t)X * g.ny + Y) * g.nz + Z];
+                const long long s2 = k == 0 ? (long long)c : nb(cx(k), cy(k), cz(k));
+                mu[k] = s2 >= 0 ? A.lam_in[(size_t)k * N + (size_t)s2] : A.lam_in[(size_t)opp(k) * N + c];
             }
             const uint32_t w = A.vox[c];
             int n = min((int)(w & VOX_NMASK), 125);
@@ -337,12 +379,18 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_step(const AdjointArgs<
             const T gvec[3] = {A.g3[0], A.g3[1], A.g3[2]};
             const CellAdj<T> R = adjoint_cell<T>(f, mu, n, B, dBdtau, uP, a, A.omega, gvec, guP, gtau, gg);
             const T om1 = n == 125 ? T(1) : T(1) - A.omega;
+            if (n == 0) {   // fluid cell: phi = mu, no solid terms
 #pragma unroll
-            for (int k = 0; k < Q; ++k) {
-                const T phi = R.sB * mu[k] + R.grbs + cdotT<T>(k, R.gjs0, R.gjs1, R.gjs2);
-                T l = om1 * phi + R.grb + cdotT<T>(k, R.gJ0, R.gJ1, R.gJ2);
-                if (n > 0) l += R.B * mu[opp(k)] + T(2) * R.B * cdotT<T>(k, a[0], a[1], a[2]);
-                A.lam_out[(size_t)k * N + c] = l;
+                for (int k = 0; k < Q; ++k)
+                    A.lam_out[(size_t)k * N + c] = om1 * mu[k] + (R.grb + cdotT<T>(k, R.gJ0, R.gJ1, R.gJ2));
+            } else {
+#pragma unroll
+                for (int k = 0; k < Q; ++k) {
+                    const T phi = R.sB * mu[k] + R.grbs + cdotT<T>(k, R.gjs0, R.gjs1, R.gjs2);
+                    T l = om1 * phi + R.grb + cdotT<T>(k, R.gJ0, R.gJ1, R.gJ2);
+                    l += R.B * mu[opp(k)] + T(2) * R.B * cdotT<T>(k, a[0], a[1], a[2]);
+                    A.lam_out[(size_t)k * N + c] = l;
+                }
             }
             if (slot >= 0) {
                 key = slot;
@@ -356,7 +404,7 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_step(const AdjointArgs<
         reduce6(key, pv, A.gvel);
     }
     // block sums of d/dg and d/dtau, one atomic per block and value
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int warp = threadIdx.x >> 5;
     double v4[4] = {(double)gg[0], (double)gg[1], (double)gg[2], (double)gtau};
 #pragma unroll
     for (int q = 0; q < 4; ++q)

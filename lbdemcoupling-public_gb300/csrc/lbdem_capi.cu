@@ -859,12 +859,28 @@ lbdem_status lbdem_adjoint_window(lbdem_handle* h, int32_t nsteps, int32_t K, in
     CK(h, cudaMemsetAsync(tape + (size_t)K * pop, 0, ALLOC_TAIL, s));
     const int64_t step0 = h->step;
     lbdem_status st;
+    // A step whose particle table equals the one voxelized last needs no new
+    // voxelization: with positions fixed the update is idempotent (every cell's
+    // owner re-sets itself, no other sphere can displace it), so the voxel
+    // words, surface velocities and tag map are already those of the step.
+    int vox_t = -1;   // step whose table the voxel state holds
+    auto same_table = [&](int a, int b) {
+        return a >= 0 && b >= 0 &&
+               std::memcmp(rec + (size_t)a * n * REC_STRIDE, rec + (size_t)b * n * REC_STRIDE,
+                           (size_t)n * REC_STRIDE * sizeof(double)) == 0;
+    };
+    auto voxelize_for = [&](int t) -> lbdem_status {
+        if (same_table(vox_t, t)) return LBDEM_OK;
+        const lbdem_status r = lbdem_set_particles_device(h, n, d_recs + (size_t)t * n * REC_STRIDE, 0);
+        if (r == LBDEM_OK) vox_t = t;
+        return r;
+    };
 
     // forward pass with checkpoints
     CK(h, cudaEventRecord(ev.e[0], s));
     for (int t = 0; t < nsteps; ++t) {
         if (t % K == 0) CK(h, cudaMemcpyAsync(ckpt + (size_t)(t / K) * pop, h->f, pop, cudaMemcpyDeviceToDevice, s));
-        if ((st = lbdem_set_particles_device(h, n, d_recs + (size_t)t * n * REC_STRIDE, 0)) != LBDEM_OK) return st;
+        if ((st = voxelize_for(t)) != LBDEM_OK) return st;
         if ((st = lbdem_collide_and_stream(h)) != LBDEM_OK) return st;
         if (n > 0) {
             CK(h, launch_loss_step(h->d_ft, d_w + (size_t)t * n * 6, n, n, d_loss, s));
@@ -886,7 +902,7 @@ lbdem_status lbdem_adjoint_window(lbdem_handle* h, int32_t nsteps, int32_t K, in
         if (e != cudaSuccess) { bst = fail_cuda(h, "adjoint checkpoint restore", e); break; }
         h->step = step0 + t0;
         for (int t = t0; t + 1 < t1 && bst == LBDEM_OK; ++t) {
-            if ((bst = lbdem_set_particles_device(h, n, d_recs + (size_t)t * n * REC_STRIDE, 0)) != LBDEM_OK) break;
+            if ((bst = voxelize_for(t)) != LBDEM_OK) break;
             if (n > 0) {
                 e = cudaMemsetAsync(h->d_ft, 0, 6 * (size_t)n * sizeof(double), s);
                 if (e != cudaSuccess) { bst = fail_cuda(h, "adjoint force reset", e); break; }
@@ -916,8 +932,7 @@ lbdem_status lbdem_adjoint_window(lbdem_handle* h, int32_t nsteps, int32_t K, in
     if (bst != LBDEM_OK) return bst;
     CK(h, cudaEventRecord(ev.e[2], s));
     // the voxel state and the forces of the window's last step
-    if ((st = lbdem_set_particles_device(h, n, d_recs + (size_t)(nsteps - 1) * n * REC_STRIDE, 0)) != LBDEM_OK)
-        return st;
+    if ((st = voxelize_for(nsteps - 1)) != LBDEM_OK) return st;
     if (n > 0) CK(h, cudaMemcpyAsync(h->d_ft, d_ft, 6 * (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
 
     double glob[4];
