@@ -55,13 +55,8 @@ __global__ void __launch_bounds__(PLANE_THREADS)
     if (RESCALE) k = J.target / avg_in[J.read];
 
     double acc = 0;
-    for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
-         c += (long long)gridDim.x * blockDim.x) {
-        const int z = J.box[4] + (int)(c % ez);
-        const long long r = c / ez;
-        const int y = J.box[2] + (int)(r % ey);
-        const int x = J.box[0] + (int)(r / ey);
-        double rb = 0;
+    auto cell = [&](int x, int y, int z) {
+        T rb = T(0);   // the cell's rhoBar in the lattice type, widened once
 #pragma unroll
         for (int i = 0; i < Q; ++i) {
             const size_t s = slot_index(i, x, y, z, phase, J.g);
@@ -70,9 +65,23 @@ __global__ void __launch_bounds__(PLANE_THREADS)
                 v = rescale_pop<T>(v, wt(i), k);
                 f[s] = v;
             }
-            rb += (double)v;
+            rb += v;
         }
-        acc += rb;
+        acc += (double)rb;
+    };
+    if (ncell < 0x7fffffffLL) {   // planes: 32-bit index arithmetic
+        const int nc = (int)ncell;
+        for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x) {
+            const int r = c / ez;
+            const int yy = r % ey;
+            cell(J.box[0] + r / ey, J.box[2] + yy, J.box[4] + (c - r * ez));
+        }
+    } else {
+        for (long long c = (long long)blockIdx.x * blockDim.x + threadIdx.x; c < ncell;
+             c += (long long)gridDim.x * blockDim.x) {
+            const long long r = c / ez;
+            cell(J.box[0] + (int)(r / ey), J.box[2] + (int)(r % ey), J.box[4] + (int)(c % ez));
+        }
     }
 
     for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
