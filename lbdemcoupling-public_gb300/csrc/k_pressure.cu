@@ -47,12 +47,14 @@ __global__ void __launch_bounds__(PLANE_THREADS)
                      double* __restrict__ avg_out, double* __restrict__ partial, unsigned* __restrict__ count) {
     __shared__ double s_warp[PLANE_THREADS / 32];
     __shared__ bool s_last;
+    __shared__ double s_k;
     const PlaneJob J = jobs[blockIdx.y];
     T* __restrict__ f = (T*)J.f;
     const int ey = J.box[3] - J.box[2] + 1, ez = J.box[5] - J.box[4] + 1;
     const long long ncell = (long long)(J.box[1] - J.box[0] + 1) * ey * ez;
-    double k = 1.0;
-    if (RESCALE) k = J.target / avg_in[J.read];
+    if (RESCALE && threadIdx.x == 0) s_k = J.target / avg_in[J.read];   // one division per block
+    __syncthreads();
+    const double k = RESCALE ? s_k : 1.0;
 
     double acc = 0;
     auto cell = [&](int x, int y, int z) {

@@ -2,6 +2,8 @@
 
     python reports.py adjoint      # periodic 128^3, 64 spheres r = 6, 200 steps, checkpoint every 20
     python reports.py precision    # periodic 512x256x256, r ~ U[4, 10] to solid fraction 0.30, 2000 steps
+    python reports.py window [--steps S --checkpoint K --fp64]   # one adjoint window of the 128^3 case, timed
+    python reports.py channels [--steps S]                       # batched 512 channels, S coupling cycles
 
 Each prints one JSON object.  Inputs are seeded synthetic workloads
 (workloads.py); the FP64 form is the reference of the FP32 deviation form.
@@ -166,15 +168,54 @@ def precision(steps: int = 2000, seed: int = 2025, tau: float = 0.6, g=(1e-6, 0.
     return out
 
 
+def window(steps: int = 6, K: int = 3, fp64: bool = False, seed: int = 2027) -> dict:
+    """One adjoint window of the 128^3 case (x-force loss over every step), timed."""
+    shape = (128, 128, 128)
+    p = W.suspension(shape, n_max=64, radius=6.0, seed=seed)
+    gh = W.with_ghosts(p, shape)
+    rec = np.repeat(lbdem.pack_records(gh.x, gh.v, gh.w, gh.r, gh.tag)[None], steps, axis=0)
+    w = np.zeros((steps, gh.n, 6))
+    w[:, :p.n, 0] = 1.0
+    prec = lbdem.PREC_FP64 if fp64 else lbdem.PREC_FP32_DEV
+    with lbdem.Lattice(*shape, 1 / 0.6, precision=prec, body_force=(1e-6, 0, 0), max_particles=gh.n,
+                       max_tag=p.n + 1, max_radius=8.0) as L:
+        o = L.adjoint_window(rec, w, K)
+        fwd, bwd = L.adjoint_timing()
+    return {"steps": steps, "checkpoint_every": K, "form": "fp64" if fp64 else "fp32", "loss": o["loss"],
+            "forward_ms": fwd, "backward_ms": bwd}
+
+
+def channels(steps: int = 6) -> dict:
+    """The batched channels of workloads.channels stepped for a few coupling cycles."""
+    ch = W.channels()
+    doms = [d for d, _ in ch]
+    g = [W.with_ghosts(p, d["shape"], d["periodic"]) for d, p in ch]
+    counts = np.array([x.n for x in g], dtype=np.int32)
+    rec = np.concatenate([lbdem.pack_records(x.x, x.v, x.w, x.r, x.tag) for x in g])
+    with lbdem.Batch(doms, precision=lbdem.PREC_FP32_DEV, max_tag=64, max_radius=8.0, autotune=False) as B:
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            B.cycle(counts, rec)
+        secs = time.perf_counter() - t0
+        cells = B.cells()
+    return {"domains": len(doms), "cells": cells, "steps": steps, "mlups": cells * steps / secs / 1e6}
+
+
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("which", choices=["adjoint", "precision"])
+    ap.add_argument("which", choices=["adjoint", "precision", "window", "channels"])
     ap.add_argument("--steps", type=int, default=None)
+    ap.add_argument("--checkpoint", type=int, default=3)
+    ap.add_argument("--fp64", action="store_true")
     a = ap.parse_args()
     if a.which == "adjoint":
         r = adjoint(steps=a.steps or 200)
-    else:
+    elif a.which == "precision":
         r = precision(steps=a.steps or 2000)
+    elif a.which == "window":
+        r = window(steps=a.steps or 6, K=a.checkpoint, fp64=a.fp64)
+    else:
+        r = channels(steps=a.steps or 6)
     print(json.dumps(r))
 
 
