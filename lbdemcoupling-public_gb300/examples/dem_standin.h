@@ -79,12 +79,25 @@ private:
     std::vector<double*> pf, pt;
 };
 
+// fix multisphere: which body (or -1) each tag belongs to.
+class FixMultisphere : public Fix {
+public:
+    std::vector<int> body_of_tag;   // indexed by tag
+    int belongs_to(int tag) const {
+        return tag >= 0 && tag < (int)body_of_tag.size() ? body_of_tag[tag] : -1;
+    }
+};
+
 class Modify {
 public:
     FixLbCouplingOnetoone* coupling = nullptr;
+    FixMultisphere* multisphere = nullptr;
     Fix* find_fix_style(const char* style, int) {
-        return std::strcmp(style, "couple/lb/onetoone") == 0 ? coupling : nullptr;
+        if (std::strcmp(style, "couple/lb/onetoone") == 0) return coupling;
+        if (std::strcmp(style, "multisphere") == 0) return multisphere;
+        return nullptr;
     }
+    int n_fixes_style(const char* style) { return find_fix_style(style, 0) ? 1 : 0; }
 };
 
 class LAMMPS {

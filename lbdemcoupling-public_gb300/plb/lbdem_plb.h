@@ -79,6 +79,41 @@ public:
     }
     void collideAndStream() { check(lbdem_collide_and_stream(h_)); }
 
+    // initializeAtEquilibrium(lattice, box, PressureGradient<T>(pHi, pLo, n, dimension))
+    // and (..., PoiseuilleProfileAndPressureGradient<T>(pHi, pLo, uMax, nx, ny, nz, dimension))
+    // over the whole lattice (src/periodicPressureFunctionals3D.hh:238-298).
+    void initializePressureGradient(double pHi, double pLo, int32_t n, int32_t dimension) {
+        int32_t nn[3] = {n, n, n};
+        check(lbdem_init_profile(h_, LBDEM_PROFILE_PRESSURE_GRADIENT, pHi, pLo, 0.0, nn, dimension));
+    }
+    void initializePoiseuille(double pHi, double pLo, double uMax, int32_t nx, int32_t ny, int32_t nz,
+                              int32_t dimension) {
+        const int32_t nn[3] = {nx, ny, nz};
+        check(lbdem_init_profile(h_, LBDEM_PROFILE_POISEUILLE, pHi, pLo, uMax, nn, dimension));
+    }
+
+    // The pressure-driven periodic channel of examples/showcaseRectChannel (:253-273)
+    // done inside every collideAndStream: inlet and outlet are Box3D-like (x0..z1).
+    template <class Box>
+    void setPressureDrop(Box const& inlet, Box const& outlet, double rhoIn, double rhoOut, int32_t dimension,
+                         int32_t inDirection = 1, int32_t outDirection = -1) {
+        lbdem_pressure_drop d;
+        d.dimension = dimension;
+        box6(inlet, d.inlet);
+        box6(outlet, d.outlet);
+        d.in_direction = inDirection;
+        d.out_direction = outDirection;
+        d.rho_in = rhoIn;
+        d.rho_out = rhoOut;
+        check(lbdem_set_pressure_drop(h_, &d));
+    }
+
+    template <class Box>
+    static void box6(Box const& b, int32_t out[6]) {
+        out[0] = (int32_t)b.x0; out[1] = (int32_t)b.x1; out[2] = (int32_t)b.y0;
+        out[3] = (int32_t)b.y1; out[4] = (int32_t)b.z0; out[5] = (int32_t)b.z1;
+    }
+
     void check(lbdem_status s) const {
         if (s != LBDEM_OK)
             throw std::runtime_error(std::string(lbdem_status_string(s)) + ": " + lbdem_last_error(h_));
@@ -93,20 +128,35 @@ private:
     int32_t nx_ = 0, ny_ = 0, nz_ = 0;
 };
 
-// setSpheresOnLattice, src/ibDataExchangeWrappers3D.hh:33-146.
+// setSpheresOnLattice, src/ibDataExchangeWrappers3D.hh:33-146.  With
+// LBDEM_USE_MULTISPHERE defined (LIGGGHTS with fix multisphere, :52-115), a sphere
+// that belongs to a multisphere body enters with its own velocity and no angular
+// velocity (its surface velocity is then the translation of its own centre); the
+// including code provides LAMMPS_NS::FixMultisphere with belongs_to(tag).
 template <class Wrapper, class Units>
 void setSpheresOnLattice(GpuLattice3D& lattice, Wrapper& wrapper, Units const& units,
                          std::vector<long>& excludeType, bool initVelFlag) {
     auto* atom = wrapper.lmp->atom;
     const long nPart = atom->nlocal + atom->nghost;
+#ifdef LBDEM_USE_MULTISPHERE
+    LAMMPS_NS::FixMultisphere* fixMultisphere = nullptr;
+    if (wrapper.lmp->modify->n_fixes_style("multisphere"))
+        fixMultisphere =
+            static_cast<LAMMPS_NS::FixMultisphere*>(wrapper.lmp->modify->find_fix_style("multisphere", 0));
+#endif
     lattice.x.clear(); lattice.v.clear(); lattice.w.clear(); lattice.r.clear(); lattice.tag.clear();
     for (long iS = 0; iS < nPart; ++iS) {
         const long type = (long)atom->type[iS];
         if (std::find(excludeType.begin(), excludeType.end(), type) != excludeType.end()) continue;
+#ifdef LBDEM_USE_MULTISPHERE
+        const bool member = fixMultisphere && fixMultisphere->belongs_to(atom->tag[iS]) > -1;
+#else
+        const bool member = false;
+#endif
         for (int i = 0; i < 3; ++i) {
             lattice.x.push_back(units.getLbPosition(atom->x[iS][i]));
             lattice.v.push_back(units.getLbVel(atom->v[iS][i]));
-            lattice.w.push_back(units.getLbFreq(atom->omega[iS][i]));
+            lattice.w.push_back(member ? 0.0 : units.getLbFreq(atom->omega[iS][i]));
         }
         lattice.r.push_back(units.getLbLength(atom->radius[iS]));
         lattice.tag.push_back((int32_t)atom->tag[iS]);
@@ -120,6 +170,26 @@ template <class Wrapper, class Units>
 void setSpheresOnLattice(GpuLattice3D& lattice, Wrapper& wrapper, Units const& units, bool initVelFlag) {
     std::vector<long> none;
     setSpheresOnLattice(lattice, wrapper, units, none, initVelFlag);
+}
+
+// Palabos computeAverageDensity(lattice, box): 1 + mean rhoBar over the box.
+template <class Box>
+double computeAverageDensity(GpuLattice3D& lattice, Box const& box) {
+    int32_t b[6];
+    GpuLattice3D::box6(box, b);
+    double rho = 0;
+    lattice.check(lbdem_average_density(lattice.handle(), b, &rho));
+    return rho;
+}
+
+// applyProcessingFunctional(new ZhangPeriodicPressureFunctional3D<T,D>(rhoTarget, rhoAvg,
+// dimension, direction), box, lattice), src/periodicPressureFunctionals3D.hh:121-159.
+template <class Box>
+void applyZhangPeriodicPressure(GpuLattice3D& lattice, Box const& box, double rhoTarget, double rhoAvg,
+                                int32_t dimension, int32_t direction) {
+    int32_t b[6];
+    GpuLattice3D::box6(box, b);
+    lattice.check(lbdem_zhang_rescale(lattice.handle(), b, dimension, direction, rhoTarget, rhoAvg));
 }
 
 // getForcesFromLattice, src/ibDataExchangeWrappers3D.hh:160-246.  FixType is the

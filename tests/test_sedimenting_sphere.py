@@ -1,6 +1,6 @@
-"""The sedimenting-sphere case driven through the C++ host shim (plb/lbdem_plb.h)
-and the C ABI, with the LIGGGHTS stand-in integrator of
-examples/dem_standin.h.
+"""The C++ host shim (plb/lbdem_plb.h) driving the C ABI, with the LIGGGHTS
+stand-in of examples/dem_standin.h: the sedimenting-sphere case, and the
+multisphere branch of setSpheresOnLattice (examples/multisphere_check.cpp).
 
 * CPU: the driver compiles and links against the library; without a GPU it
   exits with status 77.
@@ -23,21 +23,22 @@ PKG = ROOT / "lbdemcoupling-public_gb300"
 EXE = PKG / "_build" / "sedimenting_sphere"
 
 
-def build_example():
+def build_example(name="sedimenting_sphere"):
     import build as pkg_build
     lib = pkg_build.build()
     cxx = shutil.which("g++") or shutil.which("c++")
     if not cxx:
         pytest.skip("no C++ compiler")
-    src = PKG / "examples" / "sedimenting_sphere.cpp"
+    exe = PKG / "_build" / name
+    src = PKG / "examples" / f"{name}.cpp"
     deps = [src, PKG / "examples" / "dem_standin.h", PKG / "plb" / "lbdem_plb.h", PKG / "plb" / "physunits_gpu.h",
             ROOT / "include" / "lbdem_gpu.h", lib]
-    if not EXE.exists() or EXE.stat().st_mtime < max(p.stat().st_mtime for p in deps):
+    if not exe.exists() or exe.stat().st_mtime < max(p.stat().st_mtime for p in deps):
         cmd = [cxx, "-O2", "-std=c++17", "-Wall", f"-I{ROOT / 'include'}", f"-I{PKG / 'plb'}",
                f"-I{PKG / 'examples'}", str(src), f"-L{lib.parent}", "-llbdem_gb300",
-               f"-Wl,-rpath,{lib.parent}", "-o", str(EXE)]
+               f"-Wl,-rpath,{lib.parent}", "-o", str(exe)]
         subprocess.run(cmd, check=True, capture_output=True, text=True)
-    return EXE
+    return exe
 
 
 def run_example(steps, prec, trace, every):
@@ -53,6 +54,46 @@ def test_example_builds_and_needs_a_gpu(lbdem_lib, tmp_path):
         pytest.skip("a GPU is present")
     r = run_example(2, "fp64", tmp_path / "c.txt", 1)
     assert r.returncode == 77, r.stderr
+
+
+def test_multisphere_check_builds_and_needs_a_gpu(lbdem_lib):
+    torch = pytest.importorskip("torch")
+    exe = build_example("multisphere_check")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    assert subprocess.run([str(exe)], capture_output=True, text=True).returncode == 77
+
+
+@pytest.mark.gpu
+def test_multisphere_members_use_translation_only(gpu):
+    exe = build_example("multisphere_check")
+    r = subprocess.run([str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stdout + r.stderr
+
+
+def test_channel_example_builds_and_needs_a_gpu(lbdem_lib):
+    torch = pytest.importorskip("torch")
+    exe = build_example("channel")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    assert subprocess.run([str(exe), "3"], capture_output=True, text=True).returncode == 77
+
+
+@pytest.mark.gpu
+def test_channel_example_fused_equals_explicit(gpu):
+    """The reference's per-step computeAverageDensity + Zhang functional calls and the
+    fused pressure drop give the same channel (box sums differ only in summation order)."""
+    import json
+    exe = build_example("channel")
+    out = {}
+    for mode in ("explicit", "fused"):
+        r = subprocess.run([str(exe), "300", mode], capture_output=True, text=True)
+        assert r.returncode == 0, r.stderr
+        out[mode] = json.loads(r.stdout)
+    assert out["fused"]["mean_ux"] > 1e-4
+    assert out["fused"]["fx"] > 0                       # drag on the held sphere points downstream
+    for k in ("mean_ux", "fx"):
+        assert abs(out["fused"][k] - out["explicit"][k]) <= 1e-10 * abs(out["explicit"][k])
 
 
 def oracle_trace(oracle, steps):
