@@ -335,6 +335,20 @@ def run_batched(steps: int, warmup: int, single_steps: int, device: int):
     }
 
 
+def run_adjoint():
+    """A short adjoint window of the 128^3 adjoint workload in both forms: the cost of
+    the backward pass against the forward pass (reports.py adjoint has the full
+    200-step window with its accuracy checks)."""
+    import reports
+    out = {"workload": "periodic 128^3, 64 spheres r = 6, body force 1e-6, 40 steps, checkpoint every 10, "
+                       "loss = sum of x-forces of every step"}
+    for name, fp64 in (("fp32", False), ("fp64", True)):
+        r = reports.window(steps=40, K=10, fp64=fp64)
+        out[name] = {"forward_ms": r["forward_ms"], "backward_ms": r["backward_ms"],
+                     "backward_over_forward": r["backward_ms"] / r["forward_ms"], "loss": r["loss"]}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -347,6 +361,7 @@ def main():
     ap.add_argument("--no-e2e", action="store_true", help="skip the host-buffer C-ABI leg (profiling runs)")
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-channels leg")
     ap.add_argument("--batched-steps", type=int, default=60)
+    ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-window leg")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
@@ -441,6 +456,9 @@ def main():
     batched = None
     if not args.no_batched and world == 1:
         batched = run_batched(args.batched_steps, args.warmup, 8, device)
+    adjoint = None
+    if not args.no_adjoint and world == 1:
+        adjoint = run_adjoint()
 
     cpu = None
     if not args.no_cpu_baseline:
@@ -468,6 +486,7 @@ def main():
                          "k2_voxelize_ms": r64["k2_ms"]}},
         "force_rel_err_fp32_vs_fp64": ferr,
         "batched": batched,
+        "adjoint": adjoint,
         "e2e": None if args.no_e2e else {"value": world * N * args.steps / e2e_s / 1e6, "unit": "MLUPS",
                                          "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "cpu_baseline": cpu,

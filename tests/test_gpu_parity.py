@@ -28,6 +28,9 @@ CASES = {
     # rows not 16-byte aligned (nz % 4 != 0): z walls, and rows of several segments
     "odd_z_walls": ((12, 10, 37), (1, 1, 0), 1 / 0.6, 4, 2.0, 3.5, True, (0.0, 0.0, 0.0)),
     "odd_long_z": ((5, 6, 133), (0, 1, 1), 1 / 0.55, 6, 1.5, 2.4, True, (2e-6, 0.0, 0.0)),
+    # one-cell-thick lattices: rows of one cell; a single periodic x plane with z walls
+    "flat_z": ((17, 13, 1), (1, 1, 1), 1 / 0.6, 3, 1.5, 3.0, True, (0.0, 0.0, 0.0)),
+    "flat_x": ((1, 12, 20), (1, 1, 0), 1 / 0.6, 2, 1.2, 2.5, True, (0.0, 1e-6, 0.0)),
 }
 
 
