@@ -179,6 +179,19 @@ lbdem_status lbdem_device_bytes(lbdem_handle* h, size_t* bytes);
  * library; memset/memcpy not counted). */
 lbdem_status lbdem_get_launch_count(lbdem_handle* h, int64_t* count);
 
+/* ---- Checkpoint / resume ----------------------------------------------------
+ * The per-cell coupling state IBcompositeDynamics::serialize writes
+ * (src/ibCompositeDynamics3D.hh:77-107: solid fraction and owner as the voxel
+ * word, particle surface velocity) together with the populations and the step
+ * count, as one binary file: a header (magic "LBDEMCK1", format version,
+ * nx, ny, nz, periodicity, precision, omega, body force, step), the populations
+ * [19][N] in natural order, the voxel words [N] and the surface velocities
+ * [3][N].  Loading needs a handle of the same extent and precision; the run
+ * then continues exactly as the saved one would have (call lbdem_set_particles
+ * before the next step, as after any step).  Both synchronize. */
+lbdem_status lbdem_save_state(lbdem_handle* h, const char* path);
+lbdem_status lbdem_load_state(lbdem_handle* h, const char* path);
+
 /* ---- Periodic pressure drop and initial profiles ---------------------------
  * Boxes are Palabos Box3D: {x0, x1, y0, y1, z0, z1}, inclusive. */
 

@@ -964,3 +964,91 @@ lbdem_status lbdem_adjoint_timing(lbdem_handle* h, float* forward_ms, float* bac
 }
 
 }  // extern "C"
+
+namespace {
+
+struct CheckpointHeader {
+    char magic[8];           // "LBDEMCK1"
+    int32_t version;         // 1
+    int32_t nx, ny, nz;
+    int32_t periodic[3];
+    int32_t precision;
+    double omega;
+    double body_force[3];
+    int64_t step;
+};
+
+struct FileCloser {
+    std::FILE* f = nullptr;
+    ~FileCloser() {
+        if (f) std::fclose(f);
+    }
+};
+
+}  // namespace
+
+extern "C" {
+
+lbdem_status lbdem_save_state(lbdem_handle* h, const char* path) {
+    if (!h || !path) return fail(h, LBDEM_ERR_INVALID_ARG, "save_state: null argument");
+    const size_t N = h->g.N;
+    std::vector<unsigned char> pops((size_t)Q * N * h->esz);
+    lbdem_status st = lbdem_get_populations(h, pops.data());
+    if (st != LBDEM_OK) return st;
+    std::vector<uint32_t> vox(N);
+    std::vector<unsigned char> up(3 * N * h->esz);
+    {
+        DeviceGuard dg(h->device);
+        CK(h, cudaMemcpyAsync(vox.data(), h->vox, N * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaMemcpyAsync(up.data(), h->up, 3 * N * h->esz, cudaMemcpyDeviceToHost, h->stream));
+        CK(h, cudaStreamSynchronize(h->stream));
+    }
+    CheckpointHeader hd{};
+    std::memcpy(hd.magic, "LBDEMCK1", 8);
+    hd.version = 1;
+    hd.nx = h->g.nx; hd.ny = h->g.ny; hd.nz = h->g.nz;
+    for (int d = 0; d < 3; ++d) { hd.periodic[d] = h->g.per[d]; hd.body_force[d] = h->cfg.body_force[d]; }
+    hd.precision = h->prec;
+    hd.omega = h->cfg.omega;
+    hd.step = h->step;
+    FileCloser fc;
+    fc.f = std::fopen(path, "wb");
+    if (!fc.f) return fail(h, LBDEM_ERR_INVALID_ARG, std::string("save_state: cannot open ") + path);
+    bool ok = std::fwrite(&hd, sizeof(hd), 1, fc.f) == 1 && std::fwrite(pops.data(), 1, pops.size(), fc.f) == pops.size() &&
+              std::fwrite(vox.data(), sizeof(uint32_t), N, fc.f) == N && std::fwrite(up.data(), 1, up.size(), fc.f) == up.size();
+    ok = (std::fclose(fc.f) == 0) && ok;
+    fc.f = nullptr;
+    if (!ok) return fail(h, LBDEM_ERR_INVALID_ARG, std::string("save_state: write failed: ") + path);
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_load_state(lbdem_handle* h, const char* path) {
+    if (!h || !path) return fail(h, LBDEM_ERR_INVALID_ARG, "load_state: null argument");
+    FileCloser fc;
+    fc.f = std::fopen(path, "rb");
+    if (!fc.f) return fail(h, LBDEM_ERR_INVALID_ARG, std::string("load_state: cannot open ") + path);
+    CheckpointHeader hd{};
+    if (std::fread(&hd, sizeof(hd), 1, fc.f) != 1 || std::memcmp(hd.magic, "LBDEMCK1", 8) != 0 || hd.version != 1)
+        return fail(h, LBDEM_ERR_INVALID_ARG, "load_state: not a checkpoint of this library");
+    if (hd.nx != h->g.nx || hd.ny != h->g.ny || hd.nz != h->g.nz || hd.precision != h->prec)
+        return fail(h, LBDEM_ERR_INVALID_ARG, "load_state: lattice extent or precision differs");
+    const size_t N = h->g.N;
+    std::vector<unsigned char> pops((size_t)Q * N * h->esz);
+    std::vector<uint32_t> vox(N);
+    std::vector<unsigned char> up(3 * N * h->esz);
+    if (std::fread(pops.data(), 1, pops.size(), fc.f) != pops.size() ||
+        std::fread(vox.data(), sizeof(uint32_t), N, fc.f) != N || std::fread(up.data(), 1, up.size(), fc.f) != up.size())
+        return fail(h, LBDEM_ERR_INVALID_ARG, "load_state: file truncated");
+    // the step count first: it fixes the in-place layout the populations are scattered into
+    h->step = hd.step;
+    lbdem_status st = lbdem_set_populations(h, pops.data());
+    if (st != LBDEM_OK) return st;
+    DeviceGuard dg(h->device);
+    CK(h, cudaMemcpyAsync(h->vox, vox.data(), N * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaMemcpyAsync(h->up, up.data(), 3 * N * h->esz, cudaMemcpyHostToDevice, h->stream));
+    CK(h, cudaStreamSynchronize(h->stream));
+    h->pavg_valid = false;
+    return LBDEM_OK;
+}
+
+}  // extern "C"

@@ -106,6 +106,8 @@ SIGNATURES = {
     "lbdem_zhang_rescale": (C.c_int, [_P, C.POINTER(_I), _I, _I, C.c_double, C.c_double]),
     "lbdem_set_pressure_drop": (C.c_int, [_P, C.POINTER(PressureDrop)]),
     "lbdem_init_profile": (C.c_int, [_P, _I, C.c_double, C.c_double, C.c_double, C.POINTER(_I), _I]),
+    "lbdem_save_state": (C.c_int, [_P, C.c_char_p]),
+    "lbdem_load_state": (C.c_int, [_P, C.c_char_p]),
     "lbdem_adjoint_window": (C.c_int, [_P, _I, _I, _I, _D, _D, _D, _D, _D, _D, _P]),
     "lbdem_adjoint_timing": (C.c_int, [_P, C.POINTER(C.c_float), C.POINTER(C.c_float)]),
     "lbdem_batch_config_default": (None, [C.POINTER(BatchConfig)]),
@@ -339,6 +341,20 @@ class Lattice:
     def set_stream(self, stream_ptr: int | None):
         self._check(self.lib.lbdem_set_stream(self.h, _P(stream_ptr) if stream_ptr else None))
 
+    # -- checkpoint / resume ------------------------------------------------
+    def save_state(self, path):
+        self._check(self.lib.lbdem_save_state(self.h, os.fsencode(path)))
+
+    def load_state(self, path):
+        self._check(self.lib.lbdem_load_state(self.h, os.fsencode(path)))
+
+    def write_vtk(self, path, fields=("density", "velocity", "solid_fraction"), spacing=1.0, origin=(0.0, 0.0, 0.0)):
+        """The lattice's fields as a VTK ImageData file (the fields of the reference's
+        writeVTK, examples/sedimentingSphere/sedimentingSphere.cpp:41-69)."""
+        which = {"density": FIELD_DENSITY, "velocity": FIELD_VELOCITY, "solid_fraction": FIELD_SOLID_FRACTION,
+                 "particle_id": FIELD_PARTICLE_ID, "particle_velocity": FIELD_PARTICLE_VELOCITY}
+        write_vtk(path, {name: self.get_field(which[name]) for name in fields}, spacing, origin)
+
     # -- adjoint --------------------------------------------------------------
     def adjoint_window(self, rec, weights, checkpoint_every, want_f0=False):
         """lbdem_adjoint_window.  rec: [nsteps][n][12] particle tables (positions fixed),
@@ -397,6 +413,47 @@ class Lattice:
         nn = (_I * 3)(*[int(v) for v in n])
         self._check(self.lib.lbdem_init_profile(self.h, int(kind), float(rho_hi), float(rho_lo), float(u_max), nn,
                                                 int(dimension)))
+
+
+def write_vtk(path, fields: dict, spacing=1.0, origin=(0.0, 0.0, 0.0)):
+    """VTK XML ImageData (.vti) with raw appended little-endian data.  fields maps a
+    name to an [nx][ny][nz] scalar or a [3][nx][ny][nz] vector array (this library's
+    layouts, z fastest); VTK orders points x fastest, so arrays are transposed."""
+    arrays = []
+    shape = None
+    for name, a in fields.items():
+        a = np.asarray(a)
+        if a.ndim == 4:
+            comps, grid = 3, a.shape[1:]
+            data = np.ascontiguousarray(np.stack([a[k].transpose(2, 1, 0) for k in range(3)], axis=-1))
+        else:
+            comps, grid = 1, a.shape
+            data = np.ascontiguousarray(a.transpose(2, 1, 0))
+        if shape is None:
+            shape = grid
+        elif grid != shape:
+            raise ValueError("write_vtk: fields of different extent")
+        dt = {np.dtype(np.float64): "Float64", np.dtype(np.float32): "Float32", np.dtype(np.int32): "Int32",
+              np.dtype(np.uint8): "UInt8"}[data.dtype]
+        arrays.append((name, comps, dt, data.astype(data.dtype.newbyteorder("<"), copy=False).tobytes()))
+    nx, ny, nz = shape
+    ext = f"0 {nx - 1} 0 {ny - 1} 0 {nz - 1}"
+    head, offset = [], 0
+    for name, comps, dt, raw in arrays:
+        head.append(f'<DataArray type="{dt}" Name="{name}" NumberOfComponents="{comps}" format="appended" '
+                    f'offset="{offset}"/>')
+        offset += 8 + len(raw)
+    xml = ('<?xml version="1.0"?>\n<VTKFile type="ImageData" version="1.0" byte_order="LittleEndian" '
+           'header_type="UInt64">\n'
+           f'<ImageData WholeExtent="{ext}" Origin="{origin[0]} {origin[1]} {origin[2]}" '
+           f'Spacing="{spacing} {spacing} {spacing}">\n<Piece Extent="{ext}">\n<PointData>\n'
+           + "\n".join(head) + '\n</PointData>\n</Piece>\n</ImageData>\n<AppendedData encoding="raw">\n_')
+    with open(path, "wb") as fh:
+        fh.write(xml.encode())
+        for _, _, _, raw in arrays:
+            fh.write(np.uint64(len(raw)).astype("<u8").tobytes())
+            fh.write(raw)
+        fh.write(b"\n</AppendedData>\n</VTKFile>\n")
 
 
 def pack_records(x, v, w, r, tag) -> np.ndarray:
