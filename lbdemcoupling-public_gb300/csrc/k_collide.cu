@@ -26,6 +26,8 @@
 // domains in one launch (batch mode).
 #include "lbdem_internal.h"
 
+#include <cstddef>
+
 namespace lbdem {
 namespace {
 
@@ -181,18 +183,17 @@ __device__ __forceinline__ void psm(T (&f)[Q], const Mom<T>& m, T up0, T up1, T 
 // pre-collision moments (the reference recomputes them from the post-collision
 // populations, :146-148; the two differ by rounding only); with the Guo force
 // the post-collision moments are recomputed.
-template <typename T, bool FORCE, typename Pre>
-__device__ __forceinline__ void collide_cell(const CollideArgs<T>& a, T (&f)[Q], uint32_t w, size_t c, const Pre& pre,
-                                             T& Fx, T& Fy, T& Fz) {
+// up(d) returns component d of the cell's particle surface velocity.
+template <typename T, bool FORCE, typename Pre, typename Up>
+__device__ __forceinline__ void collide_cell(const CollideArgs<T>& a, T (&f)[Q], uint32_t w, const Pre& pre,
+                                             const Up& up, T& Fx, T& Fy, T& Fz) {
     const int n = min((int)(w & VOX_NMASK), 125);
     Fx = T(0); Fy = T(0); Fz = T(0);
     Mom<T> m = cell_moments(f);
     if (n < 125) bgk<T, FORCE>(f, m, a.omega, a.g3[0], a.g3[1], a.g3[2]);
     if (n > 0) {
         if (FORCE && n < 125) m = cell_moments(f);
-        const size_t N = a.g.N;
-        const T up0 = __ldg(a.up + c), up1 = __ldg(a.up + N + c), up2 = __ldg(a.up + 2 * N + c);
-        psm<T>(f, m, up0, up1, up2, __ldg(a.btab + n), pre, Fx, Fy, Fz);
+        psm<T>(f, m, up(0), up(1), up(2), __ldg(a.btab + n), pre, Fx, Fy, Fz);
     }
 }
 
@@ -303,17 +304,29 @@ constexpr int WARPS = COLLIDE_BLOCK / 32;    // warps per CTA
 constexpr int SEGW = 64;                    // cells per warp segment (2 per lane)
 constexpr int WAIT_LIMIT = 1 << 22;         // bounded mbarrier wait (iterations of try_wait)
 
-template <typename T>
-struct WarpStage {
+// 16-byte aligned, so that every warp's stage (at warp * sizeof) keeps the bulk
+// copies' shared-memory destinations on 16-byte boundaries.
+template <typename T, bool STAGE_UP = true>
+struct alignas(16) WarpStage {
     static constexpr int V = 16 / (int)sizeof(T);   // elements per 16 bytes
+    static constexpr int UW = STAGE_UP ? SEGW + V : 1;
     static constexpr int W = SEGW + 2 * V;          // row: V halo | (lead) SEGW core | V halo
     T f[2][Q][W];
     uint32_t vox[2][SEGW + 4];
+    T up[2][3][UW];        // particle surface velocity rows of the segment (when staged)
     long long row[2][9];   // element offset of row (x + dx, y + dy) at [3 (dx + 1) + dy + 1]; -1 beyond a wall
     int geo[2][8];         // x, y, z0, len, domain of the segment held in buffer b
-    unsigned long long lead[2];   // unaligned rows: lead elements of row i at bits 2i, voxel row at bits 38
+    unsigned long long lead[2];   // unaligned rows: lead elements of row i at bits 2i, voxel row at bits 38,
+                                  // surface-velocity row d at bits 40 + 2d
     unsigned long long bar[2];
 };
+
+static_assert(sizeof(WarpStage<float, true>) % 16 == 0 && sizeof(WarpStage<float, false>) % 16 == 0 &&
+                  sizeof(WarpStage<double, true>) % 16 == 0 && sizeof(WarpStage<double, false>) % 16 == 0,
+              "per-warp stages must keep 16-byte alignment");
+static_assert(offsetof(WarpStage<float>, vox) % 16 == 0 && offsetof(WarpStage<float>, up) % 16 == 0 &&
+                  offsetof(WarpStage<double>, vox) % 16 == 0 && offsetof(WarpStage<double>, up) % 16 == 0,
+              "bulk-copy destinations on 16-byte boundaries");
 
 __device__ __forceinline__ constexpr int row_slot(int dx, int dy) { return 3 * (dx + 1) + dy + 1; }
 
@@ -389,7 +402,8 @@ __device__ __forceinline__ long long row_off(const Geom& g, const SegGeo& s, int
 //                 slot opp i, or own row slot i when that row is beyond a wall);
 //   lanes 19..28: odd phase, aligned rows: the 16-byte chunk holding the halo
 //                 element of the (lane-19)-th c_z != 0 direction (none beyond a z wall);
-//   lane 29:      voxel words of the segment.
+//   lane 29:      voxel words of the segment;
+//   lanes 29-31:  (second copy) the segment's particle surface-velocity rows.
 // MIS (rows not 16-byte aligned, nz % 4 != 0): each row copy starts at the
 // 16-byte boundary below the row and is rounded up to whole chunks (the
 // allocations carry 64 bytes of tail padding); the lead of every row is
@@ -398,8 +412,8 @@ __device__ __forceinline__ long long row_off(const Geom& g, const SegGeo& s, int
 // landed: the cell that reads and writes such a slot in this step lies in
 // this segment, so no other warp touches it meanwhile.
 // Lanes 0..9 also publish the segment geometry for the compute pass.
-template <typename T, bool ODD, bool MIS>
-__device__ __forceinline__ T issue_segment(const CollideArgs<T>& a, WarpStage<T>& st, int b, long long seg,
+template <typename T, bool ODD, bool MIS, bool STAGE_UP>
+__device__ __forceinline__ T issue_segment(const CollideArgs<T>& a, WarpStage<T, STAGE_UP>& st, int b, long long seg,
                                            int nzseg, int dom) {
     constexpr int V = WarpStage<T>::V;
     const int lane = threadIdx.x & 31;
@@ -464,10 +478,27 @@ __device__ __forceinline__ T issue_segment(const CollideArgs<T>& a, WarpStage<T>
         src = reinterpret_cast<const T*>(vs);
         dst = &st.vox[b][0];
     }
+    // lanes 29, 30, 31: the surface-velocity rows (components 2, 0, 1) as a second copy
+    const T* src2 = nullptr;
+    void* dst2 = nullptr;
+    uint32_t bytes2 = 0, lead2 = 0;
+    const int ud = lane == Q + 10 ? 2 : lane - (Q + 11);
+    if (STAGE_UP && lane >= Q + 10) {
+        src2 = a.up + (size_t)ud * N + own + s.z0;
+        dst2 = &st.up[b][ud][0];
+        if (MIS) {
+            lead2 = (uint32_t)(((uintptr_t)src2 & 15u) / sizeof(T));
+            src2 -= lead2;
+            bytes2 = (uint32_t)(((lead2 + (uint32_t)s.len + V - 1) / V) * 16u);
+        } else {
+            bytes2 = (uint32_t)(s.len * sizeof(T));
+        }
+    }
     if (MIS) {
         const uint32_t lo = __reduce_or_sync(FULL, lane < 16 ? lead << (2 * lane) : 0u);
         const uint32_t hi = __reduce_or_sync(
-            FULL, (lane >= 16 && lane < Q) ? lead << (2 * (lane - 16)) : (lane == Q + 10 ? lead << 6 : 0u));
+            FULL, ((lane >= 16 && lane < Q) ? lead << (2 * (lane - 16)) : (lane == Q + 10 ? lead << 6 : 0u)) |
+                      ((STAGE_UP && lane >= Q + 10) ? lead2 << (8 + 2 * ud) : 0u));
         if (lane == 0) st.lead[b] = (unsigned long long)lo | ((unsigned long long)hi << 32);
         if (ODD && lane < 10) {
             const int i = zdir(lane);
@@ -485,10 +516,11 @@ __device__ __forceinline__ T issue_segment(const CollideArgs<T>& a, WarpStage<T>
             }
         }
     }
-    const uint32_t total = __reduce_add_sync(FULL, bytes);
+    const uint32_t total = __reduce_add_sync(FULL, bytes + bytes2);
     if (lane == 0) mbar_arrive_expect_tx(&st.bar[b], total);
     __syncwarp();
     if (bytes) bulk_g2s(dst, src, bytes, &st.bar[b]);
+    if (bytes2) bulk_g2s(dst2, src2, bytes2, &st.bar[b]);
     return halo;
 }
 
@@ -501,10 +533,14 @@ __global__ void __launch_bounds__(COLLIDE_BLOCK, sizeof(T) == 4 ? 4 : 2)
 k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const CollideArgs<T>* __restrict__ dargs,
                  const int* __restrict__ seg0, int ndom) {
     constexpr int V = WarpStage<T>::V;
+    // surface-velocity rows staged with the populations for a single lattice; the
+    // many short rows of a batch read them directly (three more small copies per
+    // segment cost more there than the loads they replace)
+    constexpr bool STAGE_UP = !BATCH;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    WarpStage<T>& st = reinterpret_cast<WarpStage<T>*>(smem_raw)[warp];
+    WarpStage<T, STAGE_UP>& st = reinterpret_cast<WarpStage<T, STAGE_UP>*>(smem_raw)[warp];
     if (lane == 0) {
         mbar_init(&st.bar[0], 1);
         mbar_init(&st.bar[1], 1);
@@ -518,9 +554,10 @@ k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const Coll
         if (BATCH) {
             const int d = find_domain(seg0, ndom, (int)sg);
             const CollideArgs<T>& A = dargs[d];
-            return issue_segment<T, ODD, MIS>(A, st, buf, sg - __ldg(seg0 + d), (A.g.nz + SEGW - 1) / SEGW, d);
+            return issue_segment<T, ODD, MIS, STAGE_UP>(A, st, buf, sg - __ldg(seg0 + d), (A.g.nz + SEGW - 1) / SEGW,
+                                                        d);
         }
-        return issue_segment<T, ODD, MIS>(a1, st, buf, sg, nzseg1, 0);
+        return issue_segment<T, ODD, MIS, STAGE_UP>(a1, st, buf, sg, nzseg1, 0);
     };
     T hcur = issue(0, seg);
     uint32_t phase = 0;   // bit b: parity expected next on buffer b
@@ -594,7 +631,12 @@ k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const Coll
                 for (int i = 0; i < Q; ++i) f[i] = at(i);
                 const uint32_t w = st.vox[b][vlead + j];
                 T Fx, Fy, Fz;
-                collide_cell<T, FORCE>(a, f, w, c, [&](int i) { return at(i); }, Fx, Fy, Fz);
+                auto upv = [&](int d) -> T {
+                    if (!STAGE_UP) return __ldg(a.up + (size_t)d * N + c);
+                    const int m = MIS ? (int)((lead >> (40 + 2 * d)) & 3u) : 0;
+                    return st.up[b][d][m + j];
+                };
+                collide_cell<T, FORCE>(a, f, w, [&](int i) { return at(i); }, upv, Fx, Fy, Fz);
                 if (!ODD) {
 #pragma unroll
                     for (int i = 0; i < Q; ++i) F[(size_t)opp(i) * N + c] = f[i];
@@ -623,7 +665,7 @@ k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const Coll
 template <typename T, bool ODD, bool FORCE, bool PER, bool MIS, bool BATCH>
 cudaError_t launch_staged(const CollideArgs<T>& a, int nzseg, long long nseg, const CollideArgs<T>* dargs,
                           const int* seg0, int ndom, int blocks_per_sm, cudaStream_t s) {
-    constexpr size_t smem = WARPS * sizeof(WarpStage<T>);
+    constexpr size_t smem = WARPS * sizeof(WarpStage<T, !BATCH>);
     static int per_sm = 0, sms = 0;
     if (per_sm == 0) {
         int dev = 0;

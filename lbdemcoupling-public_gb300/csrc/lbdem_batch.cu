@@ -488,7 +488,7 @@ lbdem_status lbdem_batch_create(const lbdem_batch_config* cfg, int32_t ndomains,
     const size_t capn = (size_t)std::max(b->nslots, 1);
     TRY(dalloc(b, &b->f, b->f_elems * b->esz + ALLOC_TAIL));
     TRY(dalloc(b, &b->vox, b->vox_elems * sizeof(uint32_t) + ALLOC_TAIL));
-    TRY(dalloc(b, &b->up, b->up_elems * b->esz));
+    TRY(dalloc(b, &b->up, b->up_elems * b->esz + ALLOC_TAIL));
     TRY(dalloc(b, &b->btab, (size_t)126 * ndomains * b->esz));
     b->rec_off = round_up(sizeof(int) * (size_t)ndomains, 16);
     b->stage_bytes = b->rec_off + capn * REC_STRIDE * sizeof(double);

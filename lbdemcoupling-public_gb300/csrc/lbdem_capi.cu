@@ -332,7 +332,7 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     TRY(cudaEventCreateWithFlags(&h->ev_staged, cudaEventDisableTiming));
     TRY(dalloc(h, &h->f, (size_t)Q * N * h->esz + ALLOC_TAIL));
     TRY(dalloc(h, &h->vox, N * sizeof(uint32_t) + ALLOC_TAIL));
-    TRY(dalloc(h, &h->up, 3 * N * h->esz));
+    TRY(dalloc(h, &h->up, 3 * N * h->esz + ALLOC_TAIL));
     if (c.flags & LBDEM_FLAG_CELL_FORCE) TRY(dalloc(h, &h->cf, 3 * N * h->esz));
     TRY(dalloc(h, &h->btab, 126 * sizeof(double)));
     TRY(dalloc(h, &h->btabf, 126 * sizeof(float)));

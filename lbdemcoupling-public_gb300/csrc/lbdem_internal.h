@@ -125,8 +125,9 @@ __device__ __forceinline__ int find_domain(const int* __restrict__ off, int n, i
     return lo;
 }
 
-// Population and voxel-word allocations carry this many bytes past their end:
-// the staged collide kernel copies whole 16-byte chunks around unaligned rows.
+// Population, voxel-word and surface-velocity allocations carry this many bytes
+// past their end: the staged collide kernel copies whole 16-byte chunks around
+// unaligned rows.
 constexpr size_t ALLOC_TAIL = 64;
 
 // Launchers (return cudaGetLastError() of the launch).
