@@ -233,7 +233,7 @@ def cpu_oracle_mlups(host_tables, budget_s: float, max_cycles: int, threads: int
     return N * done / dt / 1e6, done, dt
 
 
-def run_batched(steps: int, warmup: int, single_steps: int, device: int):
+def run_batched(steps: int, warmup: int, single_steps: int, device: int, flow_axis: int = 2):
     """Batched pressure-driven channels (workloads.channels: 512 domains, FP32
     deviation form): aggregate MLUPS of the batch -- graph replay of one launch
     per stage over all domains -- through the host-buffer cycle call, of the
@@ -243,7 +243,7 @@ def run_batched(steps: int, warmup: int, single_steps: int, device: int):
 
     import lbdem
     import workloads as W
-    ch = W.channels()
+    ch = W.channels(flow_axis=flow_axis)
     doms = [d for d, _ in ch]
     cells = sum(int(np.prod(d["shape"])) for d in doms)
     nt = min(warmup + max(steps, single_steps), 16)
@@ -318,8 +318,9 @@ def run_batched(steps: int, warmup: int, single_steps: int, device: int):
     peak, _ = peaks()
     ach = BYTES_PER_CELL["fp32"] * cells / (k1_ms * 1e-3) / 1e9 if k1_ms > 0 else None
     return {
-        "workload": f"{len(doms)} pressure-driven channels, Lx U[64,160], Ly=Lz U[24,48], walls in y and z, "
-                    f"1-40 spheres r U[3,6] each, tau 0.6, fp32 deviation form",
+        "workload": f"{len(doms)} pressure-driven channels, length U[64,160] along the flow (stored along "
+                    f"{'xyz'[flow_axis]}), square cross-section U[24,48] between walls, 1-40 spheres r U[3,6] each, "
+                    f"tau 0.6, fp32 deviation form",
         "cells": cells, "particles_local": int(sum(p.n for _, p in ch)),
         "value": cells * steps / t_e2e / 1e6, "unit": "MLUPS",
         "note": "value: lbdem_batch_cycle with host buffers (upload of the particle table and download of the "

@@ -27,6 +27,7 @@
 #include "lbdem_internal.h"
 
 #include <cstddef>
+#include <type_traits>
 
 namespace lbdem {
 namespace {
@@ -197,6 +198,177 @@ __device__ __forceinline__ void collide_cell(const CollideArgs<T>& a, T (&f)[Q],
     }
 }
 
+// ---------------------------------------------------------------------------
+// FP32 form: two cells per thread in packed f32x2 arithmetic (sm_100 family
+// add/sub/mul/fma .f32x2), the cells z and z + 1 of one row.  The same update as
+// collide_cell, arranged per opposite pair around the direction k = i + 9 (every
+// c_k has a non-negative first non-zero component, so c_k . v needs no
+// negation), with two algebraically equal rewrites:
+//   * the solid correction is applied as f + B ((fPre - f) + X), which leaves a
+//     fluid cell (B = 0) exactly unchanged, so a pair mixing a fluid and a solid
+//     cell runs it for both without a select;
+//   * with the Guo force the solid correction's momentum is the BGK post-collision
+//     momentum j + rho g (exact in arithmetic) instead of a second moment sum.
+// Rounding differs from collide_cell at the float level; the FP64 form keeps
+// collide_cell and the reference's double sequence.
+struct F2 {
+    unsigned long long r;
+};
+__device__ __forceinline__ F2 pk(float a, float b) {
+    F2 v;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(v.r) : "f"(a), "f"(b));
+    return v;
+}
+__device__ __forceinline__ F2 bc(float a) { return pk(a, a); }
+__device__ __forceinline__ float2 upk(F2 v) {
+    float2 o;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(o.x), "=f"(o.y) : "l"(v.r));
+    return o;
+}
+__device__ __forceinline__ F2 operator+(F2 a, F2 b) {
+    F2 d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d.r) : "l"(a.r), "l"(b.r));
+    return d;
+}
+__device__ __forceinline__ F2 operator-(F2 a, F2 b) {
+    F2 d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d.r) : "l"(a.r), "l"(b.r));
+    return d;
+}
+__device__ __forceinline__ F2 operator*(F2 a, F2 b) {
+    F2 d;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d.r) : "l"(a.r), "l"(b.r));
+    return d;
+}
+// a * b + c, one rounding
+__device__ __forceinline__ F2 fma2(F2 a, F2 b, F2 c) {
+    F2 d;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d.r) : "l"(a.r), "l"(b.r), "l"(c.r));
+    return d;
+}
+
+// c_k . (a, b, c) for k >= 10 (first non-zero component of c_k is +1)
+template <int K>
+__device__ __forceinline__ F2 cdotk(F2 a, F2 b, F2 c) {
+    constexpr int X = cx(K), Y = cy(K), Z = cz(K);
+    static_assert(X > 0 || (X == 0 && (Y > 0 || (Y == 0 && Z > 0))), "direction with a negative lead");
+    if constexpr (X != 0) {
+        if constexpr (Y != 0) return Y > 0 ? a + b : a - b;
+        else if constexpr (Z != 0) return Z > 0 ? a + c : a - c;
+        else return a;
+    } else if constexpr (Y != 0) {
+        if constexpr (Z != 0) return Z > 0 ? b + c : b - c;
+        else return b;
+    } else {
+        return c;
+    }
+}
+// the same with uniform scalars
+template <int K>
+__device__ __forceinline__ float cdotk_s(float a, float b, float c) {
+    return (float)cx(K) * a + (float)cy(K) * b + (float)cz(K) * c;
+}
+
+struct Mom2 {
+    F2 rhoBar, jx, jy, jz, invRho;
+};
+
+__device__ __forceinline__ Mom2 moments2(const F2 (&f)[Q]) {
+    Mom2 m;
+    m.rhoBar = ((f[0] + (f[1] + f[10])) + ((f[2] + f[11]) + (f[3] + f[12]))) +
+               (((f[4] + f[13]) + (f[5] + f[14])) + ((f[6] + f[15]) + (f[7] + f[16]))) +
+               ((f[8] + f[17]) + (f[9] + f[18]));
+    m.jx = ((f[10] + f[13]) + (f[14] + f[15]) + f[16]) - ((f[1] + f[4]) + (f[5] + f[6]) + f[7]);
+    m.jy = ((f[11] + f[13]) + (f[17] + f[18]) + f[5]) - ((f[2] + f[4]) + (f[8] + f[9]) + f[14]);
+    m.jz = ((f[12] + f[15]) + (f[17] + f[7]) + f[9]) - ((f[3] + f[6]) + (f[8] + f[16]) + f[18]);
+    const float2 rb = upk(m.rhoBar);
+    m.invRho = pk(__frcp_rn(1.f + rb.x), __frcp_rn(1.f + rb.y));
+    return m;
+}
+
+template <bool FORCE>
+__device__ __forceinline__ void bgk2(F2 (&f)[Q], const Mom2& m, float omega, float gx, float gy, float gz) {
+    const F2 one = bc(1.f);
+    const F2 rho = one + m.rhoBar, invRho = m.invRho;
+    F2 jx = m.jx, jy = m.jy, jz = m.jz;
+    if (FORCE) {
+        const F2 h = bc(0.5f) * rho;
+        jx = fma2(h, bc(gx), jx); jy = fma2(h, bc(gy), jy); jz = fma2(h, bc(gz), jz);
+    }
+    const F2 jSqr = fma2(jz, jz, fma2(jy, jy, jx * jx));
+    const F2 base = fma2(bc(-1.5f) * invRho, jSqr, m.rhoBar);
+    const F2 om1 = bc(1.f - omega);
+    const F2 q45 = bc(4.5f) * invRho;
+    F2 ux{}, uy{}, uz{}, pre{}, ug{};
+    if (FORCE) {
+        ux = jx * invRho; uy = jy * invRho; uz = jz * invRho;
+        pre = bc(1.f - 0.5f * omega) * rho;
+        ug = fma2(uz, bc(gz), fma2(uy, bc(gy), ux * bc(gx)));
+    }
+    f[0] = fma2(om1, f[0], bc(omega * (float)wt(0)) * base);
+    if (FORCE) f[0] = f[0] - bc(3.f * (float)wt(0)) * (pre * ug);
+    auto pair = [&](auto kc) {
+        constexpr int k = decltype(kc)::value, i = k - 9;
+        const F2 cj = cdotk<k>(jx, jy, jz);          // c_k . j = -c_i . j
+        const F2 ow = bc(omega * (float)wt(k));
+        const F2 e = fma2(q45 * cj, cj, base);
+        const F2 s = bc(3.f) * cj;
+        f[i] = fma2(om1, f[i], ow * (e - s));
+        f[k] = fma2(om1, f[k], ow * (e + s));
+        if (FORCE) {
+            const F2 cu = cdotk<k>(ux, uy, uz);
+            const float cg = cdotk_s<k>(gx, gy, gz);
+            const F2 tp = bc((float)wt(k)) * pre;
+            const F2 X = fma2(bc(9.f * cg), cu, bc(-3.f) * ug);
+            f[i] = fma2(tp, X - bc(3.f * cg), f[i]);
+            f[k] = fma2(tp, X + bc(3.f * cg), f[k]);
+        }
+    };
+    pair(std::integral_constant<int, 10>{}); pair(std::integral_constant<int, 11>{});
+    pair(std::integral_constant<int, 12>{}); pair(std::integral_constant<int, 13>{});
+    pair(std::integral_constant<int, 14>{}); pair(std::integral_constant<int, 15>{});
+    pair(std::integral_constant<int, 16>{}); pair(std::integral_constant<int, 17>{});
+    pair(std::integral_constant<int, 18>{});
+}
+
+// Solid correction of both cells (a no-op for a cell with B = 0), with the
+// momentum exchange accumulated in (Fx, Fy, Fz); pre(i) returns the pair's fPre_i.
+template <typename Pre>
+__device__ __forceinline__ void psm2(F2 (&f)[Q], F2 rhoBar, F2 jx, F2 jy, F2 jz, F2 invRho, F2 up0, F2 up1, F2 up2,
+                                     F2 B, const Pre& pre, F2& Fx, F2& Fy, F2& Fz) {
+    const F2 rho = bc(1.f) + rhoBar;
+    const F2 ux = up0 * rho, uy = up1 * rho, uz = up2 * rho;
+    const F2 q45 = bc(4.5f) * invRho;
+    const F2 dB = (bc(-1.5f) * invRho) * (fma2(uz, uz, fma2(uy, uy, ux * ux)) - fma2(jz, jz, fma2(jy, jy, jx * jx)));
+    {
+        const F2 p0 = pre(0);
+        f[0] = fma2(B, (p0 - f[0]) - bc((float)wt(0)) * dB, f[0]);
+    }
+    const F2 B2 = B + B;
+    Fx = bc(0.f); Fy = bc(0.f); Fz = bc(0.f);
+    auto pair = [&](auto kc) {
+        constexpr int k = decltype(kc)::value, i = k - 9;
+        const F2 t = bc((float)wt(k));
+        const F2 cj = cdotk<k>(jx, jy, jz);
+        const F2 cu = cdotk<k>(ux, uy, uz);
+        const F2 A = t * fma2(q45, (cu - cj) * (cu + cj), dB);
+        const F2 Sk = bc(3.f * (float)wt(k)) * (cj + cu);
+        const F2 pi = pre(i), pkk = pre(k);
+        const F2 E = (pkk - pi) - Sk;
+        f[i] = fma2(B, (pi - f[i]) + (A + E), f[i]);
+        f[k] = fma2(B, (pkk - f[k]) + (A - E), f[k]);
+        const F2 d = B2 * E;                          // F += c_k (bb - bbOpp)
+        if constexpr (cx(k) > 0) Fx = Fx + d;
+        if constexpr (cy(k) > 0) Fy = Fy + d; else if constexpr (cy(k) < 0) Fy = Fy - d;
+        if constexpr (cz(k) > 0) Fz = Fz + d; else if constexpr (cz(k) < 0) Fz = Fz - d;
+    };
+    pair(std::integral_constant<int, 10>{}); pair(std::integral_constant<int, 11>{});
+    pair(std::integral_constant<int, 12>{}); pair(std::integral_constant<int, 13>{});
+    pair(std::integral_constant<int, 14>{}); pair(std::integral_constant<int, 15>{});
+    pair(std::integral_constant<int, 16>{}); pair(std::integral_constant<int, 17>{});
+    pair(std::integral_constant<int, 18>{});
+}
+
 // float -> double by bit manipulation (exact for normal numbers; subnormal
 // floats become signed zero).  Keeps the conversion off GB300's narrow FP64 pipe.
 __device__ __forceinline__ double widen(float x) {
@@ -290,6 +462,78 @@ __device__ __forceinline__ void reduce_forces(const CollideArgs<T>& a, int key, 
         atomicAdd(Fp + 0, widen(v[0])); atomicAdd(Fp + 1, widen(v[1])); atomicAdd(Fp + 2, widen(v[2]));
         atomicAdd(Tp + 0, widen(v[3])); atomicAdd(Tp + 1, widen(v[4])); atomicAdd(Tp + 2, widen(v[5]));
     }
+}
+
+// FP32 form: force and torque of the cells of one row segment, reduced per run
+// of equal owner tag with the owner looked up once per run.  Every cell of a
+// particle lies within its radius of the particle's nearest image, so along a
+// row the minimum-image arm of cell z is arm(zc) + (z - zc) e_z for any point
+// zc of the segment, and
+//   sum_cells arm x F = arm(zc) x sum F + sum (z - zc) e_z x F,
+// with e_z x F = (-F_y, F_x, 0).  Per cell the kernel accumulates
+// v = (F, -(z - zc) F_y, (z - zc) F_x); the lane that ends a run (the last
+// lane of a run of equal tags, or the first solid lane when one tag covers the
+// warp) maps the tag to the particle slot, takes the arm of its own cell zr,
+// arm(zc) = arm(zr) - (zr - zc) e_z, and adds F and arm(zc) x F + (v3, v4, 0).
+__device__ __forceinline__ void finish_run(const CollideArgs<float>& a, int tag, const float (&v)[5], int sx, int sy,
+                                           int zr, int zc) {
+    const int slot = tag <= a.max_tag ? __ldg(a.tag2slot + tag) : -1;
+    if (slot < 0 || slot >= a.nslot) {
+        atomicOr(a.err, 0x8u);   // LBDEM_DEVERR_UNMAPPED_TAG
+        return;
+    }
+    const float4* p = reinterpret_cast<const float4*>(a.xpf) + 2 * (size_t)slot;
+    const float4 h = __ldg(p), l = __ldg(p + 1);
+    float dx = ((float)sx - h.x) - h.w;
+    float dy = ((float)sy - h.y) - l.x;
+    float dz = ((float)zr - h.z) - l.y;
+    const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
+    const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
+    if (dx > (float)hx) dx -= (float)nx; else if (dx < (float)-hx) dx += (float)nx;
+    if (dy > (float)hy) dy -= (float)ny; else if (dy < (float)-hy) dy += (float)ny;
+    if (dz > (float)hz) dz -= (float)nz; else if (dz < (float)-hz) dz += (float)nz;
+    dz -= (float)(zr - zc);
+    double* Fp = a.ft + 3 * (size_t)slot;
+    double* Tp = a.ft + 3 * (size_t)a.nslot + 3 * (size_t)slot;
+    // few lanes get here: the hardware conversion is cheaper than widen()
+    atomicAdd(Fp + 0, (double)v[0]); atomicAdd(Fp + 1, (double)v[1]); atomicAdd(Fp + 2, (double)v[2]);
+    atomicAdd(Tp + 0, (double)((dy * v[2] - dz * v[1]) + v[3]));
+    atomicAdd(Tp + 1, (double)((dz * v[0] - dx * v[2]) + v[4]));
+    atomicAdd(Tp + 2, (double)(dx * v[1] - dy * v[0]));
+}
+
+// Warp reduction of v over runs of equal key (owner tag, -1: no solid cell);
+// zr is a cell of the lane's run.  Must be reached by all 32 lanes.
+__device__ __forceinline__ void reduce_runs(const CollideArgs<float>& a, int key, float (&v)[5], int zr, int sx,
+                                            int sy, int zc) {
+    const unsigned solid = __ballot_sync(FULL, key >= 0);
+    if (solid == 0u) return;
+    const int lane = threadIdx.x & 31;
+    const int lead = __ffs(solid) - 1;
+    const int first = __shfl_sync(FULL, key, lead);
+    if (__all_sync(FULL, key < 0 || key == first)) {
+#pragma unroll
+        for (int d = 16; d > 0; d >>= 1)
+#pragma unroll
+            for (int k = 0; k < 5; ++k) v[k] += __shfl_xor_sync(FULL, v[k], d);
+        if (lane == lead) finish_run(a, first, v, sx, sy, zr, zc);
+        return;
+    }
+    const int prevKey = __shfl_up_sync(FULL, key, 1);
+    const bool head = (lane == 0) || (prevKey != key);
+    const unsigned heads = __ballot_sync(FULL, head);
+    const int segStart = 31 - __clz(heads & (FULL >> (31 - lane)));
+#pragma unroll
+    for (int d = 1; d < 32; d <<= 1) {
+#pragma unroll
+        for (int k = 0; k < 5; ++k) {
+            const float o = __shfl_up_sync(FULL, v[k], d);
+            if (lane - d >= segStart) v[k] += o;
+        }
+    }
+    const int nextKey = __shfl_down_sync(FULL, key, 1);
+    const bool tail = (lane == 31) || (nextKey != key);
+    if (tail && key >= 0) finish_run(a, key, v, sx, sy, zr, zc);
 }
 
 __device__ __forceinline__ int wrap_minus(int v, int n, int per) { return v > 0 ? v - 1 : (per ? n - 1 : -1); }
@@ -524,6 +768,286 @@ __device__ __forceinline__ T issue_segment(const CollideArgs<T>& a, WarpStage<T,
     return halo;
 }
 
+// ---------------------------------------------------------------------------
+// Staging of aligned rows (nz % 4 == 0) with per-thread 16-byte cp.async
+// through the load/store path: a segment's rows go out as many small copies
+// (19 population rows, the voxel row, the surface-velocity rows and up to 10
+// halo chunks), and bulk copies of that size are bounded by the per-operation
+// rate of the bulk-copy unit rather than by DRAM.  Completion is tracked per
+// thread with commit groups (one group per segment).
+__device__ __forceinline__ void cp16(void* dst, const void* src) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_addr(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int P>
+__device__ __forceinline__ void cp_wait() {
+    asm volatile("cp.async.wait_group %0;" ::"n"(P) : "memory");
+}
+
+template <typename Fn, int... Ts>
+__device__ __forceinline__ void unroll_seq(std::integer_sequence<int, Ts...>, Fn&& fn) {
+    (fn(std::integral_constant<int, Ts>{}), ...);
+}
+
+// Element offset of the source row of direction I (even: slot I of the own row;
+// odd: slot opp I of row x - c_I, or slot I of the own row beyond a wall).
+template <bool ODD, int I>
+__device__ __forceinline__ size_t src_row(const long long* row, size_t N, size_t own) {
+    if constexpr (!ODD || I == 0) {
+        return (size_t)I * N + own;
+    } else {
+        const long long r = row[row_slot(-cx(I), -cy(I))];
+        return r >= 0 ? (size_t)opp(I) * N + (size_t)r : (size_t)I * N + own;
+    }
+}
+
+template <typename T, bool ODD, bool STAGE_UP>
+__device__ __forceinline__ void issue_segment_lsu(const CollideArgs<T>& a, WarpStage<T, STAGE_UP>& st, int b,
+                                                  long long seg, int nzseg) {
+    constexpr int V = WarpStage<T>::V;   // elements per 16-byte chunk
+    constexpr int CPR = SEGW / V;        // chunks per row of a segment
+    constexpr int RPI = 32 / CPR;        // rows per warp pass
+    static_assert(CPR * RPI == 32, "a warp pass covers whole rows");
+    const int lane = threadIdx.x & 31;
+    const Geom& g = a.g;
+    const SegGeo s = seg_geo(g, seg, nzseg);
+    const size_t N = g.N;
+    const size_t own = ((size_t)s.x * g.ny + s.y) * g.nz;
+    if (lane < 9) st.row[b][lane] = row_off(g, s, lane / 3 - 1, lane % 3 - 1);
+    if (lane == 9) {
+        st.geo[b][0] = s.x; st.geo[b][1] = s.y; st.geo[b][2] = s.z0; st.geo[b][3] = s.len; st.geo[b][4] = 0;
+    }
+    __syncwarp();
+    const long long* row = st.row[b];
+    const int c = lane % CPR, sub = lane / CPR;
+    const bool cin = c * V < s.len;   // rows of aligned lattices end on a chunk boundary
+    const T* f = a.f;
+    // population rows: pass t covers directions t * RPI + sub
+    unroll_seq(std::make_integer_sequence<int, (Q + RPI - 1) / RPI>{}, [&](auto tc) {
+        constexpr int t = decltype(tc)::value;
+        constexpr int i0 = t * RPI, i1 = t * RPI + 1;
+        if constexpr (RPI == 1 || i1 >= Q) {
+            if (sub == 0 && cin) cp16(&st.f[b][i0][V + c * V], f + src_row<ODD, i0>(row, N, own) + s.z0 + c * V);
+        } else {
+            const size_t off = sub == 0 ? src_row<ODD, i0>(row, N, own) : src_row<ODD, i1>(row, N, own);
+            if (cin) cp16(&st.f[b][sub == 0 ? i0 : i1][V + c * V], f + off + s.z0 + c * V);
+        }
+    });
+    // then: halo chunks (odd phase, 10), voxel row (SEGW / 4 chunks), surface-velocity rows (3 CPR)
+    constexpr int NH = ODD ? 10 : 0, NV = SEGW / 4, NU = STAGE_UP ? 3 * CPR : 0;
+    constexpr int NX = NH + NV + NU;
+#pragma unroll
+    for (int k = lane; k < ((NX + 31) / 32) * 32; k += 32) {
+        if (k < NH) {
+            const int i = zdir(k);
+            const long long r = row[row_slot(-cx(i), -cy(i))];
+            if (r < 0) continue;
+            int zc;     // first element of the chunk holding the halo (-1: beyond a z wall)
+            T* dst;
+            if (cz(i) > 0) {
+                zc = s.z0 - V;
+                if (zc < 0) zc = g.per[2] ? zc + g.nz : -1;
+                dst = &st.f[b][i][0];
+            } else {
+                zc = s.z0 + s.len;
+                if (zc >= g.nz) zc = g.per[2] ? zc - g.nz : -1;
+                dst = &st.f[b][i][V + s.len];
+            }
+            if (zc >= 0) cp16(dst, f + (size_t)opp(i) * N + (size_t)r + zc);
+        } else if (k < NH + NV) {
+            const int cv = k - NH;
+            if (cv * 4 < s.len) cp16(&st.vox[b][cv * 4], a.vox + own + s.z0 + cv * 4);
+        } else if (k < NX) {
+            const int u = k - NH - NV, d = u / CPR, cu = u % CPR;
+            if (STAGE_UP && cu * V < s.len)
+                cp16(&st.up[b][d][cu * V], a.up + (size_t)d * N + own + s.z0 + cu * V);
+        }
+    }
+    cp_commit();
+}
+
+// FP32 compute pass over one staged segment, two cells per lane in packed
+// pairs.  Aligned rows (!MIS): lane l takes the adjacent cells j = 2 l, 2 l + 1,
+// whose staged values and destination slots are 8-byte aligned pairs, so loads
+// and stores are 64-bit (in the odd phase the c_z != 0 directions land one slot
+// over and are moved one lane over with a shuffle).  Unaligned rows (MIS): lane
+// l takes j = l and l + 32 (32-bit accesses, conflict-free and coalesced).
+// Force and torque are reduced per run of equal owner (reduce_runs); the two
+// cells of a lane go through one warp reduction when their owners agree.
+template <bool ODD, bool FORCE, bool PER, bool MIS, bool STAGE_UP>
+__device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& a, WarpStage<float, STAGE_UP>& st,
+                                                      int b, int sx, int sy, int z0, int len, uint32_t srcrow,
+                                                      unsigned long long lead) {
+    constexpr int V = WarpStage<float>::V;
+    constexpr bool ADJ = !MIS;
+    const int lane = threadIdx.x & 31;
+    const Geom& g = a.g;
+    const size_t N = g.N;
+    float* F = a.fo;
+    const size_t own = (size_t)st.row[b][row_slot(0, 0)];
+    const int j0 = ADJ ? 2 * lane : lane, j1 = ADJ ? j0 + 1 : lane + 32;
+    const bool v0 = j0 < len, v1 = j1 < len;
+    const int za = z0 + j0, zb = z0 + j1;
+    const size_t ca = own + za, cb = own + zb;
+
+    // staged values of direction i for the lane's two cells
+    auto at2 = [&](int i) -> F2 {
+        const int shift = (ODD && cz(i) != 0 && (PER || ((srcrow >> i) & 1u))) ? cz(i) : 0;
+        const int m = MIS ? (int)((lead >> (2 * i)) & 3u) : 0;
+        const float* p = &st.f[b][i][V + m - shift];
+        if (ADJ && (shift & 1) == 0) {
+            const float2 t = *reinterpret_cast<const float2*>(p + j0);
+            return pk(t.x, t.y);
+        }
+        return pk(p[j0], p[j1]);
+    };
+    F2 f[Q];
+#pragma unroll
+    for (int i = 0; i < Q; ++i) f[i] = at2(i);
+    const int vlead = MIS ? (int)((lead >> 38) & 3u) : 0;
+    const uint32_t w0 = v0 ? st.vox[b][vlead + j0] : 0u, w1 = v1 ? st.vox[b][vlead + j1] : 0u;
+    const int n0 = min((int)(w0 & VOX_NMASK), 125), n1 = min((int)(w1 & VOX_NMASK), 125);
+    const F2 B = pk(__ldg(a.btab + n0), __ldg(a.btab + n1));
+
+    // BGK runs for every cell, the fully covered ones included (their solid
+    // correction with B = 1 returns fPre + bb up to rounding), so that a cell's
+    // result does not depend on the cell it is paired with.
+    const Mom2 m = moments2(f);
+    bgk2<FORCE>(f, m, a.omega, a.g3[0], a.g3[1], a.g3[2]);
+    F2 Fx = bc(0.f), Fy = bc(0.f), Fz = bc(0.f);
+    if (n0 > 0 || n1 > 0) {
+        auto up2 = [&](int d) -> F2 {
+            if (!STAGE_UP) {
+                const float* p = a.up + (size_t)d * N + own;
+                return pk(v0 ? __ldg(p + za) : 0.f, v1 ? __ldg(p + zb) : 0.f);
+            }
+            const int mu = MIS ? (int)((lead >> (40 + 2 * d)) & 3u) : 0;
+            const float* p = &st.up[b][d][mu];
+            if (ADJ) {
+                const float2 t = *reinterpret_cast<const float2*>(p + j0);
+                return pk(t.x, t.y);
+            }
+            return pk(p[j0], p[j1]);
+        };
+        F2 jx = m.jx, jy = m.jy, jz = m.jz;
+        if (FORCE) {   // post-collision momentum of the cells that ran BGK: j + rho g
+            const F2 h = pk(n0 < 125 ? 1.f : 0.f, n1 < 125 ? 1.f : 0.f) * (bc(1.f) + m.rhoBar);
+            jx = fma2(h, bc(a.g3[0]), jx); jy = fma2(h, bc(a.g3[1]), jy); jz = fma2(h, bc(a.g3[2]), jz);
+        }
+        psm2(f, m.rhoBar, jx, jy, jz, m.invRho, up2(0), up2(1), up2(2), B, at2, Fx, Fy, Fz);
+    }
+
+    // Stores.  put(off, x, y, vx, vy): values x, y into slots off, off + 1 (ADJ:
+    // one 64-bit store when both are valid and the pair is aligned).
+    auto put = [&](size_t off, float x, float y, bool vx, bool vy) {
+        if (vx && vy && ((uintptr_t)(F + off) & 7u) == 0) {
+            *reinterpret_cast<float2*>(F + off) = make_float2(x, y);
+        } else {
+            if (vx) F[off] = x;
+            if (vy) F[off + 1] = y;
+        }
+    };
+    // the lane's two cells into slots (i, base + j0) and (i, base + j1)
+    auto put_cells = [&](size_t base, F2 v) {
+        const float2 t = upk(v);
+        if (ADJ) {
+            put(base + j0, t.x, t.y, v0, v1);
+        } else {
+            if (v0) F[base + j0] = t.x;
+            if (v1) F[base + j1] = t.y;
+        }
+    };
+    if (!ODD) {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) put_cells((size_t)opp(i) * N + own + z0, f[i]);
+    } else {
+        put_cells(own + z0, f[0]);
+        const int per_z = PER ? 1 : g.per[2];
+#pragma unroll
+        for (int i = 1; i < Q; ++i) {
+            const long long r = st.row[b][row_slot(cx(i), cy(i))];
+            if (!PER && r < 0) {            // beyond an x / y wall: bounce back in place
+                put_cells((size_t)opp(i) * N + own + z0, f[i]);
+                continue;
+            }
+            const size_t dst = (size_t)i * N + (size_t)r;   // row x + c_i
+            if (cz(i) == 0) {
+                put_cells(dst + z0, f[i]);
+                continue;
+            }
+            // c_z != 0: each cell to slot z + c_z (wrapped, or bounced back at a z wall)
+            const float2 t = upk(f[i]);
+            if (ADJ) {
+                // slots (j0, j0 + 1) of this lane receive cells (j0 - 1, j0) (c_z = +1)
+                // or (j0 + 1, j0 + 2) (c_z = -1), one lane over; the cell whose slot
+                // lies outside the segment (je) is stored on its own
+                if (cz(i) > 0) put(dst + z0 + j0, __shfl_up_sync(FULL, t.y, 1), t.x, lane > 0 && v0, v1);
+                else put(dst + z0 + j0, t.y, __shfl_down_sync(FULL, t.x, 1), v1, j0 + 2 < len);
+                const int je = cz(i) > 0 ? len - 1 : 0;
+                const int ze = z0 + je;
+                const int zd = cz(i) > 0 ? wrap_plus(ze, g.nz, per_z) : wrap_minus(ze, g.nz, per_z);
+                const size_t eoff = (PER || zd >= 0) ? dst + zd : (size_t)opp(i) * N + own + ze;
+                const float ev = (je & 1) ? t.y : t.x;
+                if (lane == (je >> 1)) F[eoff] = ev;
+            } else {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (h == 0 ? !v0 : !v1) continue;
+                    const int zz = h == 0 ? za : zb;
+                    const int zd = cz(i) > 0 ? wrap_plus(zz, g.nz, per_z) : wrap_minus(zz, g.nz, per_z);
+                    const float val = h == 0 ? t.x : t.y;
+                    if (PER || zd >= 0) F[dst + zd] = val;
+                    else F[(size_t)opp(i) * N + own + zz] = val;
+                }
+            }
+        }
+    }
+
+    const float2 fx = upk(Fx), fy = upk(Fy), fz = upk(Fz);
+    if (a.cf) {
+        if (v0) { a.cf[ca] = fx.x; a.cf[N + ca] = fy.x; a.cf[2 * N + ca] = fz.x; }
+        if (v1) { a.cf[cb] = fx.y; a.cf[N + cb] = fy.y; a.cf[2 * N + cb] = fz.y; }
+    }
+    if ((PER || g.per[2]) && len == g.nz) {
+        // the segment is a whole z-periodic row: a particle's chord may wrap
+        // around inside it, so the arms are taken per cell
+        float va[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, vb[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        const int ka = v0 ? cell_force_terms(a, w0, sx, sy, za, fx.x, fy.x, fz.x, va) : -1;
+        const int kb = v1 ? cell_force_terms(a, w1, sx, sy, zb, fx.y, fy.y, fz.y, vb) : -1;
+        if (__all_sync(FULL, ka < 0 || kb < 0 || ka == kb)) {
+            const int key = ka >= 0 ? ka : kb;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) va[q] += vb[q];
+            reduce_forces(a, key, va);
+        } else {
+            reduce_forces(a, ka, va);
+            reduce_forces(a, kb, vb);
+        }
+        return;
+    }
+    // runs of equal owner tag, arms from the segment's middle point zc
+    const int zc = z0 + SEGW / 2;
+    const int ka = (v0 && (w0 & VOX_NMASK)) ? (int)(w0 >> VOX_NBITS) : -1;
+    const int kb = (v1 && (w1 & VOX_NMASK)) ? (int)(w1 >> VOX_NBITS) : -1;
+    const float da = (float)(za - zc), db = (float)(zb - zc);
+    float va[5] = {fx.x, fy.x, fz.x, -da * fy.x, da * fx.x};
+    float vb[5] = {fx.y, fy.y, fz.y, -db * fy.y, db * fx.y};
+#pragma unroll
+    for (int q = 0; q < 5; ++q) {
+        if (ka < 0) va[q] = 0.f;
+        if (kb < 0) vb[q] = 0.f;
+    }
+    if (__all_sync(FULL, ka < 0 || kb < 0 || ka == kb)) {
+        const int key = ka >= 0 ? ka : kb;
+#pragma unroll
+        for (int q = 0; q < 5; ++q) va[q] += vb[q];
+        reduce_runs(a, key, va, ka >= 0 ? za : zb, sx, sy, zc);
+    } else {
+        reduce_runs(a, ka, va, za, sx, sy, zc);
+        reduce_runs(a, kb, vb, zb, sx, sy, zc);
+    }
+}
+
 // PER: every axis periodic (no wall cases; shifts and neighbour rows are fixed).
 // MIS: rows not 16-byte aligned (see issue_segment).
 // BATCH: segments of many domains, numbered domain after domain (seg0[d] is
@@ -537,6 +1061,8 @@ k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const Coll
     // many short rows of a batch read them directly (three more small copies per
     // segment cost more there than the loads they replace)
     constexpr bool STAGE_UP = !BATCH;
+    // FP32 form, aligned rows of a single lattice: staging by per-thread cp.async
+    constexpr bool LSU = sizeof(T) == 4 && !MIS && !BATCH;
     extern __shared__ __align__(16) unsigned char smem_raw[];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
@@ -551,6 +1077,10 @@ k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const Coll
     long long seg = (long long)blockIdx.x * WARPS + warp;
     if (seg >= nseg) return;
     auto issue = [&](int buf, long long sg) -> T {
+        if constexpr (LSU) {
+            issue_segment_lsu<T, ODD, STAGE_UP>(a1, st, buf, sg, nzseg1);
+            return T(0);
+        }
         if (BATCH) {
             const int d = find_domain(seg0, ndom, (int)sg);
             const CollideArgs<T>& A = dargs[d];
@@ -566,13 +1096,20 @@ k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const Coll
         const long long next = seg + stride;
         T hnext = T(0);
         if (next < nseg) hnext = issue(b ^ 1, next);
-        const bool ok = mbar_wait(&st.bar[b], (phase >> b) & 1u);
-        phase ^= 1u << b;
-        if (__any_sync(FULL, !ok)) {
-            // a copy did not land: report, let in-flight copies finish, leave
-            if (lane == 0) atomicOr(BATCH ? dargs[0].err : a1.err, 0x20u);   // LBDEM_DEVERR_TIMEOUT
-            if (next < nseg) mbar_wait(&st.bar[b ^ 1], (phase >> (b ^ 1)) & 1u);
-            return;
+        if constexpr (LSU) {
+            // this thread's copies of the current segment (all groups but the newest)
+            if (next < nseg) cp_wait<1>();
+            else cp_wait<0>();
+            __syncwarp();   // and every other lane's
+        } else {
+            const bool ok = mbar_wait(&st.bar[b], (phase >> b) & 1u);
+            phase ^= 1u << b;
+            if (__any_sync(FULL, !ok)) {
+                // a copy did not land: report, let in-flight copies finish, leave
+                if (lane == 0) atomicOr(BATCH ? dargs[0].err : a1.err, 0x20u);   // LBDEM_DEVERR_TIMEOUT
+                if (next < nseg) mbar_wait(&st.bar[b ^ 1], (phase >> (b ^ 1)) & 1u);
+                return;
+            }
         }
         const int sx = st.geo[b][0], sy = st.geo[b][1], z0 = st.geo[b][2], len = st.geo[b][3];
         const CollideArgs<T>& a = BATCH ? dargs[st.geo[b][4]] : a1;
@@ -611,51 +1148,57 @@ k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const Coll
             for (int i = 1; i < Q; ++i)
                 if (cz(i) != 0 && st.row[b][row_slot(-cx(i), -cy(i))] >= 0) srcrow |= 1u << i;
         }
-        const int vlead = MIS ? (int)((lead >> 38) & 3u) : 0;
+        if constexpr (sizeof(T) == 4) {
+            // FP32 form: packed pairs of cells
+            collide_segment_pairs<ODD, FORCE, PER, MIS, STAGE_UP>(a, st, b, sx, sy, z0, len, srcrow, lead);
+        } else {
+            // FP64 form: one cell per lane at a time, the reference's double sequence
+            const int vlead = MIS ? (int)((lead >> 38) & 3u) : 0;
 #pragma unroll 1
-        for (int j = lane; j < SEGW; j += 32) {
-            int key = -1;
-            T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-            if (j < len) {
-                const int z = z0 + j;
-                const size_t c = own + z;
-                // smem index of direction i: V + lead_i + j - shift_i, shift_i = c_z,i
-                // when the source row x - c_i exists (odd phase)
-                auto at = [&](int i) -> const T& {
-                    const int shift = (ODD && cz(i) != 0 && (PER || ((srcrow >> i) & 1u))) ? cz(i) : 0;
-                    const int m = MIS ? (int)((lead >> (2 * i)) & 3u) : 0;
-                    return st.f[b][i][V + m + j - shift];
-                };
-                T f[Q];
+            for (int j = lane; j < SEGW; j += 32) {
+                int key = -1;
+                T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+                if (j < len) {
+                    const int z = z0 + j;
+                    const size_t c = own + z;
+                    // smem index of direction i: V + lead_i + j - shift_i, shift_i = c_z,i
+                    // when the source row x - c_i exists (odd phase)
+                    auto at = [&](int i) -> const T& {
+                        const int shift = (ODD && cz(i) != 0 && (PER || ((srcrow >> i) & 1u))) ? cz(i) : 0;
+                        const int m = MIS ? (int)((lead >> (2 * i)) & 3u) : 0;
+                        return st.f[b][i][V + m + j - shift];
+                    };
+                    T f[Q];
 #pragma unroll
-                for (int i = 0; i < Q; ++i) f[i] = at(i);
-                const uint32_t w = st.vox[b][vlead + j];
-                T Fx, Fy, Fz;
-                auto upv = [&](int d) -> T {
-                    if (!STAGE_UP) return __ldg(a.up + (size_t)d * N + c);
-                    const int m = MIS ? (int)((lead >> (40 + 2 * d)) & 3u) : 0;
-                    return st.up[b][d][m + j];
-                };
-                collide_cell<T, FORCE>(a, f, w, [&](int i) { return at(i); }, upv, Fx, Fy, Fz);
-                if (!ODD) {
+                    for (int i = 0; i < Q; ++i) f[i] = at(i);
+                    const uint32_t w = st.vox[b][vlead + j];
+                    T Fx, Fy, Fz;
+                    auto upv = [&](int d) -> T {
+                        if (!STAGE_UP) return __ldg(a.up + (size_t)d * N + c);
+                        const int m = MIS ? (int)((lead >> (40 + 2 * d)) & 3u) : 0;
+                        return st.up[b][d][m + j];
+                    };
+                    collide_cell<T, FORCE>(a, f, w, [&](int i) { return at(i); }, upv, Fx, Fy, Fz);
+                    if (!ODD) {
 #pragma unroll
-                    for (int i = 0; i < Q; ++i) F[(size_t)opp(i) * N + c] = f[i];
-                } else {
-                    F[c] = f[0];
-                    const int zm = wrap_minus(z, g.nz, PER ? 1 : g.per[2]);
-                    const int zp = wrap_plus(z, g.nz, PER ? 1 : g.per[2]);
+                        for (int i = 0; i < Q; ++i) F[(size_t)opp(i) * N + c] = f[i];
+                    } else {
+                        F[c] = f[0];
+                        const int zm = wrap_minus(z, g.nz, PER ? 1 : g.per[2]);
+                        const int zp = wrap_plus(z, g.nz, PER ? 1 : g.per[2]);
 #pragma unroll
-                    for (int i = 1; i < Q; ++i) {
-                        const long long r = st.row[b][row_slot(cx(i), cy(i))];
-                        const int zd = pick(cz(i), zm, z, zp);
-                        if (PER || (r >= 0 && zd >= 0)) F[(size_t)i * N + (size_t)r + zd] = f[i];
-                        else F[(size_t)opp(i) * N + c] = f[i];
+                        for (int i = 1; i < Q; ++i) {
+                            const long long r = st.row[b][row_slot(cx(i), cy(i))];
+                            const int zd = pick(cz(i), zm, z, zp);
+                            if (PER || (r >= 0 && zd >= 0)) F[(size_t)i * N + (size_t)r + zd] = f[i];
+                            else F[(size_t)opp(i) * N + c] = f[i];
+                        }
                     }
+                    if (a.cf) { a.cf[c] = Fx; a.cf[N + c] = Fy; a.cf[2 * N + c] = Fz; }
+                    key = cell_force_terms(a, w, sx, sy, z, Fx, Fy, Fz, v);
                 }
-                if (a.cf) { a.cf[c] = Fx; a.cf[N + c] = Fy; a.cf[2 * N + c] = Fz; }
-                key = cell_force_terms(a, w, sx, sy, z, Fx, Fy, Fz, v);
+                reduce_forces(a, key, v);
             }
-            reduce_forces(a, key, v);
         }
         __syncwarp();   // buffer b is free for the segment after next
         hcur = hnext;

@@ -160,24 +160,41 @@ def polydisperse_512(seed: int = 2025) -> tuple[tuple[int, int, int], Particles]
 
 
 def channels(n_domains: int = 512, seed: int = 2026, tau: float = 0.6, rho_in: float = 1.0,
-             rho_out: float = 0.999) -> list[tuple[dict, Particles]]:
-    """Independent channels: Lx ~ U{64..160}, Ly = Lz ~ U{24..48}, walls in y and z,
-    x periodic and driven by the Zhang pressure drop between the planes x = 0 and
-    x = Lx - 1 (interior rows, as examples/showcaseRectChannel); 1..40 spheres
-    of radius U[3, 6] per channel (fewer where random sequential addition does not
-    fit them), v ~ N(0, 0.01), omega ~ N(0, 1e-3).  Returns (domain, locals) pairs;
-    a domain's max_particles leaves room for the periodic images."""
+             rho_out: float = 0.999, flow_axis: int = 2) -> list[tuple[dict, Particles]]:
+    """Independent channels: length U{64..160} along the flow, square cross-section
+    U{24..48}, walls on the four sides, periodic along the flow and driven by the
+    Zhang pressure drop between the first and last plane (interior rows, as
+    examples/showcaseRectChannel); 1..40 spheres of radius U[3, 6] per channel
+    (fewer where random sequential addition does not fit them), v ~ N(0, 0.01),
+    omega ~ N(0, 1e-3).  flow_axis 2 (default) stores the flow along z, the
+    fastest-varying axis of the layout (long rows for the collide-stream
+    segments); flow_axis 0 keeps it along x.  The same seed gives mirror images
+    of the same channels in either orientation.  Returns (domain, locals)
+    pairs; a domain's max_particles leaves room for the periodic images."""
     rng = np.random.default_rng(seed)
     out = []
     for k in range(n_domains):
         lx = int(rng.integers(64, 161))
         l = int(rng.integers(24, 49))
-        shape = (lx, l, l)
+        shape_x = (lx, l, l)
         want = int(rng.integers(1, 41))
-        p = suspension(shape, n_max=want, rmin=3.0, rmax=6.0, seed=seed * 100003 + k, periodic=(1, 0, 0),
+        p = suspension(shape_x, n_max=want, rmin=3.0, rmax=6.0, seed=seed * 100003 + k, periodic=(1, 0, 0),
                        max_trials=20000)
-        dom = {"shape": shape, "periodic": (1, 0, 0), "omega": 1.0 / tau, "max_particles": 2 * max(p.n, 1),
-               "drop": {"dimension": 0, "inlet": [0, 0, 1, l - 2, 1, l - 2],
-                        "outlet": [lx - 1, lx - 1, 1, l - 2, 1, l - 2], "rho_in": rho_in, "rho_out": rho_out}}
+        if flow_axis == 2:   # swap x and z: a reflection, so the angular velocity also changes sign
+            shape = (l, l, lx)
+            perm = [2, 1, 0]
+            p = Particles(np.ascontiguousarray(p.x[:, perm]), np.ascontiguousarray(p.v[:, perm]),
+                          np.ascontiguousarray(-p.w[:, perm]), p.r, p.tag)
+            periodic = (0, 0, 1)
+            inlet = [1, l - 2, 1, l - 2, 0, 0]
+            outlet = [1, l - 2, 1, l - 2, lx - 1, lx - 1]
+        else:
+            shape = shape_x
+            periodic = (1, 0, 0)
+            inlet = [0, 0, 1, l - 2, 1, l - 2]
+            outlet = [lx - 1, lx - 1, 1, l - 2, 1, l - 2]
+        dom = {"shape": shape, "periodic": periodic, "omega": 1.0 / tau, "max_particles": 2 * max(p.n, 1),
+               "drop": {"dimension": flow_axis, "inlet": inlet, "outlet": outlet, "rho_in": rho_in,
+                        "rho_out": rho_out}}
         out.append((dom, p))
     return out

@@ -109,16 +109,20 @@ def test_fp64_parity(gpu, oracle, case):
     assert any(np.abs(r[2]).max() > 0 for r in res), "no force was exercised"
 
 
-@pytest.mark.parametrize("case", ["periodic_overlap", "channel_force", "long_z_walls", "long_z_periodic"])
+@pytest.mark.parametrize("case", ["periodic_overlap", "channel_force", "closed_box", "long_z_walls", "long_z_periodic",
+                                  "odd_long_z"])
 def test_fp32_dev_parity(gpu, oracle, case):
     res = _run(gpu, oracle, case, gpu.PREC_FP32_DEV, steps=6)
     for s, (fg, fo, Fg, Fo, Tg, To, ost, g, cfg) in enumerate(res):
         assert rel_err(fg, fo) <= 2e-5, f"step {s}: populations {rel_err(fg, fo):.3e}"
-    # FP32 form against the FP64 oracle on the same inputs: per-particle force
+    # FP32 form against the FP64 oracle on the same inputs: per-particle force and
+    # torque (the FP32 form takes torque arms per run of cells of one particle)
     res64 = _run(gpu, oracle, case, gpu.PREC_FP64, steps=6)
     for s in range(len(res)):
         F32, F64 = res[s][2], res64[s][3]
+        T32, T64 = res[s][4], res64[s][5]
         assert rel_err(F32, F64) <= 1e-4, f"step {s}: FP32 force error {rel_err(F32, F64):.3e}"
+        assert rel_err(T32, T64) <= 1e-4, f"step {s}: FP32 torque error {rel_err(T32, T64):.3e}"
 
 
 def test_mass_and_fields(gpu, oracle):
