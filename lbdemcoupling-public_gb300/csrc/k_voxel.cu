@@ -318,6 +318,14 @@ __device__ __forceinline__ void voxelize_tile(VoxSmem<T, INIT_VEL>& S, int t, co
     const int tz = rem - ty * tnz;
     const int X0 = tx * TILE, Y0 = ty * TILE, Z0 = tz * TILE;
 
+    // the cell-state loads go out first: their latency overlaps the list loads
+    uint32_t wv[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int l = tid + h * VOX_THREADS;
+        const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
+        wv[h] = (X < g.nx && Y < g.ny && Z < g.nz) ? vox[((size_t)X * g.ny + Y) * g.nz + Z] : 0u;
+    }
     int cnt = tile_cnt[t];
     if (cnt <= 0) return;
     __syncthreads();
@@ -349,8 +357,7 @@ __device__ __forceinline__ void voxelize_tile(VoxSmem<T, INIT_VEL>& S, int t, co
     for (int h = 0; h < 2; ++h) {
         const int l = tid + h * VOX_THREADS;
         const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
-        uint32_t w0 = 0;
-        if (X < g.nx && Y < g.ny && Z < g.nz) w0 = vox[((size_t)X * g.ny + Y) * g.nz + Z];
+        const uint32_t w0 = wv[h];
         S.n[l] = (uint8_t)(w0 & VOX_NMASK);
         S.id[l] = w0 >> VOX_NBITS;
         S.flags[l] = 0;

@@ -21,19 +21,39 @@ constexpr uint32_t VOX_NMASK = (1u << VOX_NBITS) - 1u;
 constexpr int32_t MAX_TAG_LIMIT = (1 << 25) - 1;
 constexpr int COLLIDE_BLOCK = 128;      // threads per block along z in the collide-stream kernel
 
-// Lattice velocities, Palabos D3Q19 order.
-__host__ __device__ constexpr int cx(int i) {
+// Lattice velocities, Palabos D3Q19 order.  Each component is stored as
+// c + 1 in two bits per direction of a 64-bit constant, so that a lookup with a
+// run-time index is a shift and a mask.
+namespace lattice_table {
+constexpr int cx_of(int i) {
     return (i == 1 || i == 4 || i == 5 || i == 6 || i == 7) ? -1
          : (i == 10 || i == 13 || i == 14 || i == 15 || i == 16) ? 1 : 0;
 }
-__host__ __device__ constexpr int cy(int i) {
+constexpr int cy_of(int i) {
     return (i == 2 || i == 4 || i == 8 || i == 9 || i == 14) ? -1
          : (i == 5 || i == 11 || i == 13 || i == 17 || i == 18) ? 1 : 0;
 }
-__host__ __device__ constexpr int cz(int i) {
+constexpr int cz_of(int i) {
     return (i == 3 || i == 6 || i == 8 || i == 16 || i == 18) ? -1
          : (i == 7 || i == 9 || i == 12 || i == 15 || i == 17) ? 1 : 0;
 }
+constexpr unsigned long long pack(int axis) {
+    unsigned long long p = 0;
+    for (int i = 0; i < 19; ++i)
+        p |= (unsigned long long)((axis == 0 ? cx_of(i) : axis == 1 ? cy_of(i) : cz_of(i)) + 1) << (2 * i);
+    return p;
+}
+constexpr unsigned long long CX = pack(0), CY = pack(1), CZ = pack(2);
+}  // namespace lattice_table
+__host__ __device__ constexpr int cx(int i) { return (int)((lattice_table::CX >> (2 * i)) & 3u) - 1; }
+__host__ __device__ constexpr int cy(int i) { return (int)((lattice_table::CY >> (2 * i)) & 3u) - 1; }
+__host__ __device__ constexpr int cz(int i) { return (int)((lattice_table::CZ >> (2 * i)) & 3u) - 1; }
+namespace lattice_table {
+constexpr bool same(int i) {
+    return i == 19 || (cx(i) == cx_of(i) && cy(i) == cy_of(i) && cz(i) == cz_of(i) && same(i + 1));
+}
+static_assert(same(0), "packed lattice velocities");
+}  // namespace lattice_table
 __host__ __device__ constexpr int opp(int i) { return i == 0 ? 0 : (i <= 9 ? i + 9 : i - 9); }
 __host__ __device__ constexpr double wt(int i) {
     return i == 0 ? 1.0 / 3.0 : ((i == 1 || i == 2 || i == 3 || i == 10 || i == 11 || i == 12) ? 1.0 / 18.0 : 1.0 / 36.0);
