@@ -52,10 +52,17 @@ template <typename T>
 struct EqVals { T v[Q]; };
 
 template <typename T>
-__global__ void k_fill_equilibrium(T* __restrict__ f, EqVals<T> e, Geom g) {
+__global__ void k_fill_equilibrium(T* __restrict__ f, EqVals<T> e, int phase, Geom g) {
     for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.N; c += (size_t)gridDim.x * blockDim.x) {
+        if (phase == 0) {
 #pragma unroll
-        for (int i = 0; i < Q; ++i) f[(size_t)i * g.N + c] = e.v[i];
+            for (int i = 0; i < Q; ++i) f[(size_t)i * g.N + c] = e.v[i];
+        } else {   // odd layout: f_i of a cell sits in slot (opp i, x - c_i), or (i, x) beyond a wall
+            int x, y, z;
+            decompose(c, g, x, y, z);
+#pragma unroll
+            for (int i = 0; i < Q; ++i) f[slot_index(i, x, y, z, phase, g)] = e.v[i];
+        }
     }
 }
 
@@ -128,7 +135,7 @@ cudaError_t launch_pop_scatter(T* f, const T* in, int i, int phase, Geom g, cuda
     return cudaGetLastError();
 }
 template <typename T>
-cudaError_t launch_fill_equilibrium(T* f, double rho_bar, const double* u, Geom g, cudaStream_t s) {
+cudaError_t launch_fill_equilibrium(T* f, double rho_bar, const double* u, int phase, Geom g, cudaStream_t s) {
     // Palabos iniCellAtEquilibrium: j = rho u; feq_i = t_i [rhoBar + 3 c.j + invRho (4.5 (c.j)^2 - 1.5 j.j)]
     EqVals<T> e;
     const T rb = T(rho_bar);
@@ -140,7 +147,7 @@ cudaError_t launch_fill_equilibrium(T* f, double rho_bar, const double* u, Geom 
         const T cj = T(cx(i)) * j[0] + T(cy(i)) * j[1] + T(cz(i)) * j[2];
         e.v[i] = T(wt(i)) * (rb + T(3) * cj + invRho * (T(4.5) * cj * cj - T(1.5) * jSqr));
     }
-    k_fill_equilibrium<T><<<grid_for(g.N, 256), 256, 0, s>>>(f, e, g);
+    k_fill_equilibrium<T><<<grid_for(g.N, 256), 256, 0, s>>>(f, e, phase, g);
     return cudaGetLastError();
 }
 template <typename T>
@@ -161,7 +168,7 @@ cudaError_t launch_vox_fields(const uint32_t* vox, double* sf, int32_t* id, uint
 #define INST(T)                                                                                      \
     template cudaError_t launch_pop_gather<T>(const T*, T*, int, int, Geom, cudaStream_t);           \
     template cudaError_t launch_pop_scatter<T>(T*, const T*, int, int, Geom, cudaStream_t);          \
-    template cudaError_t launch_fill_equilibrium<T>(T*, double, const double*, Geom, cudaStream_t);  \
+    template cudaError_t launch_fill_equilibrium<T>(T*, double, const double*, int, Geom, cudaStream_t);  \
     template cudaError_t launch_macro<T>(const T*, int, double*, double*, Geom, cudaStream_t);       \
     template cudaError_t launch_mass<T>(const T*, double*, Geom, cudaStream_t);
 INST(float)

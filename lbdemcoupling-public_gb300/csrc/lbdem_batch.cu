@@ -609,11 +609,12 @@ lbdem_status lbdem_batch_init_equilibrium(lbdem_batch* b, double rho_bar, const 
     if (!b || !u) return fail(b, LBDEM_ERR_INVALID_ARG, "batch_init_equilibrium: null argument");
     if (!(rho_bar > -1.0) || !std::isfinite(rho_bar)) return fail(b, LBDEM_ERR_INVALID_ARG, "rho_bar <= -1");
     DeviceGuard dg(b->device);
+    const int phase = (int)(b->step & 1);
     for (int d = 0; d < b->ndom; ++d) {
         if (b->prec == LBDEM_PREC_FP64)
-            BK(b, launch_fill_equilibrium<double>(fptr<double>(b, d), rho_bar, u, b->views[d].g, b->stream));
+            BK(b, launch_fill_equilibrium<double>(fptr<double>(b, d), rho_bar, u, phase, b->views[d].g, b->stream));
         else
-            BK(b, launch_fill_equilibrium<float>(fptr<float>(b, d), rho_bar, u, b->views[d].g, b->stream));
+            BK(b, launch_fill_equilibrium<float>(fptr<float>(b, d), rho_bar, u, phase, b->views[d].g, b->stream));
         b->launches += 1;
     }
     b->pavg_valid = false;

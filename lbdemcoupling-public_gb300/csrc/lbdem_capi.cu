@@ -419,8 +419,11 @@ lbdem_status lbdem_init_equilibrium(lbdem_handle* h, double rho_bar, const doubl
     if (!h || !u) return fail(h, LBDEM_ERR_INVALID_ARG, "init_equilibrium: null argument");
     if (!(rho_bar > -1.0) || !std::isfinite(rho_bar)) return fail(h, LBDEM_ERR_INVALID_ARG, "rho_bar <= -1");
     DeviceGuard dg(h->device);
-    if (h->prec == LBDEM_PREC_FP64) CK(h, launch_fill_equilibrium<double>((double*)h->f, rho_bar, u, h->g, h->stream));
-    else CK(h, launch_fill_equilibrium<float>((float*)h->f, rho_bar, u, h->g, h->stream));
+    const int phase = (int)(h->step & 1);
+    if (h->prec == LBDEM_PREC_FP64)
+        CK(h, launch_fill_equilibrium<double>((double*)h->f, rho_bar, u, phase, h->g, h->stream));
+    else
+        CK(h, launch_fill_equilibrium<float>((float*)h->f, rho_bar, u, phase, h->g, h->stream));
     h->launches += 1;
     h->pavg_valid = false;
     return LBDEM_OK;

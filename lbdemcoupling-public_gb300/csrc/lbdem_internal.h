@@ -196,7 +196,7 @@ cudaError_t launch_pop_gather(const T* f, T* out, int i, int phase, Geom g, cuda
 template <typename T>
 cudaError_t launch_pop_scatter(T* f, const T* in, int i, int phase, Geom g, cudaStream_t s);
 template <typename T>
-cudaError_t launch_fill_equilibrium(T* f, double rho_bar, const double* u, Geom g, cudaStream_t s);
+cudaError_t launch_fill_equilibrium(T* f, double rho_bar, const double* u, int phase, Geom g, cudaStream_t s);
 template <typename T>
 cudaError_t launch_macro(const T* f, int phase, double* rho, double* u, Geom g, cudaStream_t s);
 template <typename T>

@@ -147,6 +147,25 @@ def advance(p: Particles, shape, periodic=(1, 1, 1), steps: int = 1) -> Particle
     return q
 
 
+def shuttle(p0: Particles, shape, step: int, half_period: int, periodic=(1, 1, 1)) -> Particles:
+    """Prescribed kinematics that stay near the seeded placement: every particle
+    moves with its seeded velocity v (and angular velocity w) for half_period
+    steps, then with -v (-w) for half_period steps, and so on, so |v| and |w|
+    keep their seeded distributions at every step while the displacement stays
+    within half_period |v|.  Returns the particles at the given step: positions
+    after `step` steps, and the velocities of the step that starts there."""
+    h = int(half_period)
+    k, t = divmod(int(step), 2 * h)
+    disp = t if t <= h else 2 * h - t          # net steps of +v after `step` steps
+    sign = 1.0 if t < h else -1.0
+    L = np.asarray(shape, dtype=np.float64)
+    x = p0.x + disp * p0.v
+    for a in range(3):
+        if periodic[a]:
+            x[:, a] = np.mod(x[:, a], L[a])
+    return Particles(x, sign * p0.v, sign * p0.w, p0.r.copy(), p0.tag.copy())
+
+
 def monodisperse_256(seed: int = 2024) -> tuple[tuple[int, int, int], Particles]:
     """Periodic 256^3, 2000 spheres r = 8, v ~ N(0, 0.01), omega ~ N(0, 1e-3)."""
     shape = (256, 256, 256)

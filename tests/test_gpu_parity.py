@@ -195,3 +195,23 @@ def test_bad_particles_rejected(gpu):
         gl.get_forces()
     assert gl.device_errors() & gpu.DEVERR_TAG_RANGE
     assert gl.device_errors() == 0
+
+
+@pytest.mark.parametrize("prec", [0, 1])
+@pytest.mark.parametrize("steps", [0, 1, 2])
+def test_init_equilibrium_in_either_phase(gpu, prec, steps):
+    """A uniform moving equilibrium written after an even or odd number of steps
+    (the in-place layout differs) reads back as that density and velocity in
+    every cell, next to walls too."""
+    shape = (10, 9, 12)
+    rb, u = 0.003, (0.02, -0.01, 0.015)
+    with gpu.Lattice(*shape, 1 / 0.6, periodic=(1, 0, 0), precision=prec, max_particles=4, max_tag=4,
+                     max_radius=4) as L:
+        for _ in range(steps):
+            L.collide_and_stream()
+        L.init_equilibrium(rb, u)
+        rho, vel = L.get_field(gpu.FIELD_DENSITY), L.get_field(gpu.FIELD_VELOCITY)
+        tol = 1e-14 if prec == 0 else 2e-6
+        assert np.max(np.abs(rho - (1 + rb))) <= tol
+        for a in range(3):
+            assert np.max(np.abs(vel[a] - u[a])) <= tol * 10, a
