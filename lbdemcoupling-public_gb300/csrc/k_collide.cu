@@ -866,6 +866,24 @@ __device__ __forceinline__ void issue_segment_lsu(const CollideArgs<T>& a, WarpS
     cp_commit();
 }
 
+// Force and torque of a segment that is a whole z-periodic row (per-cell arms),
+// kept out of line: the bench lattices never take it.
+__device__ __noinline__ void whole_row_forces(const CollideArgs<float>& a, uint32_t w0, uint32_t w1, bool v0, bool v1,
+                                              int sx, int sy, int za, int zb, float2 fx, float2 fy, float2 fz) {
+    float va[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, vb[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    const int ka = v0 ? cell_force_terms(a, w0, sx, sy, za, fx.x, fy.x, fz.x, va) : -1;
+    const int kb = v1 ? cell_force_terms(a, w1, sx, sy, zb, fx.y, fy.y, fz.y, vb) : -1;
+    if (__all_sync(FULL, ka < 0 || kb < 0 || ka == kb)) {
+        const int key = ka >= 0 ? ka : kb;
+#pragma unroll
+        for (int q = 0; q < 6; ++q) va[q] += vb[q];
+        reduce_forces(a, key, va);
+    } else {
+        reduce_forces(a, ka, va);
+        reduce_forces(a, kb, vb);
+    }
+}
+
 // FP32 compute pass over one staged segment, two cells per lane in packed
 // pairs.  Aligned rows (!MIS): lane l takes the adjacent cells j = 2 l, 2 l + 1,
 // whose staged values and destination slots are 8-byte aligned pairs, so loads
@@ -1011,18 +1029,7 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     if ((PER || g.per[2]) && len == g.nz) {
         // the segment is a whole z-periodic row: a particle's chord may wrap
         // around inside it, so the arms are taken per cell
-        float va[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, vb[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-        const int ka = v0 ? cell_force_terms(a, w0, sx, sy, za, fx.x, fy.x, fz.x, va) : -1;
-        const int kb = v1 ? cell_force_terms(a, w1, sx, sy, zb, fx.y, fy.y, fz.y, vb) : -1;
-        if (__all_sync(FULL, ka < 0 || kb < 0 || ka == kb)) {
-            const int key = ka >= 0 ? ka : kb;
-#pragma unroll
-            for (int q = 0; q < 6; ++q) va[q] += vb[q];
-            reduce_forces(a, key, va);
-        } else {
-            reduce_forces(a, ka, va);
-            reduce_forces(a, kb, vb);
-        }
+        whole_row_forces(a, w0, w1, v0, v1, sx, sy, za, zb, fx, fy, fz);
         return;
     }
     // runs of equal owner tag, arms from the segment's middle point zc
