@@ -34,8 +34,7 @@ namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
 
-// 1/x rounded to nearest (identical to the IEEE division 1/x).
-__device__ __forceinline__ float recip(float x) { return __frcp_rn(x); }
+// 1/x (the FP64 form; the FP32 form uses __frcp_rn, identical to the IEEE division 1/x).
 __device__ __forceinline__ double recip(double x) { return 1.0 / x; }
 
 // c_i . (a, b, c) with the zero terms removed at compile time (0 * x is not
@@ -358,6 +357,95 @@ __device__ __forceinline__ void psm2(F2 (&f)[Q], F2 rhoBar, F2 jx, F2 jy, F2 jz,
         f[i] = fma2(B, (pi - f[i]) + (A + E), f[i]);
         f[k] = fma2(B, (pkk - f[k]) + (A - E), f[k]);
         const F2 d = B2 * E;                          // F += c_k (bb - bbOpp)
+        if constexpr (cx(k) > 0) Fx = Fx + d;
+        if constexpr (cy(k) > 0) Fy = Fy + d; else if constexpr (cy(k) < 0) Fy = Fy - d;
+        if constexpr (cz(k) > 0) Fz = Fz + d; else if constexpr (cz(k) < 0) Fz = Fz - d;
+    };
+    pair(std::integral_constant<int, 10>{}); pair(std::integral_constant<int, 11>{});
+    pair(std::integral_constant<int, 12>{}); pair(std::integral_constant<int, 13>{});
+    pair(std::integral_constant<int, 14>{}); pair(std::integral_constant<int, 15>{});
+    pair(std::integral_constant<int, 16>{}); pair(std::integral_constant<int, 17>{});
+    pair(std::integral_constant<int, 18>{});
+}
+
+// bgk2 followed by psm2 in one pass over the opposite pairs (the same operations
+// in the same order, so the same bits): the pre-collision pair is still in
+// registers when its correction is applied, so fPre is not re-read.  Used for
+// unaligned rows (batch); aligned rows keep the two passes, which measured faster
+// there.  Per pair k = i + 9 (c_k = -c_i), with the solid
+// equilibrium at P = (1 + rhoBar) uPart and fb the BGK result:
+//   A = t (dB + 4.5 invRho ((c_k.P)^2 - (c_k.j)^2)),  S = 3 t c_k.(j + P),
+//   E = (fPre_k - fPre_i) - S,
+//   f_i = fb_i + B ((fPre_i - fb_i) + (A + E)),  f_k = fb_k + B ((fPre_k - fb_k) + (A - E)),
+//   F += c_k 2 B E      (src/ibCompositeDynamics3D.hh:150-200, regrouped).  hs = (n < 125) rho
+// per cell (FORCE: the solid correction's momentum j + hs g).  A cell with B = 0
+// comes out exactly as bgk2 leaves it.
+template <bool FORCE>
+__device__ __forceinline__ void bgk_psm2(F2 (&f)[Q], const Mom2& m, float omega, float gx, float gy, float gz, F2 hs,
+                                         F2 up0, F2 up1, F2 up2, F2 B, F2& Fx, F2& Fy, F2& Fz) {
+    const F2 one = bc(1.f);
+    const F2 rho = one + m.rhoBar, invRho = m.invRho;
+    // BGK constants (bgk2)
+    F2 jx = m.jx, jy = m.jy, jz = m.jz;
+    if (FORCE) {
+        const F2 h = bc(0.5f) * rho;
+        jx = fma2(h, bc(gx), jx); jy = fma2(h, bc(gy), jy); jz = fma2(h, bc(gz), jz);
+    }
+    const F2 jSqr = fma2(jz, jz, fma2(jy, jy, jx * jx));
+    const F2 base = fma2(bc(-1.5f) * invRho, jSqr, m.rhoBar);
+    const F2 om1 = bc(1.f - omega);
+    const F2 q45 = bc(4.5f) * invRho;
+    F2 ux{}, uy{}, uz{}, pre{}, ug{};
+    if (FORCE) {
+        ux = jx * invRho; uy = jy * invRho; uz = jz * invRho;
+        pre = bc(1.f - 0.5f * omega) * rho;
+        ug = fma2(uz, bc(gz), fma2(uy, bc(gy), ux * bc(gx)));
+    }
+    // solid-correction constants
+    F2 sjx = m.jx, sjy = m.jy, sjz = m.jz;
+    if (FORCE) {
+        sjx = fma2(hs, bc(gx), sjx); sjy = fma2(hs, bc(gy), sjy); sjz = fma2(hs, bc(gz), sjz);
+    }
+    const F2 rhoS = bc(1.f) + m.rhoBar;
+    const F2 px = up0 * rhoS, py = up1 * rhoS, pz = up2 * rhoS;
+    const F2 q45S = bc(4.5f) * invRho;
+    const F2 dB = (bc(-1.5f) * invRho) * (fma2(pz, pz, fma2(py, py, px * px)) - fma2(sjz, sjz, fma2(sjy, sjy, sjx * sjx)));
+    {
+        const F2 p0 = f[0];
+        F2 b0 = fma2(om1, f[0], bc(omega * (float)wt(0)) * base);
+        if (FORCE) b0 = b0 - bc(3.f * (float)wt(0)) * (pre * ug);
+        f[0] = fma2(B, (p0 - b0) - bc((float)wt(0)) * dB, b0);
+    }
+    const F2 B2 = B + B;
+    Fx = bc(0.f); Fy = bc(0.f); Fz = bc(0.f);
+    auto pair = [&](auto kc) {
+        constexpr int k = decltype(kc)::value, i = k - 9;
+        const F2 pi = f[i], pkk = f[k];
+        // BGK of the pair
+        const F2 cj = cdotk<k>(jx, jy, jz);
+        const F2 ow = bc(omega * (float)wt(k));
+        const F2 e = fma2(q45 * cj, cj, base);
+        const F2 s = bc(3.f) * cj;
+        F2 bi = fma2(om1, pi, ow * (e - s));
+        F2 bk = fma2(om1, pkk, ow * (e + s));
+        if (FORCE) {
+            const F2 cu = cdotk<k>(ux, uy, uz);
+            const float cg = cdotk_s<k>(gx, gy, gz);
+            const F2 tp = bc((float)wt(k)) * pre;
+            const F2 X = fma2(bc(9.f * cg), cu, bc(-3.f) * ug);
+            bi = fma2(tp, X - bc(3.f * cg), bi);
+            bk = fma2(tp, X + bc(3.f * cg), bk);
+        }
+        // solid correction of the pair
+        const F2 t = bc((float)wt(k));
+        const F2 cjS = cdotk<k>(sjx, sjy, sjz);
+        const F2 cu = cdotk<k>(px, py, pz);
+        const F2 A = t * fma2(q45S, (cu - cjS) * (cu + cjS), dB);
+        const F2 Sk = bc(3.f * (float)wt(k)) * (cjS + cu);
+        const F2 E = (pkk - pi) - Sk;
+        f[i] = fma2(B, (pi - bi) + (A + E), bi);
+        f[k] = fma2(B, (pkk - bk) + (A - E), bk);
+        const F2 d = B2 * E;
         if constexpr (cx(k) > 0) Fx = Fx + d;
         if constexpr (cy(k) > 0) Fy = Fy + d; else if constexpr (cy(k) < 0) Fy = Fy - d;
         if constexpr (cz(k) > 0) Fz = Fz + d; else if constexpr (cz(k) < 0) Fz = Fz - d;
@@ -931,28 +1019,39 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     // correction with B = 1 returns fPre + bb up to rounding), so that a cell's
     // result does not depend on the cell it is paired with.
     const Mom2 m = moments2(f);
-    bgk2<FORCE>(f, m, a.omega, a.g3[0], a.g3[1], a.g3[2]);
     F2 Fx = bc(0.f), Fy = bc(0.f), Fz = bc(0.f);
-    if (n0 > 0 || n1 > 0) {
-        auto up2 = [&](int d) -> F2 {
-            if (!STAGE_UP) {
-                const float* p = a.up + (size_t)d * N + own;
-                return pk(v0 ? __ldg(p + za) : 0.f, v1 ? __ldg(p + zb) : 0.f);
-            }
-            const int mu = MIS ? (int)((lead >> (40 + 2 * d)) & 3u) : 0;
-            const float* p = &st.up[b][d][mu];
-            if (ADJ) {
-                const float2 t = *reinterpret_cast<const float2*>(p + j0);
-                return pk(t.x, t.y);
-            }
-            return pk(p[j0], p[j1]);
-        };
-        F2 jx = m.jx, jy = m.jy, jz = m.jz;
-        if (FORCE) {   // post-collision momentum of the cells that ran BGK: j + rho g
-            const F2 h = pk(n0 < 125 ? 1.f : 0.f, n1 < 125 ? 1.f : 0.f) * (bc(1.f) + m.rhoBar);
-            jx = fma2(h, bc(a.g3[0]), jx); jy = fma2(h, bc(a.g3[1]), jy); jz = fma2(h, bc(a.g3[2]), jz);
+    auto up2 = [&](int d) -> F2 {
+        if (!STAGE_UP) {
+            const float* p = a.up + (size_t)d * N + own;
+            return pk(v0 ? __ldg(p + za) : 0.f, v1 ? __ldg(p + zb) : 0.f);
         }
-        psm2(f, m.rhoBar, jx, jy, jz, m.invRho, up2(0), up2(1), up2(2), B, at2, Fx, Fy, Fz);
+        const int mu = MIS ? (int)((lead >> (40 + 2 * d)) & 3u) : 0;
+        const float* p = &st.up[b][d][mu];
+        if (ADJ) {
+            const float2 t = *reinterpret_cast<const float2*>(p + j0);
+            return pk(t.x, t.y);
+        }
+        return pk(p[j0], p[j1]);
+    };
+    // FORCE: the solid correction's momentum is the BGK post-collision one, j + rho g,
+    // for the cells that ran BGK
+    auto hsol = [&]() -> F2 {
+        return FORCE ? pk(n0 < 125 ? 1.f : 0.f, n1 < 125 ? 1.f : 0.f) * (bc(1.f) + m.rhoBar) : bc(0.f);
+    };
+    if constexpr (MIS) {
+        if (__any_sync(FULL, n0 > 0 || n1 > 0))   // one pass; a no-op for the lanes' fluid cells
+            bgk_psm2<FORCE>(f, m, a.omega, a.g3[0], a.g3[1], a.g3[2], hsol(), up2(0), up2(1), up2(2), B, Fx, Fy, Fz);
+        else
+            bgk2<FORCE>(f, m, a.omega, a.g3[0], a.g3[1], a.g3[2]);
+    } else {
+        bgk2<FORCE>(f, m, a.omega, a.g3[0], a.g3[1], a.g3[2]);
+        if (n0 > 0 || n1 > 0) {
+            const F2 hs = hsol();
+            const F2 sjx = fma2(hs, bc(a.g3[0]), m.jx), sjy = fma2(hs, bc(a.g3[1]), m.jy),
+                     sjz = fma2(hs, bc(a.g3[2]), m.jz);
+            if (FORCE) psm2(f, m.rhoBar, sjx, sjy, sjz, m.invRho, up2(0), up2(1), up2(2), B, at2, Fx, Fy, Fz);
+            else psm2(f, m.rhoBar, m.jx, m.jy, m.jz, m.invRho, up2(0), up2(1), up2(2), B, at2, Fx, Fy, Fz);
+        }
     }
 
     // Stores.  put(off, x, y, vx, vy): values x, y into slots off, off + 1 (ADJ:
