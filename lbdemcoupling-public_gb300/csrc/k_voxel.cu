@@ -265,6 +265,21 @@ __device__ __noinline__ int slice_count_resolve(float dxf, float dyf, float dzf,
     return n;
 }
 
+// Sub-cell count of a shell cell by one thread (all five x-slices), out of line:
+// only taken when a chunk's shell queue is full.
+__device__ __noinline__ uint32_t shell_count_direct(float dxf, float dyf, float dzf, float rsq, float M, int X, int Y,
+                                                    int Z, const SphereDev& s) {
+    uint32_t n = 0;
+#pragma unroll 1
+    for (int i = 0; i < 5; ++i) {
+        bool unsure;
+        int c = slice_count_fast(dxf, dyf, dzf, i, rsq, M, &unsure);
+        if (unsure) c = slice_count_resolve(dxf, dyf, dzf, i, rsq, M, X, Y, Z, s);
+        n += (uint32_t)c;
+    }
+    return n;
+}
+
 // Shared memory of one voxelization block.
 constexpr int VOX_THREADS = 256;            // two cells of the 8^3 tile per thread
 constexpr int VOX_CHUNK = 32;               // spheres classified per pass
@@ -419,13 +434,7 @@ __device__ __forceinline__ void voxelize_tile(VoxSmem<T, INIT_VEL>& S, int t, co
                         if (pos < VOX_QUEUE) {
                             S.queue[pos] = (uint16_t)((k << 9) | l);
                         } else {
-                            const SphereDev& s = sph[S.sorted[base + k]];
-                            for (int i = 0; i < 5; ++i) {
-                                bool unsure;
-                                int c = slice_count_fast(dxf, dyf, dzf, i, q.rsq, M, &unsure);
-                                if (unsure) c = slice_count_resolve(dxf, dyf, dzf, i, q.rsq, M, X, Y, Z, s);
-                                n += (uint32_t)c;
-                            }
+                            n = shell_count_direct(dxf, dyf, dzf, q.rsq, M, X, Y, Z, sph[S.sorted[base + k]]);
                         }
                     }
                 }

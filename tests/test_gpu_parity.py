@@ -215,3 +215,39 @@ def test_init_equilibrium_in_either_phase(gpu, prec, steps):
         assert np.max(np.abs(rho - (1 + rb))) <= tol
         for a in range(3):
             assert np.max(np.abs(vel[a] - u[a])) <= tol * 10, a
+
+
+@pytest.mark.parametrize("kind", ["bin_overflow", "queue_overflow"])
+def test_voxelization_overflow_paths(gpu, oracle, kind):
+    """Clusters of spheres that overflow a tile's sphere bin (more than 64 spheres
+    reach one 8^3 tile: the tile re-collects its spheres from every box) or a
+    chunk's shell queue (more than 2048 shell pairs in one tile: the pairs past
+    the queue are counted directly).  Counts and owners bit-exact, FP64 surface
+    velocity bit-exact, FP32 within float rounding, populations after a step."""
+    rng = np.random.default_rng(41 if kind == "bin_overflow" else 42)
+    shape = (24, 24, 24)
+    if kind == "bin_overflow":
+        n, r = 90, rng.uniform(0.6, 1.2, 90)
+    else:
+        n, r = 40, rng.uniform(2.5, 3.5, 40)
+    x = 12.0 + rng.uniform(-2.0, 2.0, (n, 3))
+    v = rng.normal(0, 0.01, (n, 3))
+    w = rng.normal(0, 1e-3, (n, 3))
+    tag = np.arange(1, n + 1, dtype=np.int32)
+    for prec in (0, 1):
+        with gpu.Lattice(*shape, 1 / 0.6, precision=prec, max_particles=128, max_tag=128, max_radius=4) as L:
+            ol = oracle.OracleLattice(*shape, 1 / 0.6, threads=4)
+            L.set_particles(x, v, w, r, tag)
+            ol.set_particles(x, v, w, r, tag)
+            st = ol.state()
+            assert np.array_equal(L.get_field(gpu.FIELD_SUBCELL_COUNT), st["n"])
+            assert np.array_equal(L.get_field(gpu.FIELD_PARTICLE_ID), st["id"])
+            up = L.get_field(gpu.FIELD_PARTICLE_VELOCITY)
+            if prec == 0:
+                assert np.array_equal(up, st["up"])
+            else:
+                assert rel_err(up, st["up"]) <= 1e-6
+            L.collide_and_stream()
+            ol.collide_and_stream()
+            assert rel_err(L.get_populations(), ol.get_populations()) <= (1e-12 if prec == 0 else 2e-5)
+            assert L.device_errors() == 0
