@@ -291,6 +291,7 @@ struct VoxSmem {
     int raw[TILE_LIST_MAX];
     int sorted[TILE_LIST_MAX];
     SphereFast q[VOX_CHUNK];
+    uint32_t bm[VOX_CHUNK];                   // tile-local box of sphere k: x, y, z cell masks (8 bits each)
     uint32_t n4[VOX_CHUNK][TILE_CELLS / 4];   // count of (sphere k, cell), one byte per cell
     uint16_t queue[VOX_QUEUE];                // (k << 9) | cell of the queued shell pairs
     T u[3][TILE_CELLS];                       // cell state carried across chunks
@@ -401,6 +402,19 @@ __device__ __forceinline__ void voxelize_tile(VoxSmem<T, INIT_VEL>& S, int t, co
                 const int e = k / words, wd = k - e * words;
                 reinterpret_cast<int*>(&S.q[e])[wd] = reinterpret_cast<const int*>(&fast[S.sorted[base + e]])[wd];
             }
+            if (tid < m) {   // the sphere's box within this tile and the lattice, as cell masks
+                const SphereFast& qs = fast[S.sorted[base + tid]];
+                const int o[3] = {X0, Y0, Z0}, dims[3] = {g.nx, g.ny, g.nz};
+                uint32_t bm = 0;
+#pragma unroll
+                for (int a = 0; a < 3; ++a) {
+                    const int lo = max(qs.lo[a] - o[a], 0);
+                    const int hi = min(min(qs.hi[a] - o[a], TILE - 1), dims[a] - 1 - o[a]);
+                    const uint32_t mk = lo <= hi ? ((0xffu >> (TILE - 1 - hi)) & (0xffu << lo)) & 0xffu : 0u;
+                    bm |= mk << (8 * a);
+                }
+                S.bm[tid] = bm;
+            }
         }
         if (tid == 0) S.qcount = 0;
         __syncthreads();
@@ -412,8 +426,8 @@ __device__ __forceinline__ void voxelize_tile(VoxSmem<T, INIT_VEL>& S, int t, co
                 const int l = tid + h * VOX_THREADS;
                 const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
                 uint32_t n = N_NONE;
-                if (X < g.nx && Y < g.ny && Z < g.nz && X >= q.lo[0] && X <= q.hi[0] && Y >= q.lo[1] &&
-                    Y <= q.hi[1] && Z >= q.lo[2] && Z <= q.hi[2]) {
+                const uint32_t bm = S.bm[k];
+                if ((bm >> (l >> 6)) & (bm >> (8 + ((l >> 3) & 7))) & (bm >> (16 + (l & 7))) & 1u) {
                     const float dxf = ((float)X - q.xh[0]) - q.xl[0];
                     const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
                     const float dzf = ((float)Z - q.xh[2]) - q.xl[2];
