@@ -1,5 +1,5 @@
 // A host particle integrator with the LIGGGHTS members the coupling reads and
-// writes, standing in for LIGGGHTS 3.1 (absent here) in the example drivers.
+// writes, standing in for LIGGGHTS 3.1 (absent here) in the example programs.
 //
 // Mirrors what the reference's LIGGGHTS side does per coupling cycle
 // (examples/sedimentingSphere/in.lbdem, fix_lb_coupling_onetoone.cpp:130-163):
@@ -7,7 +7,7 @@
 //   fix gravity           buoyancy-reduced gravity g (rho_s - rho_f) / rho_s,
 //   fix couple/lb/onetoone  the hydrodynamic force/torque of the last lattice
 //                         step added in every substep.
-// Single process: no ghost atoms unless the driver adds periodic images.
+// Single process: no ghost atoms unless the calling program adds periodic images.
 #ifndef LBDEM_DEM_STANDIN_H
 #define LBDEM_DEM_STANDIN_H
 

@@ -2,7 +2,7 @@
 stand-in of examples/dem_standin.h: the sedimenting-sphere case, and the
 multisphere branch of setSpheresOnLattice (examples/multisphere_check.cpp).
 
-* CPU: the driver compiles and links against the library; without a GPU it
+* CPU: the example program compiles and links against the library; without a GPU it
   exits with status 77.
 * GPU: the first 20 coupling cycles agree with the oracle driven by the same
   integrator (trace z, vz, fz within 1e-9 relative), and a longer run shows a
@@ -97,7 +97,7 @@ def test_channel_example_fused_equals_explicit(gpu):
 
 
 def oracle_trace(oracle, steps):
-    """The driver's loop on the CPU oracle: same sphere, same integrator."""
+    """The example program's loop on the CPU oracle: same sphere, same integrator."""
     nx, ny, nz, tau, radius, rho_s, g = 60, 60, 180, 0.6, 5.0, 1.5, 1e-5
     ol = oracle.OracleLattice(nx, ny, nz, 1.0 / tau, periodic=(0, 0, 0), threads=os.cpu_count() or 1)
     x = [30.5, 30.5, 150.5]
