@@ -1068,7 +1068,9 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     auto put_cells = [&](size_t base, F2 v) {
         const float2 t = upk(v);
         if (ADJ) {
-            put(base + j0, t.x, t.y, v0, v1);
+            // aligned rows: segments hold a multiple of 4 cells, so both cells of a pair
+            // are valid together, and every pair of slots is 8-byte aligned
+            if (v0) *reinterpret_cast<float2*>(F + base + j0) = t;
         } else {
             if (v0) F[base + j0] = t.x;
             if (v1) F[base + j1] = t.y;
@@ -1343,8 +1345,11 @@ cudaError_t launch_one(const CollideArgs<T>& a, cudaStream_t s) {
     const int nzseg = (a.g.nz + SEGW - 1) / SEGW;
     const long long nseg = (long long)a.g.nx * a.g.ny * nzseg;
     // Aligned bulk copies need every row start and length 16-byte aligned:
-    // population rows (nz * sizeof(T)) and voxel-word rows (nz * 4), i.e. nz % 4 == 0.
-    if (a.g.nz % 4 == 0) {
+    // population rows (nz * sizeof(T)) and voxel-word rows (nz * 4), i.e. nz % 4 == 0,
+    // and 16-byte aligned arrays (device allocations are; a caller's out-of-place
+    // target that is not takes the unaligned-row path)
+    const bool arrays_aligned = (((uintptr_t)a.f | (uintptr_t)a.fo | (uintptr_t)a.vox | (uintptr_t)a.up) & 15u) == 0;
+    if (a.g.nz % 4 == 0 && arrays_aligned) {
         if (a.g.per[0] && a.g.per[1] && a.g.per[2])
             return launch_staged<T, ODD, FORCE, true, false, false>(a, nzseg, nseg, nullptr, nullptr, 0, 0, s);
         return launch_staged<T, ODD, FORCE, false, false, false>(a, nzseg, nseg, nullptr, nullptr, 0, 0, s);
