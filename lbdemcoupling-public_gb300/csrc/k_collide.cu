@@ -711,10 +711,12 @@ struct SegGeo {
 
 __device__ __forceinline__ SegGeo seg_geo(const Geom& g, long long seg, int nzseg) {
     SegGeo s;
-    const long long row = seg / nzseg;
-    const int zs = (int)(seg - row * nzseg);
-    s.x = (int)(row / g.ny);
-    s.y = (int)(row - (long long)s.x * g.ny);
+    // 32-bit arithmetic: a lattice holds fewer than 2^31 segments (launch checks)
+    const unsigned sg = (unsigned)seg, nzs = (unsigned)nzseg, ny = (unsigned)g.ny;
+    const unsigned row = sg / nzs;
+    const int zs = (int)(sg - row * nzs);
+    s.x = (int)(row / ny);
+    s.y = (int)(row - (unsigned)s.x * ny);
     s.z0 = zs * SEGW;
     s.len = min(SEGW, g.nz - s.z0);
     s.xm = wrap_minus(s.x, g.nx, g.per[0]); s.xp = wrap_plus(s.x, g.nx, g.per[0]);
@@ -1317,6 +1319,7 @@ template <typename T, bool ODD, bool FORCE, bool PER, bool MIS, bool BATCH>
 cudaError_t launch_staged(const CollideArgs<T>& a, int nzseg, long long nseg, const CollideArgs<T>* dargs,
                           const int* seg0, int ndom, int blocks_per_sm, cudaStream_t s) {
     constexpr size_t smem = WARPS * sizeof(WarpStage<T, !BATCH>);
+    if (nseg >= (1LL << 31)) return cudaErrorInvalidValue;   // segment indices are split in 32 bits
     static int per_sm = 0, sms = 0;
     if (per_sm == 0) {
         int dev = 0;
