@@ -633,7 +633,7 @@ __device__ __forceinline__ int pick(int c, int m, int v, int p) { return c < 0 ?
 // over SEGW-cell z-segments (no block-wide barriers, so a warp with solid
 // cells does not hold up the others).
 constexpr int WARPS = COLLIDE_BLOCK / 32;    // warps per CTA
-constexpr int SEGW = 64;                    // cells per warp segment (2 per lane)
+constexpr int SEGW = COLLIDE_SEGW;          // cells per warp segment (2 per lane)
 constexpr int WAIT_LIMIT = 1 << 22;         // bounded mbarrier wait (iterations of try_wait)
 
 // 16-byte aligned, so that every warp's stage (at warp * sizeof) keeps the bulk
@@ -709,14 +709,15 @@ struct SegGeo {
     int xm, xp, ym, yp;     // neighbour rows along x and y (-1: beyond a wall)
 };
 
-__device__ __forceinline__ SegGeo seg_geo(const Geom& g, long long seg, int nzseg) {
+// dz divides by the z-segments per row, dy by ny (CollideArgs::dz, dy).
+__device__ __forceinline__ SegGeo seg_geo(const Geom& g, long long seg, const DivMagic& dz, const DivMagic& dy) {
     SegGeo s;
     // 32-bit arithmetic: a lattice holds fewer than 2^31 segments (launch checks)
-    const unsigned sg = (unsigned)seg, nzs = (unsigned)nzseg, ny = (unsigned)g.ny;
-    const unsigned row = sg / nzs;
-    const int zs = (int)(sg - row * nzs);
-    s.x = (int)(row / ny);
-    s.y = (int)(row - (unsigned)s.x * ny);
+    const unsigned sg = (unsigned)seg;
+    const unsigned row = fast_div(sg, dz);
+    const int zs = (int)(sg - row * dz.d);
+    s.x = (int)fast_div(row, dy);
+    s.y = (int)(row - (unsigned)s.x * dy.d);
     s.z0 = zs * SEGW;
     s.len = min(SEGW, g.nz - s.z0);
     s.xm = wrap_minus(s.x, g.nx, g.per[0]); s.xp = wrap_plus(s.x, g.nx, g.per[0]);
@@ -748,11 +749,11 @@ __device__ __forceinline__ long long row_off(const Geom& g, const SegGeo& s, int
 // Lanes 0..9 also publish the segment geometry for the compute pass.
 template <typename T, bool ODD, bool MIS, bool STAGE_UP>
 __device__ __forceinline__ T issue_segment(const CollideArgs<T>& a, WarpStage<T, STAGE_UP>& st, int b, long long seg,
-                                           int nzseg, int dom) {
+                                           int dom) {
     constexpr int V = WarpStage<T>::V;
     const int lane = threadIdx.x & 31;
     const Geom& g = a.g;
-    const SegGeo s = seg_geo(g, seg, nzseg);
+    const SegGeo s = seg_geo(g, seg, a.dz, a.dy);
     const size_t N = g.N;
     const long long own = ((long long)s.x * g.ny + s.y) * g.nz;
     if (lane < 9) st.row[b][lane] = row_off(g, s, lane / 3 - 1, lane % 3 - 1);
@@ -893,14 +894,14 @@ __device__ __forceinline__ size_t src_row(const long long* row, size_t N, size_t
 
 template <typename T, bool ODD, bool STAGE_UP>
 __device__ __forceinline__ void issue_segment_lsu(const CollideArgs<T>& a, WarpStage<T, STAGE_UP>& st, int b,
-                                                  long long seg, int nzseg) {
+                                                  long long seg) {
     constexpr int V = WarpStage<T>::V;   // elements per 16-byte chunk
     constexpr int CPR = SEGW / V;        // chunks per row of a segment
     constexpr int RPI = 32 / CPR;        // rows per warp pass
     static_assert(CPR * RPI == 32, "a warp pass covers whole rows");
     const int lane = threadIdx.x & 31;
     const Geom& g = a.g;
-    const SegGeo s = seg_geo(g, seg, nzseg);
+    const SegGeo s = seg_geo(g, seg, a.dz, a.dy);
     const size_t N = g.N;
     const size_t own = ((size_t)s.x * g.ny + s.y) * g.nz;
     if (lane < 9) st.row[b][lane] = row_off(g, s, lane / 3 - 1, lane % 3 - 1);
@@ -1164,7 +1165,7 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
 // the first segment of domain d); every domain has its own CollideArgs.
 template <typename T, bool ODD, bool FORCE, bool PER, bool MIS, bool BATCH>
 __global__ void __launch_bounds__(COLLIDE_BLOCK, sizeof(T) == 4 ? 4 : 2)
-k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const CollideArgs<T>* __restrict__ dargs,
+k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* __restrict__ dargs,
                  const int* __restrict__ seg0, int ndom) {
     constexpr int V = WarpStage<T>::V;
     // surface-velocity rows staged with the populations for a single lattice; the
@@ -1188,16 +1189,15 @@ k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const Coll
     if (seg >= nseg) return;
     auto issue = [&](int buf, long long sg) -> T {
         if constexpr (LSU) {
-            issue_segment_lsu<T, ODD, STAGE_UP>(a1, st, buf, sg, nzseg1);
+            issue_segment_lsu<T, ODD, STAGE_UP>(a1, st, buf, sg);
             return T(0);
         }
         if (BATCH) {
             const int d = find_domain(seg0, ndom, (int)sg);
             const CollideArgs<T>& A = dargs[d];
-            return issue_segment<T, ODD, MIS, STAGE_UP>(A, st, buf, sg - __ldg(seg0 + d), (A.g.nz + SEGW - 1) / SEGW,
-                                                        d);
+            return issue_segment<T, ODD, MIS, STAGE_UP>(A, st, buf, sg - __ldg(seg0 + d), d);
         }
-        return issue_segment<T, ODD, MIS, STAGE_UP>(a1, st, buf, sg, nzseg1, 0);
+        return issue_segment<T, ODD, MIS, STAGE_UP>(a1, st, buf, sg, 0);
     };
     T hcur = issue(0, seg);
     uint32_t phase = 0;   // bit b: parity expected next on buffer b
@@ -1316,7 +1316,7 @@ k_collide_staged(const CollideArgs<T> a1, int nzseg1, long long nseg, const Coll
 }
 
 template <typename T, bool ODD, bool FORCE, bool PER, bool MIS, bool BATCH>
-cudaError_t launch_staged(const CollideArgs<T>& a, int nzseg, long long nseg, const CollideArgs<T>* dargs,
+cudaError_t launch_staged(const CollideArgs<T>& a, long long nseg, const CollideArgs<T>* dargs,
                           const int* seg0, int ndom, int blocks_per_sm, cudaStream_t s) {
     constexpr size_t smem = WARPS * sizeof(WarpStage<T, !BATCH>);
     if (nseg >= (1LL << 31)) return cudaErrorInvalidValue;   // segment indices are split in 32 bits
@@ -1339,13 +1339,16 @@ cudaError_t launch_staged(const CollideArgs<T>& a, int nzseg, long long nseg, co
     const long long want = (long long)sms * use;
     const long long blocks = (nseg + WARPS - 1) / WARPS;
     const unsigned grid = (unsigned)(blocks < want ? blocks : want);
-    k_collide_staged<T, ODD, FORCE, PER, MIS, BATCH><<<grid, COLLIDE_BLOCK, smem, s>>>(a, nzseg, nseg, dargs, seg0, ndom);
+    k_collide_staged<T, ODD, FORCE, PER, MIS, BATCH><<<grid, COLLIDE_BLOCK, smem, s>>>(a, nseg, dargs, seg0, ndom);
     return cudaGetLastError();
 }
 
 template <typename T, bool ODD, bool FORCE>
-cudaError_t launch_one(const CollideArgs<T>& a, cudaStream_t s) {
-    const int nzseg = (a.g.nz + SEGW - 1) / SEGW;
+cudaError_t launch_one(const CollideArgs<T>& args, cudaStream_t s) {
+    const int nzseg = (args.g.nz + SEGW - 1) / SEGW;
+    CollideArgs<T> a = args;
+    a.dz = div_magic((unsigned)nzseg);
+    a.dy = div_magic((unsigned)a.g.ny);
     const long long nseg = (long long)a.g.nx * a.g.ny * nzseg;
     // Aligned bulk copies need every row start and length 16-byte aligned:
     // population rows (nz * sizeof(T)) and voxel-word rows (nz * 4), i.e. nz % 4 == 0,
@@ -1354,17 +1357,17 @@ cudaError_t launch_one(const CollideArgs<T>& a, cudaStream_t s) {
     const bool arrays_aligned = (((uintptr_t)a.f | (uintptr_t)a.fo | (uintptr_t)a.vox | (uintptr_t)a.up) & 15u) == 0;
     if (a.g.nz % 4 == 0 && arrays_aligned) {
         if (a.g.per[0] && a.g.per[1] && a.g.per[2])
-            return launch_staged<T, ODD, FORCE, true, false, false>(a, nzseg, nseg, nullptr, nullptr, 0, 0, s);
-        return launch_staged<T, ODD, FORCE, false, false, false>(a, nzseg, nseg, nullptr, nullptr, 0, 0, s);
+            return launch_staged<T, ODD, FORCE, true, false, false>(a, nseg, nullptr, nullptr, 0, 0, s);
+        return launch_staged<T, ODD, FORCE, false, false, false>(a, nseg, nullptr, nullptr, 0, 0, s);
     }
-    return launch_staged<T, ODD, FORCE, false, true, false>(a, nzseg, nseg, nullptr, nullptr, 0, 0, s);
+    return launch_staged<T, ODD, FORCE, false, true, false>(a, nseg, nullptr, nullptr, 0, 0, s);
 }
 
 template <typename T, bool ODD, bool FORCE>
 cudaError_t launch_batch(const CollideArgs<T>* dargs, const int* seg0, int ndom, long long nseg, int blocks_per_sm,
                          cudaStream_t s) {
     CollideArgs<T> none{};
-    return launch_staged<T, ODD, FORCE, false, true, true>(none, 1, nseg, dargs, seg0, ndom, blocks_per_sm, s);
+    return launch_staged<T, ODD, FORCE, false, true, true>(none, nseg, dargs, seg0, ndom, blocks_per_sm, s);
 }
 
 }  // namespace

@@ -210,6 +210,8 @@ void fill_dargs(lbdem_batch* b, std::vector<CollideArgs<T>>& out, T* f_base, dou
         a.btab = (const T*)b->btab + (size_t)126 * d;
         a.omega = (T)b->dom[d].omega;
         for (int k = 0; k < 3; ++k) a.g3[k] = (T)b->dom[d].body_force[k];
+        a.dz = div_magic((unsigned)((v.g.nz + COLLIDE_SEGW - 1) / COLLIDE_SEGW));
+        a.dy = div_magic((unsigned)v.g.ny);
     }
 }
 
@@ -452,7 +454,7 @@ lbdem_status lbdem_batch_create(const lbdem_batch_config* cfg, int32_t ndomains,
         b->cap[d] = dm.max_particles;
         slots += dm.max_particles;
         tiles += (long long)((dm.nx + TILE - 1) / TILE) * ((dm.ny + TILE - 1) / TILE) * ((dm.nz + TILE - 1) / TILE);
-        segs += (long long)dm.nx * dm.ny * ((dm.nz + 63) / 64);
+        segs += (long long)dm.nx * dm.ny * ((dm.nz + COLLIDE_SEGW - 1) / COLLIDE_SEGW);
         fo += round_up((size_t)Q * v.g.N, 32);
         co += round_up(v.g.N, 32);
         uo += round_up(3 * v.g.N, 32);

@@ -20,6 +20,7 @@ constexpr int VOX_NBITS = 7;            // voxel word: sub-cell count n (7 bits)
 constexpr uint32_t VOX_NMASK = (1u << VOX_NBITS) - 1u;
 constexpr int32_t MAX_TAG_LIMIT = (1 << 25) - 1;
 constexpr int COLLIDE_BLOCK = 128;      // threads per block along z in the collide-stream kernel
+constexpr int COLLIDE_SEGW = 64;        // cells per z-segment of the collide-stream kernel
 
 // Lattice velocities, Palabos D3Q19 order.  Each component is stored as
 // c + 1 in two bits per direction of a 64-bit constant, so that a lookup with a
@@ -80,6 +81,29 @@ __device__ __forceinline__ size_t slot_index(int i, int x, int y, int z, int pha
 }
 
 // Arguments of one collide-stream launch.
+// Division by an invariant divisor d >= 1 as a multiply-high and a shift, exact
+// for numerators below 2^31: with l = ceil(log2 d), s = l - 1 and
+// m = ceil(2^(32+s) / d) (< 2^32), n / d = umulhi(n, m) >> s, because
+// n m / 2^(31+l) - n / d < n / 2^(31+l) < 2^-l <= 1 / d  (Granlund and
+// Montgomery, "Division by invariant integers using multiplication", 1994).
+struct DivMagic {
+    unsigned m;
+    int s;
+    unsigned d;
+};
+inline DivMagic div_magic(unsigned d) {
+    DivMagic r{0u, 0, d};
+    if (d <= 1) return r;
+    int l = 0;
+    while ((1ull << l) < d) ++l;
+    r.s = l - 1;
+    r.m = (unsigned)(((1ull << (32 + r.s)) + d - 1) / d);
+    return r;
+}
+__device__ __forceinline__ unsigned fast_div(unsigned n, const DivMagic& q) {
+    return q.d <= 1 ? n : (__umulhi(n, q.m) >> q.s);
+}
+
 template <typename T>
 struct CollideArgs {
     Geom g;
@@ -99,6 +123,7 @@ struct CollideArgs {
     const T* btab;           // [126] B(n) = sf ooo / ((1 - sf) + ooo), evaluated in double
     T omega;                 // BGK relaxation frequency
     T g3[3];                 // Guo body-force acceleration
+    DivMagic dz, dy;         // division by the z-segments per row and by ny (set by the launchers)
 };
 
 // Exact (double) description of one sphere of the list, for the decisions

@@ -91,3 +91,26 @@ def test_no_device_is_an_error_not_a_fallback(lbdem_lib):
     with pytest.raises(lbdem_lib.LbdemError) as ei:
         lbdem_lib.Lattice(8, 8, 8, 1.0)
     assert ei.value.status == 6
+
+
+def test_division_by_invariant_divisor():
+    """The multiply-high division the collide kernel uses to split a segment index
+    (DivMagic in csrc/lbdem_internal.h): for d >= 2, s = ceil(log2 d) - 1,
+    m = ceil(2^(32+s) / d) fits in 32 bits and (n * m) >> (32 + s) == n // d for
+    every n < 2^31; checked here at the multiples of d and their neighbours."""
+    import numpy as np
+    rng = np.random.default_rng(3)
+    divisors = list(range(2, 600)) + [1023, 1024, 1025, 4095, 4096, 65535, 65536, 65537, 2**20 + 7, 2**30, 2**31 - 1]
+    for d in divisors:
+        l = 0
+        while (1 << l) < d:
+            l += 1
+        s = l - 1
+        m = ((1 << (32 + s)) + d - 1) // d
+        assert m < 2**32
+        ks = np.unique(np.concatenate([np.arange(0, 50), rng.integers(0, (2**31 - 1) // d + 1, 200),
+                                       [(2**31 - 1) // d]]))
+        for k in ks:
+            for n in (int(k) * d - 1, int(k) * d, int(k) * d + 1, int(k) * d + d - 1):
+                if 0 <= n < 2**31:
+                    assert ((n * m) >> 32) >> s == n // d, (d, n)
