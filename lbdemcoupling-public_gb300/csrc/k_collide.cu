@@ -882,17 +882,19 @@ __device__ __forceinline__ void unroll_seq(std::integer_sequence<int, Ts...>, Fn
 
 // Element offset of the source row of direction I (even: slot I of the own row;
 // odd: slot opp I of row x - c_I, or slot I of the own row beyond a wall).
-template <bool ODD, int I>
+// PER: every axis periodic, the row x - c_I always exists.
+template <bool ODD, bool PER, int I>
 __device__ __forceinline__ size_t src_row(const long long* row, size_t N, size_t own) {
     if constexpr (!ODD || I == 0) {
         return (size_t)I * N + own;
     } else {
         const long long r = row[row_slot(-cx(I), -cy(I))];
-        return r >= 0 ? (size_t)opp(I) * N + (size_t)r : (size_t)I * N + own;
+        if constexpr (PER) return (size_t)opp(I) * N + (size_t)r;
+        else return r >= 0 ? (size_t)opp(I) * N + (size_t)r : (size_t)I * N + own;
     }
 }
 
-template <typename T, bool ODD, bool STAGE_UP>
+template <typename T, bool ODD, bool PER, bool STAGE_UP>
 __device__ __forceinline__ void issue_segment_lsu(const CollideArgs<T>& a, WarpStage<T, STAGE_UP>& st, int b,
                                                   long long seg) {
     constexpr int V = WarpStage<T>::V;   // elements per 16-byte chunk
@@ -918,9 +920,9 @@ __device__ __forceinline__ void issue_segment_lsu(const CollideArgs<T>& a, WarpS
         constexpr int t = decltype(tc)::value;
         constexpr int i0 = t * RPI, i1 = t * RPI + 1;
         if constexpr (RPI == 1 || i1 >= Q) {
-            if (sub == 0 && cin) cp16(&st.f[b][i0][V + c * V], f + src_row<ODD, i0>(row, N, own) + s.z0 + c * V);
+            if (sub == 0 && cin) cp16(&st.f[b][i0][V + c * V], f + src_row<ODD, PER, i0>(row, N, own) + s.z0 + c * V);
         } else {
-            const size_t off = sub == 0 ? src_row<ODD, i0>(row, N, own) : src_row<ODD, i1>(row, N, own);
+            const size_t off = sub == 0 ? src_row<ODD, PER, i0>(row, N, own) : src_row<ODD, PER, i1>(row, N, own);
             if (cin) cp16(&st.f[b][sub == 0 ? i0 : i1][V + c * V], f + off + s.z0 + c * V);
         }
     });
@@ -932,16 +934,16 @@ __device__ __forceinline__ void issue_segment_lsu(const CollideArgs<T>& a, WarpS
         if (k < NH) {
             const int i = zdir(k);
             const long long r = row[row_slot(-cx(i), -cy(i))];
-            if (r < 0) continue;
+            if (!PER && r < 0) continue;
             int zc;     // first element of the chunk holding the halo (-1: beyond a z wall)
             T* dst;
             if (cz(i) > 0) {
                 zc = s.z0 - V;
-                if (zc < 0) zc = g.per[2] ? zc + g.nz : -1;
+                if (zc < 0) zc = (PER || g.per[2]) ? zc + g.nz : -1;
                 dst = &st.f[b][i][0];
             } else {
                 zc = s.z0 + s.len;
-                if (zc >= g.nz) zc = g.per[2] ? zc - g.nz : -1;
+                if (zc >= g.nz) zc = (PER || g.per[2]) ? zc - g.nz : -1;
                 dst = &st.f[b][i][V + s.len];
             }
             if (zc >= 0) cp16(dst, f + (size_t)opp(i) * N + (size_t)r + zc);
@@ -1189,7 +1191,7 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
     if (seg >= nseg) return;
     auto issue = [&](int buf, long long sg) -> T {
         if constexpr (LSU) {
-            issue_segment_lsu<T, ODD, STAGE_UP>(a1, st, buf, sg);
+            issue_segment_lsu<T, ODD, PER, STAGE_UP>(a1, st, buf, sg);
             return T(0);
         }
         if (BATCH) {
