@@ -709,7 +709,9 @@ struct SegGeo {
     int xm, xp, ym, yp;     // neighbour rows along x and y (-1: beyond a wall)
 };
 
-// dz divides by the z-segments per row, dy by ny (CollideArgs::dz, dy).
+// dz divides by the z-segments per row, dy by ny (CollideArgs::dz, dy).  PER: all
+// axes periodic (known at compile time).
+template <bool PER = false>
 __device__ __forceinline__ SegGeo seg_geo(const Geom& g, long long seg, const DivMagic& dz, const DivMagic& dy) {
     SegGeo s;
     // 32-bit arithmetic: a lattice holds fewer than 2^31 segments (launch checks)
@@ -720,15 +722,16 @@ __device__ __forceinline__ SegGeo seg_geo(const Geom& g, long long seg, const Di
     s.y = (int)(row - (unsigned)s.x * dy.d);
     s.z0 = zs * SEGW;
     s.len = min(SEGW, g.nz - s.z0);
-    s.xm = wrap_minus(s.x, g.nx, g.per[0]); s.xp = wrap_plus(s.x, g.nx, g.per[0]);
-    s.ym = wrap_minus(s.y, g.ny, g.per[1]); s.yp = wrap_plus(s.y, g.ny, g.per[1]);
+    s.xm = wrap_minus(s.x, g.nx, PER ? 1 : g.per[0]); s.xp = wrap_plus(s.x, g.nx, PER ? 1 : g.per[0]);
+    s.ym = wrap_minus(s.y, g.ny, PER ? 1 : g.per[1]); s.yp = wrap_plus(s.y, g.ny, PER ? 1 : g.per[1]);
     return s;
 }
 
 // Row (x + dx, y + dy) as an element offset, or -1 beyond a wall.
+template <bool PER = false>
 __device__ __forceinline__ long long row_off(const Geom& g, const SegGeo& s, int dx, int dy) {
     const int X = pick(dx, s.xm, s.x, s.xp), Y = pick(dy, s.ym, s.y, s.yp);
-    if (X < 0 || Y < 0) return -1;
+    if (!PER && (X < 0 || Y < 0)) return -1;
     return ((long long)X * g.ny + Y) * g.nz;
 }
 
@@ -903,10 +906,10 @@ __device__ __forceinline__ void issue_segment_lsu(const CollideArgs<T>& a, WarpS
     static_assert(CPR * RPI == 32, "a warp pass covers whole rows");
     const int lane = threadIdx.x & 31;
     const Geom& g = a.g;
-    const SegGeo s = seg_geo(g, seg, a.dz, a.dy);
+    const SegGeo s = seg_geo<PER>(g, seg, a.dz, a.dy);
     const size_t N = g.N;
     const size_t own = ((size_t)s.x * g.ny + s.y) * g.nz;
-    if (lane < 9) st.row[b][lane] = row_off(g, s, lane / 3 - 1, lane % 3 - 1);
+    if (lane < 9) st.row[b][lane] = row_off<PER>(g, s, lane / 3 - 1, lane % 3 - 1);
     if (lane == 9) {
         st.geo[b][0] = s.x; st.geo[b][1] = s.y; st.geo[b][2] = s.z0; st.geo[b][3] = s.len; st.geo[b][4] = 0;
     }
