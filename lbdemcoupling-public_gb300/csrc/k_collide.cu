@@ -929,11 +929,15 @@ __device__ __forceinline__ void issue_segment_lsu(const CollideArgs<T>& a, WarpS
             if (cin) cp16(&st.f[b][sub == 0 ? i0 : i1][V + c * V], f + off + s.z0 + c * V);
         }
     });
-    // then: halo chunks (odd phase, 10), voxel row (SEGW / 4 chunks), surface-velocity rows (3 CPR)
+    // then: voxel row (SEGW / 4 chunks), surface-velocity rows (3 CPR), halo chunks
+    // (odd phase, 10) -- in that order, so that only the first pass mixes two kinds
     constexpr int NH = ODD ? 10 : 0, NV = SEGW / 4, NU = STAGE_UP ? 3 * CPR : 0;
     constexpr int NX = NH + NV + NU;
 #pragma unroll
-    for (int k = lane; k < ((NX + 31) / 32) * 32; k += 32) {
+    for (int kk = lane; kk < ((NX + 31) / 32) * 32; kk += 32) {
+        // item order voxel, velocity, halo, mapped onto the halo-first numbering below
+        const int k = kk < NV + NU ? kk + NH : kk - (NV + NU);
+        if (kk >= NX) continue;
         if (k < NH) {
             const int i = zdir(k);
             const long long r = row[row_slot(-cx(i), -cy(i))];
@@ -1065,7 +1069,9 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     // Stores.  put(off, x, y, vx, vy): values x, y into slots off, off + 1 (ADJ:
     // one 64-bit store when both are valid and the pair is aligned).
     auto put = [&](size_t off, float x, float y, bool vx, bool vy) {
-        if (vx && vy && ((uintptr_t)(F + off) & 7u) == 0) {
+        // aligned rows only (the launcher sends arrays that are not 16-byte aligned
+        // to the unaligned-row path): an even slot offset is an 8-byte aligned pair
+        if (vx && vy) {
             *reinterpret_cast<float2*>(F + off) = make_float2(x, y);
         } else {
             if (vx) F[off] = x;
