@@ -17,12 +17,16 @@
 //
 // One kernel implements the step: persistent CTAs of 128 threads whose warps
 // walk 64-cell z-segments.  The 19 population rows of a segment (plus, in the
-// odd phase, the halo element of every c_z != 0 direction) and the voxel words
-// are copied into shared memory with cp.async.bulk on an mbarrier,
-// double-buffered, so the next segment's bytes are in flight while the current
-// one is collided.  The staged pre-collision values double as fPre of the PSM
-// update.  Rows that are not 16-byte aligned (nz % 4 != 0) are copied in whole
-// 16-byte chunks around the row.  The same kernel steps many independent
+// odd phase, the halo element of every c_z != 0 direction), the voxel words and
+// (single lattice) the particle surface-velocity rows are staged in shared
+// memory, double-buffered, so the next segment's bytes are in flight while the
+// current one is collided: per-thread 16-byte cp.async with commit groups for
+// FP32 lattices with 16-byte aligned rows, cp.async.bulk on an mbarrier
+// otherwise; rows that are not 16-byte aligned (nz % 4 != 0) are copied in whole
+// 16-byte chunks around the row.  The staged pre-collision values double as
+// fPre of the PSM update.  The FP32 form collides two cells per thread in packed
+// f32x2 arithmetic (collide_segment_pairs); the FP64 form one cell per thread in
+// the reference's double sequence.  The same kernel steps many independent
 // domains in one launch (batch mode).
 #include "lbdem_internal.h"
 
