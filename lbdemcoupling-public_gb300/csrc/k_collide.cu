@@ -929,7 +929,15 @@ __device__ __forceinline__ void issue_segment_lsu(const CollideArgs<T>& a, WarpS
         if constexpr (RPI == 1 || i1 >= Q) {
             if (sub == 0 && cin) cp16(&st.f[b][i0][V + c * V], f + src_row<ODD, PER, i0>(row, N, own) + s.z0 + c * V);
         } else {
-            const size_t off = sub == 0 ? src_row<ODD, PER, i0>(row, N, own) : src_row<ODD, PER, i1>(row, N, own);
+            size_t off;
+            if constexpr (ODD && PER && i0 != 0) {
+                // one row lookup per pass: the lane's direction picks slot and array
+                constexpr int s0 = row_slot(-cx(i0), -cy(i0)), s1 = row_slot(-cx(i1), -cy(i1));
+                const long long r = row[sub == 0 ? s0 : s1];
+                off = (size_t)(sub == 0 ? opp(i0) : opp(i1)) * N + (size_t)r;
+            } else {
+                off = sub == 0 ? src_row<ODD, PER, i0>(row, N, own) : src_row<ODD, PER, i1>(row, N, own);
+            }
             if (cin) cp16(&st.f[b][sub == 0 ? i0 : i1][V + c * V], f + off + s.z0 + c * V);
         }
     });
