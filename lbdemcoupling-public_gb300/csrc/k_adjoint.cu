@@ -443,15 +443,20 @@ __global__ void k_loss_step(const double* __restrict__ ft, const double* __restr
 
 template <typename T>
 cudaError_t launch_adjoint_step(const AdjointArgs<T>& a, cudaStream_t s) {
-    static int blocks = 0;
+    static std::atomic<int> cached[LBDEM_MAX_DEVICES];   // per device: grid size
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= LBDEM_MAX_DEVICES) return cudaErrorInvalidDevice;
+    int blocks = cached[dev].load(std::memory_order_relaxed);
     if (blocks == 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int sms = 0, per_sm = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
             e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adjoint_step<T>, ADJ_THREADS, 0);
         if (e != cudaSuccess) return e;
         blocks = sms * (per_sm > 0 ? per_sm : 1);
+        cached[dev].store(blocks, std::memory_order_relaxed);
     }
     const size_t need = (a.g.N + ADJ_THREADS - 1) / ADJ_THREADS;
     const unsigned grid = (unsigned)(need < (size_t)blocks ? (need > 0 ? need : 1) : (size_t)blocks);

@@ -1343,11 +1343,16 @@ cudaError_t launch_staged(const CollideArgs<T>& a, long long nseg, const Collide
                           const int* seg0, int ndom, int blocks_per_sm, cudaStream_t s) {
     constexpr size_t smem = WARPS * sizeof(WarpStage<T, !BATCH>);
     if (nseg >= (1LL << 31)) return cudaErrorInvalidValue;   // segment indices are split in 32 bits
-    static int per_sm = 0, sms = 0;
-    if (per_sm == 0) {
-        int dev = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    // per device: (resident blocks per SM << 16) | SM count, 0 until first use there
+    static std::atomic<int> shape[LBDEM_MAX_DEVICES];
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= LBDEM_MAX_DEVICES) return cudaErrorInvalidDevice;
+    int packed = shape[dev].load(std::memory_order_relaxed);
+    if (packed == 0) {
+        int sms = 0, per_sm = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_collide_staged<T, ODD, FORCE, PER, MIS, BATCH>,
                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1356,7 +1361,10 @@ cudaError_t launch_staged(const CollideArgs<T>& a, long long nseg, const Collide
                                                               COLLIDE_BLOCK, smem);
         if (e != cudaSuccess) return e;
         if (per_sm < 1) per_sm = 1;
+        packed = (per_sm << 16) | (sms & 0xffff);
+        shape[dev].store(packed, std::memory_order_relaxed);
     }
+    const int per_sm = packed >> 16, sms = packed & 0xffff;
     if (nseg <= 0) return cudaSuccess;
     const int use = (blocks_per_sm > 0 && blocks_per_sm < per_sm) ? blocks_per_sm : per_sm;
     const long long want = (long long)sms * use;

@@ -634,11 +634,15 @@ cudaError_t launch_vox(const SphereDev* sph, const SphereFast* fast, int n, int*
                        unsigned* err, const DomView* doms, const int* toff, int ndom, const int* ncur,
                        cudaStream_t s) {
     constexpr size_t smem = sizeof(VoxSmem<T, INIT_VEL>);
-    static int blocks = 0;
+    static std::atomic<int> cached[LBDEM_MAX_DEVICES];   // per device: persistent grid size
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return e;
+    if (dev < 0 || dev >= LBDEM_MAX_DEVICES) return cudaErrorInvalidDevice;
+    int blocks = cached[dev].load(std::memory_order_relaxed);
     if (blocks == 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaError_t e = cudaGetDevice(&dev);
-        if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        int sms = 0, per_sm = 0;
+        e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(k_voxelize<T, INIT_VEL, BATCH>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)smem);
@@ -647,6 +651,7 @@ cudaError_t launch_vox(const SphereDev* sph, const SphereFast* fast, int n, int*
                                                               smem);
         if (e != cudaSuccess) return e;
         blocks = sms * (per_sm > 0 ? per_sm : 1);
+        cached[dev].store(blocks, std::memory_order_relaxed);
     }
     const int grid = ntiles < blocks ? ntiles : blocks;
     k_voxelize<T, INIT_VEL, BATCH><<<grid, VOX_THREADS, smem, s>>>(sph, fast, n, tile_cnt, bins, work, work_n, vox, up,

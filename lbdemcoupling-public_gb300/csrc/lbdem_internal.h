@@ -5,6 +5,7 @@
 #pragma once
 
 #include <cstddef>
+#include <atomic>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -81,6 +82,10 @@ __device__ __forceinline__ size_t slot_index(int i, int x, int y, int z, int pha
 }
 
 // Arguments of one collide-stream launch.
+// Launch shapes cached per device (the SM count, the resident blocks of a kernel
+// and its dynamic shared-memory opt-in are properties of one device).
+constexpr int LBDEM_MAX_DEVICES = 64;
+
 // Division by an invariant divisor d >= 1 as a multiply-high and a shift, exact
 // for numerators below 2^31: with l = ceil(log2 d), s = l - 1 and
 // m = ceil(2^(32+s) / d) (< 2^32), n / d = umulhi(n, m) >> s, because
