@@ -148,6 +148,7 @@ lbdem_status lbdem_collide_and_stream(lbdem_handle* h);
  * [n][3] doubles indexed like the particle list: the entry of the first list
  * index carrying a tag holds that tag's sum, ghost-image entries are zero
  * (the reference's force/torque vectors, src/ibDataExchangeWrappers3D.hh:194-218).
+ * Zero between an lbdem_set_particles and the step that follows it.
  * Synchronizes; returns LBDEM_ERR_DEVICE if the device error word is set. */
 lbdem_status lbdem_get_forces(lbdem_handle* h, int32_t n, double* force, double* torque);
 

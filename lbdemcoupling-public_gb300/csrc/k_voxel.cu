@@ -61,14 +61,20 @@ __device__ __forceinline__ int tiles_along(int n) { return (n + TILE - 1) / TILE
 // owned atom, which precedes its ghost images).
 // BATCH: slot i belongs to the domain d with soff[d] <= i; slots past the
 // domain's particle count are skipped; the map stores domain-local slots.
+// ft_zero (may be null): the 6 n force/torque sums of the coming collide-stream
+// step, zeroed here instead of by a separate memset launch.
 template <bool BATCH>
 __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereDev* __restrict__ sph,
                                   SphereFast* __restrict__ fast, float* __restrict__ xpf,
                                   int* __restrict__ tag2slot, unsigned* __restrict__ err, Geom g, int max_tag,
                                   double max_radius, const DomView* __restrict__ doms, const int* __restrict__ soff,
-                                  int ndom, const int* __restrict__ ncur) {
+                                  int ndom, const int* __restrict__ ncur, double* __restrict__ ft_zero) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
+    if (ft_zero) {
+#pragma unroll
+        for (int k = 0; k < 6; ++k) ft_zero[(size_t)k * n + i] = 0.0;
+    }
     int il = i;
     if (BATCH) {
         const int d = find_domain(soff, ndom, i);
@@ -592,20 +598,20 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
 
 cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
                                    int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
-                                   cudaStream_t s) {
+                                   double* ft_zero, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     k_prepare_spheres<false><<<(n + 127) / 128, 128, 0, s>>>(rec, n, sph, fast, xpf, tag2slot, err, g, max_tag,
-                                                            max_radius, nullptr, nullptr, 0, nullptr);
+                                                            max_radius, nullptr, nullptr, 0, nullptr, ft_zero);
     return cudaGetLastError();
 }
 
 cudaError_t launch_prepare_spheres_batch(const double* rec, int nslots, SphereDev* sph, SphereFast* fast, float* xpf,
                                          int* tag2slot, unsigned* err, int max_tag, double max_radius,
                                          const DomView* doms, const int* soff, int ndom, const int* ncur,
-                                         cudaStream_t s) {
+                                         double* ft_zero, cudaStream_t s) {
     if (nslots <= 0) return cudaSuccess;
     k_prepare_spheres<true><<<(nslots + 127) / 128, 128, 0, s>>>(rec, nslots, sph, fast, xpf, tag2slot, err, Geom{},
-                                                                max_tag, max_radius, doms, soff, ndom, ncur);
+                                                                max_tag, max_radius, doms, soff, ndom, ncur, ft_zero);
     return cudaGetLastError();
 }
 

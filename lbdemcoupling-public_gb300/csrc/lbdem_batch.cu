@@ -252,7 +252,7 @@ cudaError_t enqueue_step(lbdem_batch* b, bool odd, int init_vel) {
         return e;
     if ((e = launch_prepare_spheres_batch(b->d_rec, b->nslots, b->d_sph, b->d_fast, b->d_xpf, b->d_tag2slot, b->d_err,
                                           b->cfg.max_tag, b->cfg.max_radius, b->d_views, b->d_soff, b->ndom,
-                                          b->d_ncur, s)) != cudaSuccess)
+                                          b->d_ncur, b->d_ft, s)) != cudaSuccess)   // also zeroes the sums
         return e;
     if ((e = launch_bin_spheres_batch(b->d_fast, b->nslots, b->d_tile_cnt, b->d_bins, b->d_work, b->d_work_n,
                                       b->d_views, b->d_soff, b->ndom, b->d_ncur, s)) != cudaSuccess)
@@ -266,7 +266,6 @@ cudaError_t enqueue_step(lbdem_batch* b, bool odd, int init_vel) {
                                          b->ntiles, b->vox, (float*)b->up, (float*)b->f, init_vel, P, b->d_views,
                                          b->d_toff, b->ndom, b->d_ncur, b->d_err, s);
     if (e != cudaSuccess) return e;
-    if ((e = cudaMemsetAsync(b->d_ft, 0, sizeof(double) * 6 * (size_t)b->nslots, s)) != cudaSuccess) return e;
     if (b->njobs > 0 && !b->pavg_valid) {
         if ((e = launch_planes(b, P, 0, nullptr, b->d_pavg + (size_t)b->njobs * P)) != cudaSuccess) return e;
     }

@@ -61,6 +61,7 @@ struct lbdem_handle {
     double* h_pavg = nullptr;   // pinned
     bool pdrop_on = false;
     bool pavg_valid = false;
+    bool ft_dirty = false;      // d_ft holds sums of a step (zeroed by the next voxelization)
     int pdrop_bpj = 1;
 
     void* scratch = nullptr;
@@ -157,7 +158,8 @@ lbdem_status voxelize(lbdem_handle* h, int n, int init_vel) {
     CK(h, cudaMemsetAsync(h->d_tag2slot, 0x7F, sizeof(int) * ((size_t)h->cfg.max_tag + 1), s));
     if (n > 0) {
         CK(h, launch_prepare_spheres(h->d_rec, n, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot, h->d_err, h->g,
-                                     h->cfg.max_tag, h->cfg.max_radius, s));
+                                     h->cfg.max_tag, h->cfg.max_radius, h->d_ft, s));
+        h->ft_dirty = false;   // the prepare launch zeroed the 6 n sums
         CK(h, launch_bin_spheres(h->d_fast, n, h->d_tile_cnt, h->d_bins, h->d_work, h->d_work_n, h->g, s));
         const int phase = (int)(h->step & 1);
         if (h->prec == LBDEM_PREC_FP64)
@@ -209,6 +211,7 @@ PlaneJob make_job(const lbdem_handle* h, const int32_t* box, int dim, int dir, d
 // array of the same layout).  Particle state, force sums and the step parity
 // are the handle's.
 cudaError_t k1_launch(lbdem_handle* h, void* fin, void* fout) {
+    h->ft_dirty = true;
     const bool odd = (h->step & 1) != 0;
     const bool force = h->cfg.body_force[0] != 0.0 || h->cfg.body_force[1] != 0.0 || h->cfg.body_force[2] != 0.0;
     const int n = h->n_cur;
@@ -496,7 +499,9 @@ lbdem_status lbdem_collide_and_stream(lbdem_handle* h) {
     if (!h) return LBDEM_ERR_INVALID_ARG;
     DeviceGuard dg(h->device);
     const int n = h->n_cur;
-    if (n > 0) CK(h, cudaMemsetAsync(h->d_ft, 0, 6 * (size_t)n * sizeof(double), h->stream));
+    // the sums start from zero: the voxelization of this list zeroed them unless
+    // a step has run since
+    if (n > 0 && h->ft_dirty) CK(h, cudaMemsetAsync(h->d_ft, 0, 6 * (size_t)n * sizeof(double), h->stream));
     const int P = (int)(h->step & 1);
     if (h->pdrop_on && !h->pavg_valid) {
         // averages of the state before the step (computeAverageDensity before collideAndStream)

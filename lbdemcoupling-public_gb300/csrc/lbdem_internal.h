@@ -190,9 +190,11 @@ template <typename T>
 cudaError_t launch_collide_batch(const CollideArgs<T>* dargs, const int* seg0, int ndom, long long nseg, bool odd,
                                  bool force, int blocks_per_sm, cudaStream_t s);
 
+// ft_zero (may be null): 6 n doubles set to zero by the same launch (the force
+// and torque sums of the next collide-stream step).
 cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
                                    int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
-                                   cudaStream_t s);
+                                   double* ft_zero, cudaStream_t s);
 // tile_cnt must be zero on entry; launch_voxelize leaves it zero again.  Every
 // tile that receives a sphere is appended to work[] (work_n counts them; zero
 // on entry, left zero by launch_voxelize).
@@ -210,7 +212,7 @@ cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, int n,
 cudaError_t launch_prepare_spheres_batch(const double* rec, int nslots, SphereDev* sph, SphereFast* fast, float* xpf,
                                          int* tag2slot, unsigned* err, int max_tag, double max_radius,
                                          const DomView* doms, const int* soff, int ndom, const int* ncur,
-                                         cudaStream_t s);
+                                         double* ft_zero, cudaStream_t s);
 cudaError_t launch_bin_spheres_batch(const SphereFast* fast, int nslots, int* tile_cnt, int* bins, int* work,
                                      int* work_n, const DomView* doms, const int* soff, int ndom, const int* ncur,
                                      cudaStream_t s);
