@@ -132,7 +132,9 @@ lbdem_status lbdem_set_particles(lbdem_handle* h, int32_t n, const double* x, co
                                  int32_t init_vel);
 
 /* Same, with the particle table already in device memory: rec is [n][12]
- * doubles {x0,x1,x2, v0,v1,v2, w0,w1,w2, r, tag, 0} (tag stored as a double). */
+ * doubles {x0,x1,x2, v0,v1,v2, w0,w1,w2, r, tag, 0} (tag stored as a double).
+ * The handle keeps its own copy, taken on its stream: rec may be reused once
+ * the work queued so far on that stream has run. */
 lbdem_status lbdem_set_particles_device(lbdem_handle* h, int32_t n, const double* rec,
                                         int32_t init_vel);
 

@@ -62,13 +62,15 @@ __device__ __forceinline__ int tiles_along(int n) { return (n + TILE - 1) / TILE
 // BATCH: slot i belongs to the domain d with soff[d] <= i; slots past the
 // domain's particle count are skipped; the map stores domain-local slots.
 // ft_zero (may be null): the 6 n force/torque sums of the coming collide-stream
-// step, zeroed here instead of by a separate memset launch.
+// step, zeroed here instead of by a separate memset launch.  rec_copy (may be
+// null, never overlapping rec): receives a copy of the n records.
 template <bool BATCH>
 __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereDev* __restrict__ sph,
                                   SphereFast* __restrict__ fast, float* __restrict__ xpf,
                                   int* __restrict__ tag2slot, unsigned* __restrict__ err, Geom g, int max_tag,
                                   double max_radius, const DomView* __restrict__ doms, const int* __restrict__ soff,
-                                  int ndom, const int* __restrict__ ncur, double* __restrict__ ft_zero) {
+                                  int ndom, const int* __restrict__ ncur, double* __restrict__ ft_zero,
+                                  double* __restrict__ rec_copy) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= n) return;
     if (ft_zero) {
@@ -84,6 +86,10 @@ __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereD
         tag2slot += doms[d].tag0;
     }
     const double* p = rec + (size_t)i * REC_STRIDE;
+    if (rec_copy) {
+#pragma unroll
+        for (int k = 0; k < REC_STRIDE; ++k) rec_copy[(size_t)i * REC_STRIDE + k] = p[k];
+    }
     SphereDev s;
     SphereFast q;
     for (int d = 0; d < 3; ++d) { s.x[d] = p[d]; s.v[d] = p[3 + d]; s.w[d] = p[6 + d]; }
@@ -598,10 +604,11 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
 
 cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
                                    int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
-                                   double* ft_zero, cudaStream_t s) {
+                                   double* ft_zero, double* rec_copy, cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
     k_prepare_spheres<false><<<(n + 127) / 128, 128, 0, s>>>(rec, n, sph, fast, xpf, tag2slot, err, g, max_tag,
-                                                            max_radius, nullptr, nullptr, 0, nullptr, ft_zero);
+                                                            max_radius, nullptr, nullptr, 0, nullptr, ft_zero,
+                                                            rec_copy);
     return cudaGetLastError();
 }
 
@@ -611,7 +618,8 @@ cudaError_t launch_prepare_spheres_batch(const double* rec, int nslots, SphereDe
                                          double* ft_zero, cudaStream_t s) {
     if (nslots <= 0) return cudaSuccess;
     k_prepare_spheres<true><<<(nslots + 127) / 128, 128, 0, s>>>(rec, nslots, sph, fast, xpf, tag2slot, err, Geom{},
-                                                                max_tag, max_radius, doms, soff, ndom, ncur, ft_zero);
+                                                                max_tag, max_radius, doms, soff, ndom, ncur, ft_zero,
+                                                                nullptr);
     return cudaGetLastError();
 }
 

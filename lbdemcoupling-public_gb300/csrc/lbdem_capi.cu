@@ -152,13 +152,15 @@ lbdem_status wait_staging(lbdem_handle* h) {
     return LBDEM_OK;
 }
 
-// Voxelization of the particle table already in h->d_rec (n records).
-lbdem_status voxelize(lbdem_handle* h, int n, int init_vel) {
+// Voxelization of n records read from src (h->d_rec, or a device table of the
+// caller that the prepare launch copies into h->d_rec as it reads it).
+lbdem_status voxelize(lbdem_handle* h, int n, int init_vel, const double* src) {
     cudaStream_t s = h->stream;
     CK(h, cudaMemsetAsync(h->d_tag2slot, 0x7F, sizeof(int) * ((size_t)h->cfg.max_tag + 1), s));
     if (n > 0) {
-        CK(h, launch_prepare_spheres(h->d_rec, n, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot, h->d_err, h->g,
-                                     h->cfg.max_tag, h->cfg.max_radius, h->d_ft, s));
+        CK(h, launch_prepare_spheres(src, n, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot, h->d_err, h->g,
+                                     h->cfg.max_tag, h->cfg.max_radius, h->d_ft, src == h->d_rec ? nullptr : h->d_rec,
+                                     s));
         h->ft_dirty = false;   // the prepare launch zeroed the 6 n sums
         CK(h, launch_bin_spheres(h->d_fast, n, h->d_tile_cnt, h->d_bins, h->d_work, h->d_work_n, h->g, s));
         const int phase = (int)(h->step & 1);
@@ -480,7 +482,7 @@ lbdem_status lbdem_set_particles(lbdem_handle* h, int32_t n, const double* x, co
         CK(h, cudaEventRecord(h->ev_staged, h->stream));
         h->staged_pending = true;
     }
-    return voxelize(h, n, init_vel);
+    return voxelize(h, n, init_vel, h->d_rec);
 }
 
 lbdem_status lbdem_set_particles_device(lbdem_handle* h, int32_t n, const double* rec, int32_t init_vel) {
@@ -489,10 +491,11 @@ lbdem_status lbdem_set_particles_device(lbdem_handle* h, int32_t n, const double
     if (n > h->cap) return fail(h, LBDEM_ERR_CAPACITY, "set_particles_device: n exceeds max_particles");
     if (n > 0 && !rec) return fail(h, LBDEM_ERR_INVALID_ARG, "set_particles_device: null table");
     DeviceGuard dg(h->device);
-    if (n > 0 && rec != h->d_rec)
-        CK(h, cudaMemcpyAsync(h->d_rec, rec, (size_t)n * REC_STRIDE * sizeof(double), cudaMemcpyDeviceToDevice,
-                              h->stream));
-    return voxelize(h, n, init_vel);
+    // a table overlapping the handle's own (other than being it) cannot be read and copied in one pass
+    const uintptr_t a = (uintptr_t)rec, b = (uintptr_t)h->d_rec, len = (uintptr_t)n * REC_STRIDE * sizeof(double);
+    if (n > 0 && a != b && a < b + len && b < a + len)
+        return fail(h, LBDEM_ERR_INVALID_ARG, "set_particles_device: table overlaps the handle's particle table");
+    return voxelize(h, n, init_vel, rec);
 }
 
 lbdem_status lbdem_collide_and_stream(lbdem_handle* h) {

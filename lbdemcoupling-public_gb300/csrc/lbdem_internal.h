@@ -191,10 +191,11 @@ cudaError_t launch_collide_batch(const CollideArgs<T>* dargs, const int* seg0, i
                                  bool force, int blocks_per_sm, cudaStream_t s);
 
 // ft_zero (may be null): 6 n doubles set to zero by the same launch (the force
-// and torque sums of the next collide-stream step).
+// and torque sums of the next collide-stream step).  rec_copy (may be null, never
+// overlapping rec): receives a copy of the n records.
 cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
                                    int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
-                                   double* ft_zero, cudaStream_t s);
+                                   double* ft_zero, double* rec_copy, cudaStream_t s);
 // tile_cnt must be zero on entry; launch_voxelize leaves it zero again.  Every
 // tile that receives a sphere is appended to work[] (work_n counts them; zero
 // on entry, left zero by launch_voxelize).

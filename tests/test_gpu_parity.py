@@ -217,6 +217,54 @@ def test_init_equilibrium_in_either_phase(gpu, prec, steps):
             assert np.max(np.abs(vel[a] - u[a])) <= tol * 10, a
 
 
+@pytest.mark.parametrize("prec", [0, 1])
+def test_device_table_equals_host_buffers(gpu, prec):
+    """Particle tables handed over in device memory -- a slice of a larger table,
+    overwritten by the caller right after each call (the handle keeps its own
+    copy) -- give the populations of the host-buffer path bit for bit, and its
+    forces up to the order of the double atomic sums (read back through the
+    device-pointer variant); forces read between a voxelization and its step
+    are zero."""
+    import torch
+    shape = (24, 20, 28)
+    p = small_suspension(shape, 5, 2.5, 4.0, seed=31, overlap=True)
+    n = len(p.r)
+    res = []
+    for on_device in (False, True):
+        x = p.x.copy()
+        with gpu.Lattice(*shape, 1 / 0.6, precision=prec, max_particles=8, max_tag=16, max_radius=6) as L, \
+                torch.cuda.stream(torch.cuda.Stream(device=0)):
+            # the handle and the caller's tensors on one stream
+            L.set_stream(torch.cuda.current_stream(0).cuda_stream)
+            big = torch.zeros((n + 3) * 12, dtype=torch.float64, device="cuda:0")
+            ft = torch.zeros(6 * n, dtype=torch.float64, device="cuda:0")
+            for it in range(4):
+                if on_device:
+                    rec = gpu.pack_records(x, p.v, p.w, p.r, p.tag)
+                    big[36:36 + 12 * n] = torch.from_numpy(rec.ravel()).to("cuda:0")
+                    L.set_particles_device(n, big.data_ptr() + 36 * 8, init_vel=(it == 0))
+                    big.fill_(float("nan"))            # queued after the handle's copy
+                else:
+                    L.set_particles(x, p.v, p.w, p.r, p.tag, init_vel=(it == 0))
+                if it == 2:
+                    F0, T0 = L.get_forces()
+                    assert not F0.any() and not T0.any()
+                L.collide_and_stream()
+                if on_device:
+                    L.get_forces_device(ft.data_ptr())
+                    F = ft[:3 * n].cpu().numpy().reshape(n, 3)
+                    T = ft[3 * n:].cpu().numpy().reshape(n, 3)
+                else:
+                    F, T = L.get_forces()
+                x = np.mod(x + p.v, shape)
+            L.set_stream(None)
+            res.append((L.get_populations(), F, T))
+    (fh, Fh, Th), (fd, Fd, Td) = res
+    assert np.array_equal(fh, fd)
+    assert rel_err(Fd, Fh) <= 1e-12 and rel_err(Td, Th) <= 1e-12
+    assert np.abs(Fh).max() > 0
+
+
 @pytest.mark.parametrize("kind", ["bin_overflow", "queue_overflow"])
 def test_voxelization_overflow_paths(gpu, oracle, kind):
     """Clusters of spheres that overflow a tile's sphere bin (more than 64 spheres
