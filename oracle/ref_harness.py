@@ -1,7 +1,8 @@
 """ctypes wrapper of the reference harness (oracle/_ref/libref_harness.so) --
 TEST INFRASTRUCTURE.  Drives the reference's own SetSingleSphere3D,
-IBcompositeDynamics::collide and SumForceTorque3D (compiled against Palabos /
-LIGGGHTS stand-ins) on a periodic FP64 lattice."""
+IBcompositeDynamics::collide, SumForceTorque3D, ZhangPeriodicPressureFunctional3D
+and the PressureGradient / PoiseuilleProfileAndPressureGradient functors
+(compiled against Palabos / LIGGGHTS stand-ins) on a periodic FP64 lattice."""
 from __future__ import annotations
 
 import ctypes as C
@@ -35,6 +36,8 @@ def load():
         lib.ref_collide_stream.argtypes = [C.c_void_p]
         lib.ref_sum_force_torque.argtypes = [C.c_void_p, C.c_int, _D, _I, _D, _D]
         lib.ref_get_state.argtypes = [C.c_void_p, _D, _I, _D, _D]
+        lib.ref_zhang_rescale.argtypes = [C.c_void_p, _I, C.c_int, C.c_int, C.c_double, C.c_double]
+        lib.ref_init_profile.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, _I, C.c_int]
         _lib = lib
     return _lib
 
@@ -84,6 +87,16 @@ class RefLattice:
         T = np.zeros((n, 3))
         self.lib.ref_sum_force_torque(self.h, n, _d(self._x), self._tag.ctypes.data_as(_I), _d(F), _d(T))
         return F, T
+
+    def zhang_rescale(self, box, dimension, direction, rho_target, rho_avg):
+        b = np.ascontiguousarray(box, dtype=np.int32).reshape(6)
+        self.lib.ref_zhang_rescale(self.h, b.ctypes.data_as(_I), int(dimension), int(direction), float(rho_target),
+                                   float(rho_avg))
+
+    def init_profile(self, kind, rho_hi, rho_lo, u_max, n, dimension):
+        nn = np.ascontiguousarray(n, dtype=np.int32).reshape(3)
+        self.lib.ref_init_profile(self.h, int(kind), float(rho_hi), float(rho_lo), float(u_max),
+                                  nn.ctypes.data_as(_I), int(dimension))
 
     def state(self):
         sf = np.empty(self.shape)

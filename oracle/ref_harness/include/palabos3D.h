@@ -1,6 +1,7 @@
 // Minimal stand-ins for the Palabos v1.5r1 types used by the LBDEMcoupling PSM
 // headers (src/ibCompositeDynamics3D.*, src/ibProcessors3D.*, src/utils.h,
-// src/physunits.h) -- TEST INFRASTRUCTURE for the reference harness only.
+// src/physunits.h, src/periodicPressureFunctionals3D.*) -- TEST INFRASTRUCTURE
+// for the reference harness only.
 //
 // Palabos is not available here.  These declarations give the reference
 // headers the interface they call; the lattice-Boltzmann arithmetic inside
@@ -242,6 +243,28 @@ struct BoxProcessingFunctional3D_L {
     virtual void process(Box3D domain, BlockLattice3D<T, Descriptor>& lattice) = 0;
     virtual void getTypeOfModification(std::vector<modif::ModifT>& modified) const = 0;
 };
+
+// Declared only so that src/periodicPressureFunctionals3D.h parses: the Kim
+// functional and PeriodicPressureManager, which use them, are never instantiated
+// (the harness drives ZhangPeriodicPressureFunctional3D and the two initial-state
+// functors, which need nothing beyond the types above).
+class AtomicBlock3D {
+public:
+    virtual ~AtomicBlock3D() {}
+};
+class MultiBlock3D {
+public:
+    virtual ~MultiBlock3D() {}
+};
+class BoxProcessingFunctional3D {
+public:
+    virtual ~BoxProcessingFunctional3D() {}
+};
+template <typename T> class ScalarField3D;
+template <typename T, int nDim> class TensorField3D;
+template <typename T, template <typename U> class Descriptor> class MultiBlockLattice3D;
+template <typename T> class MultiScalarField3D;
+template <typename T, int nDim> class MultiTensorField3D;
 
 // Used only so that src/physunits.h compiles.
 template <typename T>

@@ -6,6 +6,9 @@
 //   src/ibProcessors3D.hh         SetSingleSphere3D::process / calcSolidFraction / setValues,
 //                                 SumForceTorque3D::process
 //   src/utils.h                   getParticleDataFromCell
+//   src/periodicPressureFunctionals3D.hh
+//                                 ZhangPeriodicPressureFunctional3D::process,
+//                                 PressureGradient, PoiseuilleProfileAndPressureGradient
 // and drives them the way src/ibDataExchangeWrappers3D.hh does (sphere loop,
 // bounding box intersected with the local block, force/torque vectors), with
 // push streaming on a periodic lattice standing in for Palabos' collideAndStream.
@@ -23,6 +26,7 @@
 #include "ibDynamicsParticleData.h"
 #include "ibCompositeDynamics3D.h"
 #include "ibProcessors3D.h"
+#include "periodicPressureFunctionals3D.h"
 
 // LIGGGHTS' coupling wrapper: only its atom map is used by SumForceTorque3D.
 LiggghtsCouplingWrapper::LiggghtsCouplingWrapper(char**, MPI_Comm) : lmp(0) {}
@@ -55,6 +59,17 @@ struct Harness {
         return getParticleDataFromCell<T, DESCRIPTOR>(cell(x, y, z));
     }
 };
+
+// Stand-in for Palabos' iniCellAtEquilibrium, through which initializeAtEquilibrium
+// applies a density/velocity functor: j = density u, rhoBar = density - 1,
+// f_i = feq_i(rhoBar, 1 / (1 + rhoBar), j, |j|^2).
+void ini_at_equilibrium(Cell<T, DESCRIPTOR>& c, T density, Array<T, 3> const& u) {
+    Array<T, 3> j(density * u[0], density * u[1], density * u[2]);
+    const T jSqr = VectorTemplateImpl<T, 3>::normSqr(j);
+    const T rhoBar = density - (T)1;
+    const T invRho = DESCRIPTOR<T>::invRho(rhoBar);
+    for (plint i = 0; i < DESCRIPTOR<T>::q; ++i) c[i] = dynamicsTemplates<T, DESCRIPTOR>::feq(i, rhoBar, invRho, j, jSqr);
+}
 
 }  // namespace
 
@@ -154,6 +169,33 @@ void ref_sum_force_torque(void* hp, int n, const double* xs, const int32_t* tags
     SumForceTorque3D<T, DESCRIPTOR> sft(x_lb, &force.front(), &torque.front(), wrapper);
     sft.process(Box3D(1, h.nx, 1, h.ny, 1, h.nz), h.lattice);
     for (int i = 0; i < 3 * n; ++i) { F[i] = force[i]; Tq[i] = torque[i]; }
+}
+
+// ZhangPeriodicPressureFunctional3D::process (src/periodicPressureFunctionals3D.hh:137-159)
+// on box = {x0, x1, y0, y1, z0, z1} in lattice coordinates.
+void ref_zhang_rescale(void* hp, const int32_t* b, int dim, int dir, double rhoTarget, double rhoAvg) {
+    Harness& h = *(Harness*)hp;
+    ZhangPeriodicPressureFunctional3D<T, DESCRIPTOR> fn(rhoTarget, rhoAvg, dim, dir);
+    fn.process(Box3D(b[0] + 1, b[1] + 1, b[2] + 1, b[3] + 1, b[4] + 1, b[5] + 1), h.lattice);
+}
+
+// Every cell at equilibrium with the density and velocity of PressureGradient
+// (kind 0, src/periodicPressureFunctionals3D.hh:238-256; grid size n[dim]) or
+// PoiseuilleProfileAndPressureGradient (kind 1, :259-298; grid sizes n[0..2]),
+// evaluated at the cell's lattice coordinates.
+void ref_init_profile(void* hp, int kind, double pHi, double pLo, double uMax, const int32_t* n, int dim) {
+    Harness& h = *(Harness*)hp;
+    const PressureGradient<T> gradient(pHi, pLo, n[dim], dim);
+    const PoiseuilleProfileAndPressureGradient<T> poiseuille(pHi, pLo, uMax, n[0], n[1], n[2], dim);
+    for (plint x = 0; x < h.nx; ++x)
+        for (plint y = 0; y < h.ny; ++y)
+            for (plint z = 0; z < h.nz; ++z) {
+                T density = 0;
+                Array<T, 3> u;
+                if (kind == 0) gradient(x, y, z, density, u);
+                else poiseuille(x, y, z, density, u);
+                ini_at_equilibrium(h.cell(x, y, z), density, u);
+            }
 }
 
 // Per-cell particle data (IBdynamicsParticleData): sf, partId, uPart, hydrodynamicForce.
