@@ -1,7 +1,8 @@
 // Minimal stand-ins for the Palabos v1.5r1 types used by the LBDEMcoupling PSM
 // headers (src/ibCompositeDynamics3D.*, src/ibProcessors3D.*, src/utils.h,
-// src/physunits.h, src/periodicPressureFunctionals3D.*) -- TEST INFRASTRUCTURE
-// for the reference harness only.
+// src/physunits.h, src/periodicPressureFunctionals3D.*,
+// src/ibDataWritingFunctionals3D.*) -- TEST INFRASTRUCTURE for the reference
+// harness only.
 //
 // Palabos is not available here.  These declarations give the reference
 // headers the interface they call; the lattice-Boltzmann arithmetic inside
@@ -244,14 +245,46 @@ struct BoxProcessingFunctional3D_L {
     virtual void getTypeOfModification(std::vector<modif::ModifT>& modified) const = 0;
 };
 
-// Declared only so that src/periodicPressureFunctionals3D.h parses: the Kim
-// functional and PeriodicPressureManager, which use them, are never instantiated
-// (the harness drives ZhangPeriodicPressureFunctional3D and the two initial-state
-// functors, which need nothing beyond the types above).
 class AtomicBlock3D {
 public:
     virtual ~AtomicBlock3D() {}
 };
+
+// Scalar and tensor fields of one atomic block, indexed like BlockLattice3D
+// (the caller sizes them with the lattice's envelope).
+template <typename T>
+class ScalarField3D : public AtomicBlock3D {
+public:
+    ScalarField3D(plint nx_, plint ny_, plint nz_) : nx(nx_), ny(ny_), nz(nz_), data(nx_ * ny_ * nz_) {}
+    T& get(plint x, plint y, plint z) { return data[(x * ny + y) * nz + z]; }
+    plint nx, ny, nz;
+    std::vector<T> data;
+};
+template <typename T, int nDim>
+class TensorField3D : public AtomicBlock3D {
+public:
+    TensorField3D(plint nx_, plint ny_, plint nz_) : nx(nx_), ny(ny_), nz(nz_), data(nx_ * ny_ * nz_) {}
+    Array<T, nDim>& get(plint x, plint y, plint z) { return data[(x * ny + y) * nz + z]; }
+    plint nx, ny, nz;
+    std::vector<Array<T, nDim> > data;
+};
+template <typename T1, template <typename U> class Descriptor, typename T2>
+struct BoxProcessingFunctional3D_LS {
+    virtual ~BoxProcessingFunctional3D_LS() {}
+    virtual void process(Box3D domain, BlockLattice3D<T1, Descriptor>& lattice, ScalarField3D<T2>& field) = 0;
+    virtual void getTypeOfModification(std::vector<modif::ModifT>& modified) const = 0;
+};
+template <typename T1, template <typename U> class Descriptor, typename T2, int nDim>
+struct BoxProcessingFunctional3D_LT {
+    virtual ~BoxProcessingFunctional3D_LT() {}
+    virtual void process(Box3D domain, BlockLattice3D<T1, Descriptor>& lattice, TensorField3D<T2, nDim>& field) = 0;
+    virtual void getTypeOfModification(std::vector<modif::ModifT>& modified) const = 0;
+};
+
+// Declared only so that src/periodicPressureFunctionals3D.h parses: the Kim
+// functional and PeriodicPressureManager, which use them, are never instantiated
+// (the harness drives ZhangPeriodicPressureFunctional3D and the two initial-state
+// functors, which need nothing beyond the types above).
 class MultiBlock3D {
 public:
     virtual ~MultiBlock3D() {}
@@ -260,8 +293,6 @@ class BoxProcessingFunctional3D {
 public:
     virtual ~BoxProcessingFunctional3D() {}
 };
-template <typename T> class ScalarField3D;
-template <typename T, int nDim> class TensorField3D;
 template <typename T, template <typename U> class Descriptor> class MultiBlockLattice3D;
 template <typename T> class MultiScalarField3D;
 template <typename T, int nDim> class MultiTensorField3D;

@@ -9,6 +9,8 @@
 //   src/periodicPressureFunctionals3D.hh
 //                                 ZhangPeriodicPressureFunctional3D::process,
 //                                 PressureGradient, PoiseuilleProfileAndPressureGradient
+//   src/ibDataWritingFunctionals3D.hh
+//                                 Get{Scalar,Vector}QuantityFromDynamicsFunctional (field export)
 // and drives them the way src/ibDataExchangeWrappers3D.hh does (sphere loop,
 // bounding box intersected with the local block, force/torque vectors), with
 // push streaming on a periodic lattice standing in for Palabos' collideAndStream.
@@ -27,6 +29,7 @@
 #include "ibCompositeDynamics3D.h"
 #include "ibProcessors3D.h"
 #include "periodicPressureFunctionals3D.h"
+#include "ibDataWritingFunctionals3D.h"
 
 // LIGGGHTS' coupling wrapper: only its atom map is used by SumForceTorque3D.
 LiggghtsCouplingWrapper::LiggghtsCouplingWrapper(char**, MPI_Comm) : lmp(0) {}
@@ -55,9 +58,6 @@ struct Harness {
     }
     Cell<T, DESCRIPTOR>& cell(plint x, plint y, plint z) { return lattice.get(x + 1, y + 1, z + 1); }
     size_t idx(plint x, plint y, plint z) const { return ((size_t)x * ny + y) * nz + z; }
-    IBdynamicsParticleData<T, DESCRIPTOR>* pd(plint x, plint y, plint z) {
-        return getParticleDataFromCell<T, DESCRIPTOR>(cell(x, y, z));
-    }
 };
 
 // Stand-in for Palabos' iniCellAtEquilibrium, through which initializeAtEquilibrium
@@ -198,20 +198,31 @@ void ref_init_profile(void* hp, int kind, double pHi, double pLo, double uMax, c
             }
 }
 
-// Per-cell particle data (IBdynamicsParticleData): sf, partId, uPart, hydrodynamicForce.
+// Per-cell particle data (IBdynamicsParticleData: sf, partId, uPart,
+// hydrodynamicForce) exported the way the reference's case drivers export it,
+// through GetScalarQuantityFromDynamicsFunctional (SolidFraction, ParticleId) and
+// GetVectorQuantityFromDynamicsFunctional (ParticleVelocity, HydrodynamicForce),
+// src/ibDataWritingFunctionals3D.hh:30-114, into fields of type T.
 void ref_get_state(void* hp, double* sf, int32_t* id, double* up, double* cf) {
     Harness& h = *(Harness*)hp;
+    const plint ex = h.nx + 2, ey = h.ny + 2, ez = h.nz + 2;
+    const Box3D inner(1, h.nx, 1, h.ny, 1, h.nz);
+    ScalarField3D<T> fsf(ex, ey, ez), fid(ex, ey, ez);
+    TensorField3D<T, 3> fup(ex, ey, ez), fcf(ex, ey, ez);
+    GetScalarQuantityFromDynamicsFunctional<T, DESCRIPTOR, T>(SolidFraction).process(inner, h.lattice, fsf);
+    GetScalarQuantityFromDynamicsFunctional<T, DESCRIPTOR, T>(ParticleId).process(inner, h.lattice, fid);
+    GetVectorQuantityFromDynamicsFunctional<T, DESCRIPTOR, T, 3>(ParticleVelocity).process(inner, h.lattice, fup);
+    GetVectorQuantityFromDynamicsFunctional<T, DESCRIPTOR, T, 3>(HydrodynamicForce).process(inner, h.lattice, fcf);
     const size_t N = (size_t)h.nx * h.ny * h.nz;
     for (plint x = 0; x < h.nx; ++x)
         for (plint y = 0; y < h.ny; ++y)
             for (plint z = 0; z < h.nz; ++z) {
-                IBdynamicsParticleData<T, DESCRIPTOR>* p = h.pd(x, y, z);
                 const size_t c = h.idx(x, y, z);
-                sf[c] = p->solidFraction;
-                id[c] = (int32_t)p->partId;
+                sf[c] = fsf.get(x + 1, y + 1, z + 1);
+                id[c] = (int32_t)fid.get(x + 1, y + 1, z + 1);
                 for (int d = 0; d < 3; ++d) {
-                    up[d * N + c] = p->uPart[d];
-                    cf[d * N + c] = p->hydrodynamicForce[d];
+                    up[d * N + c] = fup.get(x + 1, y + 1, z + 1)[d];
+                    cf[d * N + c] = fcf.get(x + 1, y + 1, z + 1)[d];
                 }
             }
 }
