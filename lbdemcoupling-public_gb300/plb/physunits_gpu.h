@@ -37,6 +37,9 @@ private:
     T lx, ly, lz;
 };
 
+// Lattice positions are cell centres: physical position = (lattice + offset)
+// deltaX l_p with offset 1/2 by default; setLbOffset changes the per-axis
+// offsets used by the X/Y/Z variants (getLbPosition / getPhysPosition keep 1/2).
 template <typename T>
 class PhysUnits3D {
 public:
@@ -47,29 +50,57 @@ public:
           forceFactor(std::pow(param.getDeltaX(), 4) / std::pow(param.getDeltaT(), 2) * rho_p * std::pow(l_p, 4) /
                       std::pow(t_p, 2)),
           torqueFactor(std::pow(param.getDeltaX(), 5) / std::pow(param.getDeltaT(), 2) * rho_p * std::pow(l_p, 5) /
-                       std::pow(t_p, 2)) {}
+                       std::pow(t_p, 2)),
+          lbOffsetX(0.5), lbOffsetY(0.5), lbOffsetZ(0.5) {}
 
     T getRe() const { return Re; }
+    void setLbOffset(T const ox, T const oy, T const oz) {
+        lbOffsetX = ox;
+        lbOffsetY = oy;
+        lbOffsetZ = oz;
+    }
+
+    // physical -> lattice
     T getLbLength(T const physL) const { return physL / l_p / param.getDeltaX(); }
     T getLbPosition(T const physL) const { return physL / l_p / param.getDeltaX() - 0.5; }
+    T getLbPositionX(T const physL) const { return physL / l_p / param.getDeltaX() - lbOffsetX; }
+    T getLbPositionY(T const physL) const { return physL / l_p / param.getDeltaX() - lbOffsetY; }
+    T getLbPositionZ(T const physL) const { return physL / l_p / param.getDeltaX() - lbOffsetZ; }
     T getLbVel(T const physVel) const { return physVel / u_p * param.getLatticeU(); }
-    T getLbFreq(T const physFreq) const { return physFreq * t_p * param.getDeltaT(); }
+    T getLbTime(T const physTime) const { return physTime / t_p / param.getDeltaT(); }
+    T getLbDensity(T const physDensity) const { return physDensity / rho_p; }
     T getLbAccel(T const physAccel) const {
         return physAccel * (t_p * t_p / l_p) * (param.getDeltaT() * param.getDeltaT() / param.getDeltaX());
     }
+    T getLbFreq(T const physFreq) const { return physFreq * t_p * param.getDeltaT(); }
     long getLbSteps(T const physTime) const { return (long)(physTime / param.getDeltaT() / t_p + 0.5); }
+    // lattice density from a pressure: p = c_s^2 rho (lattice), c_s^2 = 1/3
+    T getLbRho(T const physPress, T const pOffset = 0) const {
+        return (physPress - pOffset) * 3. / getPhysForce(1.) * std::pow(getPhysLength(1.), 2);
+    }
+
+    // lattice -> physical
     T getPhysLength(T const lbLength) const { return lbLength * param.getDeltaX() * l_p; }
     T getPhysPosition(T const lbLength) const { return (lbLength + 0.5) * param.getDeltaX() * l_p; }
+    T getPhysPositionX(T const lbLength) const { return (lbLength + lbOffsetX) * param.getDeltaX() * l_p; }
+    T getPhysPositionY(T const lbLength) const { return (lbLength + lbOffsetY) * param.getDeltaX() * l_p; }
+    T getPhysPositionZ(T const lbLength) const { return (lbLength + lbOffsetZ) * param.getDeltaX() * l_p; }
     T getPhysVel(T const lbVel) const { return lbVel / param.getLatticeU() * u_p; }
     T getPhysTime(T const lbTime) const { return lbTime * param.getDeltaT() * t_p; }
+    T getPhysDensity(T const lbDensity) const { return lbDensity * rho_p; }
+    T getPhysAccel(T const lbAccel) const { return lbAccel / getLbAccel(1.); }
     T getPhysForce(T const lbForce) const { return lbForce * forceFactor; }
     T getPhysTorque(T const lbTorque) const { return lbTorque * torqueFactor; }
+    T getPhysPress(T const lbRho, T pOffset = 0) const {
+        return (lbRho - 1.) / 3. * getPhysForce(1) / std::pow(getPhysLength(1.), 2) + pOffset;
+    }
     LbdemFlowParam<T> const& getLbParam() const { return param; }
 
 private:
     T const l_p, u_p, t_p, nu_p, rho_p, Re;
     LbdemFlowParam<T> param;
     T const forceFactor, torqueFactor;
+    T lbOffsetX, lbOffsetY, lbOffsetZ;
 };
 
 }  // namespace plb
