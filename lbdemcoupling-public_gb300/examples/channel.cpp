@@ -6,7 +6,12 @@
 // both ways: explicitly (mode "explicit") and as the fused drop (mode "fused").
 //
 // usage: channel [steps=300] [explicit|fused]
-// Prints the mean x velocity of the fluid and the x force on the sphere.
+// Prints the mean x velocity of the fluid, the x force on the sphere and, through
+// the shim's field export (the reference's Get{Scalar,Vector}QuantityFromDynamics
+// functionals), the cells the sphere covers, those it owns and the largest
+// surface speed (zero: the sphere is held at rest).
+#include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -58,8 +63,20 @@ int main(int argc, char** argv) {
         lattice.check(lbdem_get_field(lattice.handle(), LBDEM_FIELD_VELOCITY, u.data()));
         double ux = 0;
         for (size_t c = 0; c < N; ++c) ux += u[c];
-        std::printf("{\"mode\": \"%s\", \"steps\": %ld, \"mean_ux\": %.17g, \"fx\": %.17g}\n", fused ? "fused" : "explicit",
-                    steps, ux / (double)N, wrapper.fix.f[0][0]);
+        std::vector<double> sf, id, up;
+        plb::getScalarQuantityFromDynamics(lattice, plb::SolidFraction, sf);
+        plb::getScalarQuantityFromDynamics(lattice, plb::ParticleId, id);
+        plb::getVectorQuantityFromDynamics(lattice, plb::ParticleVelocity, up);
+        long solid = 0, owned = 0;
+        double upMax = 0;
+        for (size_t c = 0; c < N; ++c) {
+            solid += sf[c] > 0;
+            owned += id[c] == 1.0;
+            for (int d = 0; d < 3; ++d) upMax = std::max(upMax, std::abs(up[3 * c + d]));
+        }
+        std::printf("{\"mode\": \"%s\", \"steps\": %ld, \"mean_ux\": %.17g, \"fx\": %.17g, \"solid_cells\": %ld, "
+                    "\"owned_cells\": %ld, \"max_up\": %.17g}\n",
+                    fused ? "fused" : "explicit", steps, ux / (double)N, wrapper.fix.f[0][0], solid, owned, upMax);
     } catch (std::exception const& e) {
         std::fprintf(stderr, "channel: %s\n", e.what());
         return std::strstr(e.what(), "no suitable CUDA device") ? 77 : 1;

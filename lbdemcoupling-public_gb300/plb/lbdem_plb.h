@@ -62,6 +62,7 @@ public:
         const lbdem_status s = lbdem_create(&c, &h_);
         if (s != LBDEM_OK) throw std::runtime_error(std::string("lbdem_create: ") + lbdem_status_string(s));
         nx_ = nx; ny_ = ny; nz_ = nz;
+        prec_ = o.precision;
     }
     ~GpuLattice3D() { if (h_) lbdem_destroy(h_); }
     GpuLattice3D(GpuLattice3D const&) = delete;
@@ -70,6 +71,8 @@ public:
     int32_t getNx() const { return nx_; }
     int32_t getNy() const { return ny_; }
     int32_t getNz() const { return nz_; }
+    size_t cells() const { return (size_t)nx_ * ny_ * nz_; }
+    int32_t precision() const { return prec_; }
     lbdem_handle* handle() { return h_; }
 
     // lattice.initialize() of a lattice at rest, or initializeAtEquilibrium with uniform rho, u.
@@ -126,6 +129,7 @@ public:
 private:
     lbdem_handle* h_ = nullptr;
     int32_t nx_ = 0, ny_ = 0, nz_ = 0;
+    int32_t prec_ = LBDEM_PREC_FP64;
 };
 
 // setSpheresOnLattice, src/ibDataExchangeWrappers3D.hh:33-146.  With
@@ -190,6 +194,46 @@ void applyZhangPeriodicPressure(GpuLattice3D& lattice, Box const& box, double rh
     int32_t b[6];
     GpuLattice3D::box6(box, b);
     lattice.check(lbdem_zhang_rescale(lattice.handle(), b, dimension, direction, rhoTarget, rhoAvg));
+}
+
+// Per-cell quantities of the reference's field export (src/ibDataWritingFunctionals3D.h:30-31).
+enum IBscalarQuantity { SolidFraction, ParticleId };
+enum IBvectorQuantity { ParticleVelocity, HydrodynamicForce };
+
+// applyProcessingFunctional(new GetScalarQuantityFromDynamicsFunctional<T, DESCRIPTOR, T>(which),
+// lattice.getBoundingBox(), lattice, field), src/ibDataWritingFunctionals3D.hh:30-60, over the
+// whole lattice: out[(x ny + y) nz + z] as doubles (the owner tag converted like the
+// functional's cast).
+inline void getScalarQuantityFromDynamics(GpuLattice3D& lattice, IBscalarQuantity which, std::vector<double>& out) {
+    const size_t N = lattice.cells();
+    out.assign(N, 0.0);
+    if (which == SolidFraction) {
+        lattice.check(lbdem_get_field(lattice.handle(), LBDEM_FIELD_SOLID_FRACTION, out.data()));
+        return;
+    }
+    std::vector<int32_t> id(N);
+    lattice.check(lbdem_get_field(lattice.handle(), LBDEM_FIELD_PARTICLE_ID, id.data()));
+    for (size_t c = 0; c < N; ++c) out[c] = (double)id[c];
+}
+
+// applyProcessingFunctional(new GetVectorQuantityFromDynamicsFunctional<T, DESCRIPTOR, T, 3>(which),
+// ...), src/ibDataWritingFunctionals3D.hh:68-114: out[3 cell + d], the layout of a
+// TensorField3D<T, 3>.  HydrodynamicForce needs Options::flags with LBDEM_FLAG_CELL_FORCE.
+inline void getVectorQuantityFromDynamics(GpuLattice3D& lattice, IBvectorQuantity which, std::vector<double>& out) {
+    const size_t N = lattice.cells();
+    const int32_t field = which == ParticleVelocity ? LBDEM_FIELD_PARTICLE_VELOCITY : LBDEM_FIELD_HYDRO_FORCE;
+    out.assign(3 * N, 0.0);
+    if (lattice.precision() == LBDEM_PREC_FP64) {
+        std::vector<double> planar(3 * N);
+        lattice.check(lbdem_get_field(lattice.handle(), field, planar.data()));
+        for (size_t c = 0; c < N; ++c)
+            for (int d = 0; d < 3; ++d) out[3 * c + d] = planar[d * N + c];
+    } else {
+        std::vector<float> planar(3 * N);
+        lattice.check(lbdem_get_field(lattice.handle(), field, planar.data()));
+        for (size_t c = 0; c < N; ++c)
+            for (int d = 0; d < 3; ++d) out[3 * c + d] = (double)planar[d * N + c];
+    }
 }
 
 // getForcesFromLattice, src/ibDataExchangeWrappers3D.hh:160-246.  FixType is the

@@ -80,9 +80,11 @@ def test_channel_example_builds_and_needs_a_gpu(lbdem_lib):
 
 
 @pytest.mark.gpu
-def test_channel_example_fused_equals_explicit(gpu):
+def test_channel_example_fused_equals_explicit(gpu, oracle):
     """The reference's per-step computeAverageDensity + Zhang functional calls and the
-    fused pressure drop give the same channel (box sums differ only in summation order)."""
+    fused pressure drop give the same channel (box sums differ only in summation order).
+    The shim's field export (solid fraction, owner tag, surface velocity) covers
+    exactly the cells the oracle's voxelization of the held sphere covers."""
     import json
     exe = build_example("channel")
     out = {}
@@ -92,6 +94,16 @@ def test_channel_example_fused_equals_explicit(gpu):
         out[mode] = json.loads(r.stdout)
     assert out["fused"]["mean_ux"] > 1e-4
     assert out["fused"]["fx"] > 0                       # drag on the held sphere points downstream
+    # the held sphere: physical centre (32.5, 12.5, 12.5) = lattice (32, 12, 12), radius 4, tag 1
+    ol = oracle.OracleLattice(64, 24, 24, 1 / 0.6, periodic=(1, 0, 0))
+    ol.set_particles(np.array([[32.0, 12.0, 12.0]]), np.zeros((1, 3)), np.zeros((1, 3)), np.array([4.0]),
+                     np.array([1], dtype=np.int32))
+    covered = int(np.count_nonzero(ol.state()["sf"] > 0))
+    assert covered > 400
+    for mode in out:
+        assert out[mode]["solid_cells"] == covered
+        assert out[mode]["owned_cells"] == covered
+        assert out[mode]["max_up"] == 0.0
     for k in ("mean_ux", "fx"):
         assert abs(out["fused"][k] - out["explicit"][k]) <= 1e-10 * abs(out["explicit"][k])
 
