@@ -368,6 +368,15 @@ def run_adjoint():
     return out
 
 
+def max_over_ranks(values, dist, device):
+    """Element-wise maximum of per-rank timings over all ranks of the process group
+    (a replica's time is the slowest rank's: every rank runs its own lattice)."""
+    import torch
+    t = torch.tensor([float(v) for v in values], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return [float(v) for v in t.tolist()]
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -451,10 +460,7 @@ def main():
 
     t32 = r32["total_ms"]
     if dist:
-        t = torch.tensor([t32, r64["total_ms"] if r64 else 0.0, e2e_s], dtype=torch.float64,
-                         device=f"cuda:{device}")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        t32, t64, e2e_s = (float(v) for v in t.tolist())
+        t32, t64, e2e_s = max_over_ranks([t32, r64["total_ms"] if r64 else 0.0, e2e_s], dist, f"cuda:{device}")
     else:
         t64 = r64["total_ms"] if r64 else float("nan")
     if rank != 0:
