@@ -347,7 +347,7 @@ def run_batched(steps: int, warmup: int, single_steps: int, device: int, flow_ax
         "one_at_a_time": cells * single_steps / t_one / 1e6,
         "one_at_a_time_steps": single_steps,
         "speedup_vs_one_at_a_time": (cells * steps / t_e2e) / (cells * single_steps / t_one),
-        "launches_per_step": launches, "launches_per_step_one_at_a_time": 5 * len(doms),
+        "launches_per_step": launches, "launches_per_step_one_at_a_time": 4 * len(doms),
         "collide_blocks_per_sm": bps, "k1_ms": k1_ms,
         "k1_roofline": None if ach is None else {"achieved": ach, "peak": peak, "unit": "GB/s", "frac": ach / peak,
                                                    "bytes_per_cell": BYTES_PER_CELL["fp32"]},

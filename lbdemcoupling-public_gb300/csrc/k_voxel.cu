@@ -58,38 +58,12 @@ __device__ __forceinline__ int tiles_along(int n) { return (n + TILE - 1) / TILE
 // src/ibProcessors3D.h:43-45) intersected with the lattice
 // (src/ibDataExchangeWrappers3D.hh:127-133), thresholds, the float split of
 // the centre, and the tag -> lowest list index map (LAMMPS atom->map keeps the
-// owned atom, which precedes its ghost images).
-// BATCH: slot i belongs to the domain d with soff[d] <= i; slots past the
-// domain's particle count are skipped; the map stores domain-local slots.
-// ft_zero (may be null): the 6 n force/torque sums of the coming collide-stream
-// step, zeroed here instead of by a separate memset launch.  rec_copy (may be
-// null, never overlapping rec): receives a copy of the n records.
-template <bool BATCH>
-__global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereDev* __restrict__ sph,
-                                  SphereFast* __restrict__ fast, float* __restrict__ xpf,
-                                  int* __restrict__ tag2slot, unsigned* __restrict__ err, Geom g, int max_tag,
-                                  double max_radius, const DomView* __restrict__ doms, const int* __restrict__ soff,
-                                  int ndom, const int* __restrict__ ncur, double* __restrict__ ft_zero,
-                                  double* __restrict__ rec_copy) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= n) return;
-    if (ft_zero) {
-#pragma unroll
-        for (int k = 0; k < 6; ++k) ft_zero[(size_t)k * n + i] = 0.0;
-    }
-    int il = i;
-    if (BATCH) {
-        const int d = find_domain(soff, ndom, i);
-        il = i - __ldg(soff + d);
-        if (il >= __ldg(ncur + d)) return;
-        g = doms[d].g;
-        tag2slot += doms[d].tag0;
-    }
-    const double* p = rec + (size_t)i * REC_STRIDE;
-    if (rec_copy) {
-#pragma unroll
-        for (int k = 0; k < REC_STRIDE; ++k) rec_copy[(size_t)i * REC_STRIDE + k] = p[k];
-    }
+// owned atom, which precedes its ghost images).  Returns the cell box that the
+// sphere's tiles are binned by (lo > hi: the sphere reaches no cell).
+__device__ __forceinline__ void prepare_sphere(const double* __restrict__ p, int i, int il, const Geom& g,
+                                               int max_tag, double max_radius, SphereDev* __restrict__ sph,
+                                               SphereFast* __restrict__ fast, float* __restrict__ xpf,
+                                               int* __restrict__ tag2slot, unsigned* __restrict__ err, int box[6]) {
     SphereDev s;
     SphereFast q;
     for (int d = 0; d < 3; ++d) { s.x[d] = p[d]; s.v[d] = p[3 + d]; s.w[d] = p[6 + d]; }
@@ -138,6 +112,8 @@ __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereD
         q.hi[d] = s.valid ? s.hi[d] : 0;
         q.v[d] = (float)s.v[d];
         q.w[d] = (float)s.w[d];
+        box[2 * d] = q.lo[d];
+        box[2 * d + 1] = q.hi[d];
     }
     q.tag = s.tag;
     q.pad = 0;
@@ -149,30 +125,47 @@ __global__ void k_prepare_spheres(const double* __restrict__ rec, int n, SphereD
     if (s.tag >= 1) atomicMin(tag2slot + s.tag, il);
 }
 
-// One warp per sphere, lanes stride over the tiles its box overlaps and
-// append the sphere to each tile's bin (entries past TILE_BIN are dropped; the
-// voxelization of such a tile re-collects its spheres).  The first sphere of a
-// tile also appends the tile to the work list.
+// One warp per sphere: lane 0 prepares the sphere (prepare_sphere), then the
+// lanes stride over the tiles its box overlaps and append the sphere to each
+// tile's bin (entries past TILE_BIN are dropped; the voxelization of such a
+// tile re-collects its spheres; a tile's bin is rank-sorted there, so the
+// append order does not matter).  The first sphere of a tile also appends the
+// tile to the work list.
+// BATCH: slot i belongs to the domain d with soff[d] <= i; slots past the
+// domain's particle count are skipped; the map stores domain-local slots.
+// ft_zero (may be null): the 6 n force/torque sums of the coming collide-stream
+// step, zeroed here instead of by a separate memset launch.  rec_copy (may be
+// null, never overlapping rec): receives a copy of the n records.
 template <bool BATCH>
-__global__ void k_bin_spheres(const SphereFast* __restrict__ fast, int n, int* __restrict__ tile_cnt,
-                              int* __restrict__ bins, int* __restrict__ work, int* __restrict__ work_n, Geom g,
+__global__ void k_prepare_bin(const double* __restrict__ rec, int n, SphereDev* __restrict__ sph,
+                              SphereFast* __restrict__ fast, float* __restrict__ xpf, int* __restrict__ tag2slot,
+                              unsigned* __restrict__ err, Geom g, int max_tag, double max_radius,
                               const DomView* __restrict__ doms, const int* __restrict__ soff, int ndom,
-                              const int* __restrict__ ncur) {
+                              const int* __restrict__ ncur, double* __restrict__ ft_zero,
+                              double* __restrict__ rec_copy, int* __restrict__ tile_cnt, int* __restrict__ bins,
+                              int* __restrict__ work, int* __restrict__ work_n) {
     const int i = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
     const int lane = threadIdx.x & 31;
-    if (i >= n) return;
+    if (i >= n) return;   // warp-uniform from here on
+    if (ft_zero && lane < 6) ft_zero[(size_t)lane * n + i] = 0.0;
     int il = i, t0 = 0;
     if (BATCH) {
         const int d = find_domain(soff, ndom, i);
         il = i - __ldg(soff + d);
         if (il >= __ldg(ncur + d)) return;
         g = doms[d].g;
+        tag2slot += doms[d].tag0;
         t0 = doms[d].t0;
     }
-    const SphereFast& q = fast[i];
-    if (q.lo[0] > q.hi[0] || q.lo[1] > q.hi[1] || q.lo[2] > q.hi[2]) return;
-    const int tx0 = q.lo[0] / TILE, ty0 = q.lo[1] / TILE, tz0 = q.lo[2] / TILE;
-    const int ex = q.hi[0] / TILE - tx0 + 1, ey = q.hi[1] / TILE - ty0 + 1, ez = q.hi[2] / TILE - tz0 + 1;
+    const double* p = rec + (size_t)i * REC_STRIDE;
+    if (rec_copy && lane < REC_STRIDE) rec_copy[(size_t)i * REC_STRIDE + lane] = p[lane];
+    int box[6] = {1, 0, 1, 0, 1, 0};
+    if (lane == 0) prepare_sphere(p, i, il, g, max_tag, max_radius, sph, fast, xpf, tag2slot, err, box);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) box[k] = __shfl_sync(0xffffffffu, box[k], 0);
+    if (box[0] > box[1] || box[2] > box[3] || box[4] > box[5]) return;
+    const int tx0 = box[0] / TILE, ty0 = box[2] / TILE, tz0 = box[4] / TILE;
+    const int ex = box[1] / TILE - tx0 + 1, ey = box[3] / TILE - ty0 + 1, ez = box[5] / TILE - tz0 + 1;
     const int tny = tiles_along(g.ny), tnz = tiles_along(g.nz);
     const int total = ex * ey * ez;
     for (int k = lane; k < total; k += 32) {
@@ -602,41 +595,26 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
 
 }  // namespace
 
-cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
-                                   int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
-                                   double* ft_zero, double* rec_copy, cudaStream_t s) {
+cudaError_t launch_prepare_bin(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
+                               int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
+                               double* ft_zero, double* rec_copy, int* tile_cnt, int* bins, int* work, int* work_n,
+                               cudaStream_t s) {
     if (n <= 0) return cudaSuccess;
-    k_prepare_spheres<false><<<(n + 127) / 128, 128, 0, s>>>(rec, n, sph, fast, xpf, tag2slot, err, g, max_tag,
-                                                            max_radius, nullptr, nullptr, 0, nullptr, ft_zero,
-                                                            rec_copy);
+    k_prepare_bin<false><<<(n + 7) / 8, 256, 0, s>>>(rec, n, sph, fast, xpf, tag2slot, err, g, max_tag, max_radius,
+                                                     nullptr, nullptr, 0, nullptr, ft_zero, rec_copy, tile_cnt, bins,
+                                                     work, work_n);
     return cudaGetLastError();
 }
 
-cudaError_t launch_prepare_spheres_batch(const double* rec, int nslots, SphereDev* sph, SphereFast* fast, float* xpf,
-                                         int* tag2slot, unsigned* err, int max_tag, double max_radius,
-                                         const DomView* doms, const int* soff, int ndom, const int* ncur,
-                                         double* ft_zero, cudaStream_t s) {
-    if (nslots <= 0) return cudaSuccess;
-    k_prepare_spheres<true><<<(nslots + 127) / 128, 128, 0, s>>>(rec, nslots, sph, fast, xpf, tag2slot, err, Geom{},
-                                                                max_tag, max_radius, doms, soff, ndom, ncur, ft_zero,
-                                                                nullptr);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_bin_spheres(const SphereFast* fast, int n, int* tile_cnt, int* bins, int* work, int* work_n,
-                               Geom g, cudaStream_t s) {
-    if (n <= 0) return cudaSuccess;
-    k_bin_spheres<false><<<(n + 7) / 8, 256, 0, s>>>(fast, n, tile_cnt, bins, work, work_n, g, nullptr, nullptr, 0,
-                                                     nullptr);
-    return cudaGetLastError();
-}
-
-cudaError_t launch_bin_spheres_batch(const SphereFast* fast, int nslots, int* tile_cnt, int* bins, int* work,
-                                     int* work_n, const DomView* doms, const int* soff, int ndom, const int* ncur,
+cudaError_t launch_prepare_bin_batch(const double* rec, int nslots, SphereDev* sph, SphereFast* fast, float* xpf,
+                                     int* tag2slot, unsigned* err, int max_tag, double max_radius,
+                                     const DomView* doms, const int* soff, int ndom, const int* ncur,
+                                     double* ft_zero, int* tile_cnt, int* bins, int* work, int* work_n,
                                      cudaStream_t s) {
     if (nslots <= 0) return cudaSuccess;
-    k_bin_spheres<true><<<(nslots + 7) / 8, 256, 0, s>>>(fast, nslots, tile_cnt, bins, work, work_n, Geom{}, doms,
-                                                         soff, ndom, ncur);
+    k_prepare_bin<true><<<(nslots + 7) / 8, 256, 0, s>>>(rec, nslots, sph, fast, xpf, tag2slot, err, Geom{}, max_tag,
+                                                         max_radius, doms, soff, ndom, ncur, ft_zero, nullptr,
+                                                         tile_cnt, bins, work, work_n);
     return cudaGetLastError();
 }
 

@@ -250,12 +250,10 @@ cudaError_t enqueue_step(lbdem_batch* b, bool odd, int init_vel) {
     if ((e = cudaMemsetAsync(b->d_tag2slot, 0x7F, sizeof(int) * ((size_t)b->cfg.max_tag + 1) * b->ndom, s)) !=
         cudaSuccess)
         return e;
-    if ((e = launch_prepare_spheres_batch(b->d_rec, b->nslots, b->d_sph, b->d_fast, b->d_xpf, b->d_tag2slot, b->d_err,
-                                          b->cfg.max_tag, b->cfg.max_radius, b->d_views, b->d_soff, b->ndom,
-                                          b->d_ncur, b->d_ft, s)) != cudaSuccess)   // also zeroes the sums
-        return e;
-    if ((e = launch_bin_spheres_batch(b->d_fast, b->nslots, b->d_tile_cnt, b->d_bins, b->d_work, b->d_work_n,
-                                      b->d_views, b->d_soff, b->ndom, b->d_ncur, s)) != cudaSuccess)
+    if ((e = launch_prepare_bin_batch(b->d_rec, b->nslots, b->d_sph, b->d_fast, b->d_xpf, b->d_tag2slot, b->d_err,
+                                      b->cfg.max_tag, b->cfg.max_radius, b->d_views, b->d_soff, b->ndom, b->d_ncur,
+                                      b->d_ft, b->d_tile_cnt, b->d_bins, b->d_work, b->d_work_n, s)) !=
+        cudaSuccess)   // also zeroes the force/torque sums
         return e;
     if (b->prec == LBDEM_PREC_FP64)
         e = launch_voxelize_batch<double>(b->d_sph, b->d_fast, b->d_tile_cnt, b->d_bins, b->d_work, b->d_work_n,
@@ -282,7 +280,7 @@ cudaError_t enqueue_step(lbdem_batch* b, bool odd, int init_vel) {
 }
 
 int launches_per_step(const lbdem_batch* b, bool stale) {
-    return 4 + (b->njobs > 0 ? (stale ? 2 : 1) : 0);
+    return 3 + (b->njobs > 0 ? (stale ? 2 : 1) : 0);   // prepare + bin, voxelize, collide-stream, planes
 }
 
 // Collide-stream grid shapes timed on a copy of the populations (the state is

@@ -158,11 +158,10 @@ lbdem_status voxelize(lbdem_handle* h, int n, int init_vel, const double* src) {
     cudaStream_t s = h->stream;
     CK(h, cudaMemsetAsync(h->d_tag2slot, 0x7F, sizeof(int) * ((size_t)h->cfg.max_tag + 1), s));
     if (n > 0) {
-        CK(h, launch_prepare_spheres(src, n, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot, h->d_err, h->g,
-                                     h->cfg.max_tag, h->cfg.max_radius, h->d_ft, src == h->d_rec ? nullptr : h->d_rec,
-                                     s));
+        CK(h, launch_prepare_bin(src, n, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot, h->d_err, h->g,
+                                 h->cfg.max_tag, h->cfg.max_radius, h->d_ft, src == h->d_rec ? nullptr : h->d_rec,
+                                 h->d_tile_cnt, h->d_bins, h->d_work, h->d_work_n, s));
         h->ft_dirty = false;   // the prepare launch zeroed the 6 n sums
-        CK(h, launch_bin_spheres(h->d_fast, n, h->d_tile_cnt, h->d_bins, h->d_work, h->d_work_n, h->g, s));
         const int phase = (int)(h->step & 1);
         if (h->prec == LBDEM_PREC_FP64)
             CK(h, launch_voxelize<double>(h->d_sph, h->d_fast, n, h->d_tile_cnt, h->d_bins, h->d_work, h->d_work_n,
@@ -172,7 +171,7 @@ lbdem_status voxelize(lbdem_handle* h, int n, int init_vel, const double* src) {
             CK(h, launch_voxelize<float>(h->d_sph, h->d_fast, n, h->d_tile_cnt, h->d_bins, h->d_work, h->d_work_n,
                                          h->ntiles, h->vox,
                                          (float*)h->up, (float*)h->f, init_vel, phase, h->g, h->d_err, s));
-        h->launches += 3;
+        h->launches += 2;
         if (init_vel) h->pavg_valid = false;
     }
     h->n_cur = n;

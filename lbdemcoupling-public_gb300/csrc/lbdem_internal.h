@@ -190,17 +190,17 @@ template <typename T>
 cudaError_t launch_collide_batch(const CollideArgs<T>* dargs, const int* seg0, int ndom, long long nseg, bool odd,
                                  bool force, int blocks_per_sm, cudaStream_t s);
 
-// ft_zero (may be null): 6 n doubles set to zero by the same launch (the force
-// and torque sums of the next collide-stream step).  rec_copy (may be null, never
-// overlapping rec): receives a copy of the n records.
-cudaError_t launch_prepare_spheres(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
-                                   int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
-                                   double* ft_zero, double* rec_copy, cudaStream_t s);
-// tile_cnt must be zero on entry; launch_voxelize leaves it zero again.  Every
-// tile that receives a sphere is appended to work[] (work_n counts them; zero
-// on entry, left zero by launch_voxelize).
-cudaError_t launch_bin_spheres(const SphereFast* fast, int n, int* tile_cnt, int* bins, int* work, int* work_n,
-                               Geom g, cudaStream_t s);
+// Sphere tables (sph, fast, xpf), the tag -> lowest slot map (tag2slot must
+// hold "no slot" on entry) and the tile bins, in one launch.  tile_cnt must be
+// zero on entry; launch_voxelize leaves it zero again.  Every tile that receives
+// a sphere is appended to work[] (work_n counts them; zero on entry, left zero
+// by launch_voxelize).  ft_zero (may be null): 6 n doubles set to zero by the
+// same launch (the force and torque sums of the next collide-stream step).
+// rec_copy (may be null, never overlapping rec): receives a copy of the n records.
+cudaError_t launch_prepare_bin(const double* rec, int n, SphereDev* sph, SphereFast* fast, float* xpf,
+                               int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
+                               double* ft_zero, double* rec_copy, int* tile_cnt, int* bins, int* work, int* work_n,
+                               cudaStream_t s);
 template <typename T>
 cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, int n, int* tile_cnt, const int* bins,
                             const int* work, int* work_n, int ntiles, uint32_t* vox, T* up, T* f, int init_vel,
@@ -210,12 +210,10 @@ cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, int n,
 // soff[d] = doms[d].s0, toff[d] = doms[d].t0 (ascending); ncur[d] particles of
 // domain d are in use (slots s0 .. s0 + ncur[d] - 1); tag2slot holds a
 // (max_tag + 1)-entry map per domain, with domain-local slots.
-cudaError_t launch_prepare_spheres_batch(const double* rec, int nslots, SphereDev* sph, SphereFast* fast, float* xpf,
-                                         int* tag2slot, unsigned* err, int max_tag, double max_radius,
-                                         const DomView* doms, const int* soff, int ndom, const int* ncur,
-                                         double* ft_zero, cudaStream_t s);
-cudaError_t launch_bin_spheres_batch(const SphereFast* fast, int nslots, int* tile_cnt, int* bins, int* work,
-                                     int* work_n, const DomView* doms, const int* soff, int ndom, const int* ncur,
+cudaError_t launch_prepare_bin_batch(const double* rec, int nslots, SphereDev* sph, SphereFast* fast, float* xpf,
+                                     int* tag2slot, unsigned* err, int max_tag, double max_radius,
+                                     const DomView* doms, const int* soff, int ndom, const int* ncur,
+                                     double* ft_zero, int* tile_cnt, int* bins, int* work, int* work_n,
                                      cudaStream_t s);
 template <typename T>
 cudaError_t launch_voxelize_batch(const SphereDev* sph, const SphereFast* fast, int* tile_cnt, const int* bins,

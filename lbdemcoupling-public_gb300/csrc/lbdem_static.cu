@@ -98,9 +98,8 @@ extern "C" lbdem_status lbdem_voxelize_static(int32_t nx, int32_t ny, int32_t nz
         cudaMemsetAsync(tag2slot, 0x7F, sizeof(int) * ((size_t)LBDEM_STATIC_MAX_TAG + 1), s) != cudaSuccess)
         return LBDEM_ERR_CUDA;
     if (n == 0) return LBDEM_OK;   // no sphere touches a cell (as in the reference)
-    cudaError_t e = launch_prepare_spheres(dev_rec, n, sph, fast, xpf, tag2slot, dev_err, g,
-                                           LBDEM_STATIC_MAX_TAG, 1024.0, nullptr, nullptr, s);
-    if (e == cudaSuccess) e = launch_bin_spheres(fast, n, tile_cnt, bins, work, work_n, g, s);
+    cudaError_t e = launch_prepare_bin(dev_rec, n, sph, fast, xpf, tag2slot, dev_err, g, LBDEM_STATIC_MAX_TAG, 1024.0,
+                                       nullptr, nullptr, tile_cnt, bins, work, work_n, s);
     if (e == cudaSuccess) {
         if (precision == LBDEM_PREC_FP64)
             e = launch_voxelize<double>(sph, fast, n, tile_cnt, bins, work, work_n, (int)ntiles, dev_vox,
