@@ -111,6 +111,44 @@ def test_mass_conservation_periodic(oracle):
     assert abs(ol.mass() - m0) <= 1e-12 * m0
 
 
+def _momentum(f):
+    c = np.array(pyref.C, dtype=np.float64)
+    return c.T @ np.asarray(f).reshape(19, -1).sum(axis=1)
+
+
+def test_momentum_balance_periodic(oracle):
+    """Periodic box without walls or body force: with no particles the fluid
+    momentum is conserved; with moving spheres, each step changes it by minus
+    the sum of the particle forces (the momentum exchange of the PSM collision,
+    src/ibCompositeDynamics3D.hh:160-200), to rounding."""
+    import workloads as W
+    shape = (14, 12, 16)
+    rng = np.random.default_rng(17)
+    f0 = rng.standard_normal((19, *shape)) * 1e-3
+    ol = oracle.OracleLattice(*shape, 1 / 0.6)
+    ol.set_populations(f0)
+    p0 = _momentum(ol.get_populations())
+    for _ in range(5):
+        ol.collide_and_stream()
+    assert np.abs(_momentum(ol.get_populations()) - p0).max() <= 1e-14 * np.abs(f0).sum()
+
+    ol = oracle.OracleLattice(*shape, 1 / 0.6)
+    ol.set_populations(f0)
+    p = W.suspension(shape, n_max=4, rmin=2.0, rmax=3.5, seed=5, v_std=0.05, w_std=0.01)
+    total = 0.0
+    for s in range(5):
+        g = W.with_ghosts(p, shape)
+        ol.set_particles(g.x, g.v, g.w, g.r, g.tag, init_vel=(s == 0))
+        before = _momentum(ol.get_populations())
+        ol.collide_and_stream()
+        F, _ = ol.get_forces()
+        gain = _momentum(ol.get_populations()) - before
+        total += np.abs(F.sum(axis=0)).max()
+        assert np.abs(gain + F.sum(axis=0)).max() <= 1e-12 * np.abs(F).sum(), s
+        p = W.advance(p, shape)
+    assert total > 1e-6                       # the spheres do exchange momentum
+
+
 def test_mass_conservation_bounce_back_with_sphere(oracle):
     """Walls and a resting sphere in fluid at rest: mass is conserved, and a
     particle at rest in a fluid at rest feels no force."""
