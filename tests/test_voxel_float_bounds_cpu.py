@@ -8,7 +8,7 @@ only when a float value lies within M = 2^-18 (r + 4)^2 of its threshold.  This
 emulates that float arithmetic in IEEE single precision on the CPU (numpy, one
 rounding per operation; with and without the fused multiply-adds the compiler
 may form) and checks, over random spheres up to r = 32 with centres anywhere in
-[0, 2^20):
+[0, 2^23) (the kernel takes |x| < 2^24):
   * |dist_f - dist_d| <= 22 u (r + 3.2)^2 and |t_f - t_d| <= 27 u (r + 3.5)^2,
     u = 2^-24, the bounds the kernel's comment states;
   * M exceeds each bound plus the rounding of the threshold to float;
@@ -45,7 +45,7 @@ def _split(x):
 def _spheres(seed, n):
     rng = np.random.default_rng(seed)
     r = np.concatenate([rng.uniform(0.5, 8.0, n // 2), rng.uniform(8.0, 32.0, n - n // 2)])
-    scale = rng.choice([16.0, 4096.0, 2.0 ** 20], n)
+    scale = rng.choice([16.0, 4096.0, 2.0 ** 20, 2.0 ** 23], n)
     x = rng.uniform(0.0, 1.0, (n, 3)) * scale[:, None]
     return x, r
 
