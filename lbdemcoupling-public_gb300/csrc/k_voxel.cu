@@ -382,8 +382,11 @@ __device__ __forceinline__ void voxelize_tile(VoxSmem<T, INIT_VEL>& S, int t, co
         S.n[l] = (uint8_t)(w0 & VOX_NMASK);
         S.id[l] = w0 >> VOX_NBITS;
         S.flags[l] = 0;
+        // The surface velocity a cell holds is only read back by defineVelocity
+        // (a fully covered cell that no sphere of this pass sets keeps it); the
+        // velocity written back is always the one a set or zero of this pass made.
         T u0 = T(0), u1 = T(0), u2 = T(0);
-        if ((w0 & VOX_NMASK) > 0) {
+        if (INIT_VEL && (w0 & VOX_NMASK) > 0) {
             const size_t c = ((size_t)X * g.ny + Y) * g.nz + Z;
             u0 = up[c]; u1 = up[g.N + c]; u2 = up[2 * g.N + c];
         }
