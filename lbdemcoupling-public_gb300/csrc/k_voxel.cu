@@ -28,8 +28,12 @@
 // FP64 form also reproduces the particle surface velocity bit for bit.
 #include "lbdem_internal.h"
 
+#include <climits>
+
 namespace lbdem {
 namespace {
+
+constexpr unsigned FULL_MASK = 0xffffffffu;
 
 constexpr double SQRT3HALF = 0.8803408430829505;  // sqrt(3.1)/2, src/ibProcessors3D.hh:128-130
 // -0.5 + (i + 0.5) * (1./5.), src/ibProcessors3D.hh:141-147, evaluated in double:
@@ -39,6 +43,15 @@ __device__ __forceinline__ double sub_delta(int i) {
 __device__ __forceinline__ float sub_delta_f(int i) {
     return i == 0 ? -0.4f : i == 1 ? -0.2f : i == 2 ? 0.0f : i == 3 ? 0.2f : 0.4f;
 }
+
+// Single operations with round-to-nearest and no contraction into fused
+// multiply-adds (results independent of how the compiler schedules a kernel).
+__device__ __forceinline__ double mul_rn(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add_rn(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub_rn(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ float mul_rn(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float add_rn(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float sub_rn(float a, float b) { return __fsub_rn(a, b); }
 
 // Region of a cell against the early-out thresholds in the reference's double
 // arithmetic: 0 outside (dist > rp2), 1 inside (dist < rm2), 2 shell.
@@ -270,325 +283,314 @@ __device__ __noinline__ int slice_count_resolve(float dxf, float dyf, float dzf,
     return n;
 }
 
-// Sub-cell count of a shell cell by one thread (all five x-slices), out of line:
-// only taken when a chunk's shell queue is full.
-__device__ __noinline__ uint32_t shell_count_direct(float dxf, float dyf, float dzf, float rsq, float M, int X, int Y,
-                                                    int Z, const SphereDev& s) {
-    uint32_t n = 0;
-#pragma unroll 1
-    for (int i = 0; i < 5; ++i) {
-        bool unsure;
-        int c = slice_count_fast(dxf, dyf, dzf, i, rsq, M, &unsure);
-        if (unsure) c = slice_count_resolve(dxf, dyf, dzf, i, rsq, M, X, Y, Z, s);
-        n += (uint32_t)c;
-    }
-    return n;
-}
+// ---------------------------------------------------------------------------
+// Voxelization, one warp per 8^3 tile.
+//
+// The tile's cell state (voxel words, and per cell the list index of the
+// sphere that last set or cleared it) lives in per-warp shared memory while
+// the tile's spheres are applied in list order.  Lane `lane` handles cells
+// l = lane + 32 j (j = 0..15): the half x-plane j holds x = j >> 1,
+// y = (lane >> 3) + 4 (j & 1), z = lane & 7.  Per sphere (apply_sphere):
+//  1  the half-planes that meet the sphere's box are classified in float
+//     (outside: n = 0, inside: n = 125, shell); comparisons within the float
+//     error band are decided in the reference's double arithmetic; outside and
+//     inside cells are folded through decFlag at once, shell cells queued;
+//  2  all lanes take the queued cells' sub-cell counts, five x-slices (25
+//     samples) per cell, added into per-cell bytes with shared-memory atomics;
+//  3  the queued cells are folded through decFlag.
+// No block-wide barrier is involved, so the warps of a block work on
+// unrelated tiles.  The spheres of a tile come from its bin (at most
+// TILE_BIN, put in ascending list order by repeated warp minima), or, for a
+// tile whose bin overflowed, from a scan of every sphere's box in list order.
+constexpr int VOX_WARPS = 8;                        // warps per block
+constexpr int VOX_THREADS = 32 * VOX_WARPS;
+constexpr int VOX_STAGE = 32;                       // sphere records staged at a time
+constexpr uint32_t SETTER_ZERO = 0xffffffffu;       // the cell was set to zero (setToZero)
+constexpr uint32_t SETTER_KEEP = 0xfffffffeu;       // the cell keeps its state (and velocity)
 
-// Shared memory of one voxelization block.
-constexpr int VOX_THREADS = 256;            // two cells of the 8^3 tile per thread
-constexpr int VOX_CHUNK = 32;               // spheres classified per pass
-constexpr int VOX_QUEUE = 2048;             // shell (sphere, cell) pairs per pass
-constexpr uint32_t N_NONE = 255;            // cell outside the sphere's box
-
-template <typename T, bool INIT_VEL>
-struct VoxSmem {
-    int raw[TILE_LIST_MAX];
-    int sorted[TILE_LIST_MAX];
-    SphereFast q[VOX_CHUNK];
-    uint32_t bm[VOX_CHUNK];                   // tile-local box of sphere k: x, y, z cell masks (8 bits each)
-    uint32_t n4[VOX_CHUNK][TILE_CELLS / 4];   // count of (sphere k, cell), one byte per cell
-    uint16_t queue[VOX_QUEUE];                // (k << 9) | cell of the queued shell pairs
-    T u[3][TILE_CELLS];                       // cell state carried across chunks
-    T d[INIT_VEL ? 3 : 1][INIT_VEL ? TILE_CELLS : 1];
-    uint32_t id[TILE_CELLS];
-    uint8_t n[TILE_CELLS];
-    uint8_t flags[TILE_CELLS];                // bit 0: state changed, bit 1: define velocity
-    int qcount;
-    int cnt;
+// Per-warp shared memory.  setter: the list index of the sphere that last set
+// the cell in this pass (or SETTER_ZERO / SETTER_KEEP); defv (INIT_VEL): the
+// setter code at the cell's last full coverage (defineVelocity), SETTER_ZERO
+// + SETTER_KEEP markers as for setter, DEFV_NONE without full coverage.
+constexpr uint32_t DEFV_NONE = 0xfffffffdu;
+template <bool INIT_VEL>
+struct alignas(16) WarpVox {
+    SphereFast q[VOX_STAGE];                        // staged sphere records
+    int list[TILE_BIN];                             // the tile's spheres in list order
+    uint32_t w[TILE_CELLS];                         // voxel words (n | tag << 7)
+    uint32_t setter[TILE_CELLS];
+    uint32_t defv[INIT_VEL ? TILE_CELLS : 1];
+    uint32_t cnt4[TILE_CELLS / 4];                  // shell sub-cell counts, one byte per cell
+    uint16_t queue[TILE_CELLS];                     // shell cells of the current sphere
 };
 
-__device__ __forceinline__ uint32_t get_n(const uint32_t* row, int l) { return (row[l >> 2] >> (8 * (l & 3))) & 0xffu; }
-__device__ __forceinline__ void set_n(uint32_t* row, int l, uint32_t n) {
-    uint8_t* b = reinterpret_cast<uint8_t*>(row);
-    b[l] = (uint8_t)n;
+// decFlag, src/ibProcessors3D.hh:85-105 (sf > 0.001 <=> n > 0; sf > sf_old <=>
+// n > n_old), for cell l with the sub-cell count n of sphere m.
+template <bool INIT_VEL>
+__device__ __forceinline__ void fold_cell(WarpVox<INIT_VEL>& S, int l, uint32_t n, uint32_t tag, int m) {
+    const uint32_t w = S.w[l];
+    const uint32_t nold = w & VOX_NMASK, idold = w >> VOX_NBITS;
+    const int dec = (n > 0u ? 1 : 0) + (nold > 0u ? 2 : 0);
+    if (dec == 2 && idold == tag) {
+        S.w[l] = 0u;
+        S.setter[l] = SETTER_ZERO;
+    } else if (dec == 1 || (dec == 3 && ((n > nold) || (idold == tag)))) {
+        S.w[l] = n | (tag << VOX_NBITS);
+        S.setter[l] = (uint32_t)m;
+    }
+    // dec == 0 is setToZero on a cell that is already empty
+    // the velocity the cell holds right after this sphere (src/ibProcessors3D.hh:107-108)
+    if (INIT_VEL && n == 125u) S.defv[l] = S.setter[l];
 }
 
-// One block per 8^3 tile, 256 threads.  Spheres are taken in sorted chunks of
-// VOX_CHUNK; each chunk runs three phases separated by block barriers:
-//  A  classify every (sphere, cell) pair in float: outside the box, outside
-//     (n = 0) and inside (n = 125) are final, shell pairs are queued with n = 0;
-//  B  the queue is split into x-slices (25 samples each) and drained by all
-//     threads, slice counts added into the pair's byte with shared atomics;
-//  C  every cell folds the chunk's counts, in sphere order, through decFlag.
-// INIT_VEL: defineVelocity (src/ibCompositeDynamics3D.hh:118-127) is applied
-// with the uPart the cell holds right after each sphere that covers it fully
-// (src/ibProcessors3D.hh:107-108); it depends only on that uPart, so the last
-// such sphere decides the populations written.
+// Steps 1-3 above for sphere m (float record q in shared memory) on the tile at
+// (X0, Y0, Z0).  Out of line: one copy of the code serves both sphere sources.
+template <bool INIT_VEL>
+__device__ __noinline__ void apply_sphere(WarpVox<INIT_VEL>& S, const SphereFast& q, int m,
+                                          const SphereDev* __restrict__ sph, int X0, int Y0, int Z0) {
+    const int lane = threadIdx.x & 31;
+    const int bx0 = max(q.lo[0] - X0, 0), bx1 = min(q.hi[0] - X0, TILE - 1);
+    const int by0 = max(q.lo[1] - Y0, 0), by1 = min(q.hi[1] - Y0, TILE - 1);
+    const int bz0 = max(q.lo[2] - Z0, 0), bz1 = min(q.hi[2] - Z0, TILE - 1);
+    if (bx0 > bx1 || by0 > by1 || bz0 > bz1) return;
+    const float M = q.margin, rp2 = q.rp2, rm2 = q.rm2;
+    const uint32_t tag = (uint32_t)q.tag;
+    const int z = lane & 7, yl = lane >> 3;
+    const bool zin = z >= bz0 && z <= bz1;
+    const float dzf = ((float)(Z0 + z) - q.xh[2]) - q.xl[2];
+    uint8_t* cnt8 = reinterpret_cast<uint8_t*>(S.cnt4);
+    const unsigned below = (1u << lane) - 1u;
+    int qn = 0;
+    // 1: the half-planes j = 2 x + (0 | 1) of the box's x range whose rows meet its y range
+    for (int j = 2 * bx0; j <= 2 * bx1 + 1; ++j) {
+        const int yh = 4 * (j & 1);
+        if (yh > by1 || yh + 3 < by0) continue;
+        const int x = j >> 1, y = yl + yh;
+        int region = -1;
+        if (zin && y >= by0 && y <= by1) {
+            const float dxf = ((float)(X0 + x) - q.xh[0]) - q.xl[0];
+            const float dyf = ((float)(Y0 + y) - q.xh[1]) - q.xl[1];
+            const float distf = (dxf * dxf + dyf * dyf) + dzf * dzf;
+            if (fabsf(distf - rp2) <= M || fabsf(distf - rm2) <= M)
+                region = region_exact(X0 + x, Y0 + y, Z0 + z, sph[m]);
+            else
+                region = distf > rp2 ? 0 : (distf < rm2 ? 1 : 2);
+        }
+        const int l = lane + 32 * j;
+        const unsigned bal = __ballot_sync(FULL_MASK, region == 2);
+        if (region == 2) {
+            S.queue[qn + __popc(bal & below)] = (uint16_t)l;
+            cnt8[l] = 0;
+        } else if (region >= 0) {
+            fold_cell(S, l, region == 1 ? 125u : 0u, tag, m);
+        }
+        qn += __popc(bal);
+    }
+    if (qn == 0) return;
+    __syncwarp();
+    // 2: counts of the queued cells by x-slice
+    for (int u = lane; u < 5 * qn; u += 32) {
+        const int e = u / 5, i = u - 5 * e;
+        const int l = S.queue[e];
+        const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
+        const float dxf = ((float)X - q.xh[0]) - q.xl[0];
+        const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
+        const float dzq = ((float)Z - q.xh[2]) - q.xl[2];
+        bool unsure;
+        int cs = slice_count_fast(dxf, dyf, dzq, i, q.rsq, M, &unsure);
+        if (unsure) cs = slice_count_resolve(dxf, dyf, dzq, i, q.rsq, M, X, Y, Z, sph[m]);
+        if (cs) atomicAdd(&S.cnt4[l >> 2], (uint32_t)cs << (8 * (l & 3)));
+    }
+    __syncwarp();
+    // 3
+    for (int e = lane; e < qn; e += 32) {
+        const int l = S.queue[e];
+        fold_cell(S, l, (uint32_t)cnt8[l], tag, m);
+    }
+    __syncwarp();
+}
+
+// Surface velocity of a cell set by sphere `code` (SETTER_ZERO: zero).
+template <typename T>
+__device__ __forceinline__ void setter_velocity(uint32_t code, const SphereDev* __restrict__ sph,
+                                                const SphereFast* __restrict__ fast, int X, int Y, int Z, T& u0,
+                                                T& u1, T& u2) {
+    if (code == SETTER_ZERO) {
+        u0 = u1 = u2 = T(0);
+    } else if (sizeof(T) == 8) {
+        // setValues, src/ibProcessors3D.hh:163-174 (com == x for single spheres)
+        double a0, a1, a2;
+        surface_velocity(sph[code], X, Y, Z, a0, a1, a2);
+        u0 = T(a0); u1 = T(a1); u2 = T(a2);
+    } else {
+        const SphereFast& q = fast[code];
+        const float dxf = ((float)X - q.xh[0]) - q.xl[0];
+        const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
+        const float dzf = ((float)Z - q.xh[2]) - q.xl[2];
+        u0 = T(add_rn(q.v[0], sub_rn(mul_rn(q.w[1], dzf), mul_rn(q.w[2], dyf))));
+        u1 = T(add_rn(q.v[1], add_rn(mul_rn(-q.w[0], dzf), mul_rn(q.w[2], dxf))));
+        u2 = T(add_rn(q.v[2], sub_rn(mul_rn(q.w[0], dyf), mul_rn(q.w[1], dxf))));
+    }
+}
+
+// One tile by one warp.  up == nullptr: no surface-velocity field is kept.
+// INIT_VEL: defineVelocity (src/ibCompositeDynamics3D.hh:118-127) with the
+// velocity a fully covered cell holds right after the last sphere covering it.
 template <typename T, bool INIT_VEL>
-__device__ __forceinline__ void voxelize_tile(VoxSmem<T, INIT_VEL>& S, int t, const SphereDev* __restrict__ sph,
+__device__ __forceinline__ void voxelize_tile(WarpVox<INIT_VEL>& S, int t, const SphereDev* __restrict__ sph,
                                               const SphereFast* __restrict__ fast, int nsph,
                                               int* __restrict__ tile_cnt, const int* __restrict__ bins,
                                               uint32_t* __restrict__ vox, T* __restrict__ up, T* __restrict__ f,
-                                              int phase, const Geom& g, unsigned* __restrict__ err) {
-    const int tid = threadIdx.x;
+                                              int phase, const Geom& g) {
+    const int lane = threadIdx.x & 31;
     const int tny = tiles_along(g.ny), tnz = tiles_along(g.nz);
     const int tx = t / (tny * tnz);
     const int rem = t - tx * tny * tnz;
     const int ty = rem / tnz;
     const int tz = rem - ty * tnz;
     const int X0 = tx * TILE, Y0 = ty * TILE, Z0 = tz * TILE;
-
-    // the cell-state loads go out first: their latency overlaps the list loads
-    uint32_t wv[2];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int l = tid + h * VOX_THREADS;
-        const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
-        wv[h] = (X < g.nx && Y < g.ny && Z < g.nz) ? vox[((size_t)X * g.ny + Y) * g.nz + Z] : 0u;
-    }
-    int cnt = tile_cnt[t];
-    if (cnt <= 0) return;
-    __syncthreads();
-    if (tid == 0) tile_cnt[t] = 0;   // bins are reused by the next voxelization
+    const int cnt = tile_cnt[t];
+    int a = INT_MAX, b = INT_MAX;      // the lane's bin entries (list indices)
     if (cnt <= TILE_BIN) {
-        for (int k = tid; k < cnt; k += VOX_THREADS) S.raw[k] = bins[(size_t)t * TILE_BIN + k];
+        if (lane < cnt) a = bins[(size_t)t * TILE_BIN + lane];
+        if (lane + 32 < cnt) b = bins[(size_t)t * TILE_BIN + lane + 32];
+    }
+    // cell state; a lane's cells share z and, per plane half, the row
+    const int z = lane & 7, Z = Z0 + z;
+    const bool zok = Z < g.nz;
+#pragma unroll 4
+    for (int j = 0; j < 16; ++j) {
+        const int l = lane + 32 * j;
+        const int X = X0 + (j >> 1), Y = Y0 + (lane >> 3) + 4 * (j & 1);
+        S.w[l] = (zok && X < g.nx && Y < g.ny) ? vox[((size_t)X * g.ny + Y) * g.nz + Z] : 0u;
+        S.setter[l] = SETTER_KEEP;
+        if (INIT_VEL) S.defv[l] = DEFV_NONE;
+    }
+    if (cnt <= 0) return;
+    if (lane == 0) tile_cnt[t] = 0;    // the bins are reused by the next voxelization
+    constexpr int W4 = (int)(sizeof(SphereFast) / 16);
+    const uint4* src = reinterpret_cast<const uint4*>(fast);
+    uint4* dst = reinterpret_cast<uint4*>(S.q);
+    if (cnt <= TILE_BIN) {
+        for (int k = 0; k < cnt; ++k) {
+            const int m = __reduce_min_sync(FULL_MASK, min(a, b));
+            if (a == m) a = INT_MAX;
+            if (b == m) b = INT_MAX;
+            if (lane == 0) S.list[k] = m;
+        }
+        for (int base = 0; base < cnt; base += VOX_STAGE) {
+            const int nst = min(VOX_STAGE, cnt - base);
+            __syncwarp();
+            for (int i = lane; i < W4 * nst; i += 32) {
+                const int e = i / W4;
+                dst[i] = __ldg(src + (size_t)S.list[base + e] * W4 + (i - W4 * e));
+            }
+            __syncwarp();
+            for (int k = 0; k < nst; ++k) apply_sphere(S, S.q[k], S.list[base + k], sph, X0, Y0, Z0);
+        }
     } else {
-        // bin overflow: collect every sphere whose box overlaps this tile
-        if (tid == 0) S.cnt = 0;
-        __syncthreads();
-        for (int i = tid; i < nsph; i += VOX_THREADS) {
-            const SphereFast& q = fast[i];
-            if (q.lo[0] <= X0 + TILE - 1 && q.hi[0] >= X0 && q.lo[1] <= Y0 + TILE - 1 && q.hi[1] >= Y0 &&
-                q.lo[2] <= Z0 + TILE - 1 && q.hi[2] >= Z0 && q.lo[0] <= q.hi[0] && q.lo[1] <= q.hi[1] &&
-                q.lo[2] <= q.hi[2]) {
-                const int pos = atomicAdd(&S.cnt, 1);
-                if (pos < TILE_LIST_MAX) S.raw[pos] = i;
+        // bin overflow: every sphere whose box reaches the tile, in list order
+        for (int base = 0; base < nsph; base += 32) {
+            const int i = base + lane;
+            bool hit = false;
+            if (i < nsph) {
+                const SphereFast& q = fast[i];
+                hit = q.lo[0] <= q.hi[0] && q.lo[1] <= q.hi[1] && q.lo[2] <= q.hi[2] && q.lo[0] <= X0 + TILE - 1 &&
+                      q.hi[0] >= X0 && q.lo[1] <= Y0 + TILE - 1 && q.hi[1] >= Y0 && q.lo[2] <= Z0 + TILE - 1 &&
+                      q.hi[2] >= Z0;
+            }
+            unsigned bal = __ballot_sync(FULL_MASK, hit);
+            while (bal) {
+                const int m = base + __ffs(bal) - 1;
+                bal &= bal - 1u;
+                __syncwarp();
+                if (lane < W4) dst[lane] = __ldg(src + (size_t)m * W4 + lane);
+                __syncwarp();
+                apply_sphere(S, S.q[0], m, sph, X0, Y0, Z0);
             }
         }
-        __syncthreads();
-        cnt = S.cnt;
-        if (cnt > TILE_LIST_MAX) {
-            if (tid == 0) atomicOr(err, 0x1u);  // LBDEM_DEVERR_TILE_LIST
-            return;
-        }
     }
-    // cell state into shared memory
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-        const int l = tid + h * VOX_THREADS;
-        const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
-        const uint32_t w0 = wv[h];
-        S.n[l] = (uint8_t)(w0 & VOX_NMASK);
-        S.id[l] = w0 >> VOX_NBITS;
-        S.flags[l] = 0;
-        // The surface velocity a cell holds is only read back by defineVelocity
-        // (a fully covered cell that no sphere of this pass sets keeps it); the
-        // velocity written back is always the one a set or zero of this pass made.
-        T u0 = T(0), u1 = T(0), u2 = T(0);
-        if (INIT_VEL && (w0 & VOX_NMASK) > 0) {
+    __syncwarp();
+
+    // defineVelocity first: it may need the surface velocity a cell held before this pass
+    if (INIT_VEL) {
+#pragma unroll 1
+        for (int j = 0; j < 16; ++j) {
+            const int l = lane + 32 * j;
+            const uint32_t code = S.defv[l];
+            if (code == DEFV_NONE) continue;
+            const int X = X0 + (j >> 1), Y = Y0 + (lane >> 3) + 4 * (j & 1);
             const size_t c = ((size_t)X * g.ny + Y) * g.nz + Z;
-            u0 = up[c]; u1 = up[g.N + c]; u2 = up[2 * g.N + c];
-        }
-        S.u[0][l] = u0; S.u[1][l] = u1; S.u[2][l] = u2;
-    }
-    __syncthreads();
-    // rank sort by sphere index (the indices of one list are distinct)
-    for (int k = tid; k < cnt; k += VOX_THREADS) {
-        const int vk = S.raw[k];
-        int rank = 0;
-        for (int m = 0; m < cnt; ++m) rank += (S.raw[m] < vk) ? 1 : 0;
-        S.sorted[rank] = vk;
-    }
-
-    for (int base = 0; base < cnt; base += VOX_CHUNK) {
-        const int m = min(VOX_CHUNK, cnt - base);
-        __syncthreads();   // sorted list ready / previous chunk finished with S.q and S.n4
-        {
-            const int words = (int)(sizeof(SphereFast) / 4);
-            for (int k = tid; k < m * words; k += VOX_THREADS) {
-                const int e = k / words, wd = k - e * words;
-                reinterpret_cast<int*>(&S.q[e])[wd] = reinterpret_cast<const int*>(&fast[S.sorted[base + e]])[wd];
+            T d0, d1, d2;
+            if (code == SETTER_KEEP) {
+                d0 = up[c]; d1 = up[g.N + c]; d2 = up[2 * g.N + c];
+            } else {
+                setter_velocity<T>(code, sph, fast, X, Y, Z, d0, d1, d2);
             }
-            if (tid < m) {   // the sphere's box within this tile and the lattice, as cell masks
-                const SphereFast& qs = fast[S.sorted[base + tid]];
-                const int o[3] = {X0, Y0, Z0}, dims[3] = {g.nx, g.ny, g.nz};
-                uint32_t bm = 0;
-#pragma unroll
-                for (int a = 0; a < 3; ++a) {
-                    const int lo = max(qs.lo[a] - o[a], 0);
-                    const int hi = min(min(qs.hi[a] - o[a], TILE - 1), dims[a] - 1 - o[a]);
-                    const uint32_t mk = lo <= hi ? ((0xffu >> (TILE - 1 - hi)) & (0xffu << lo)) & 0xffu : 0u;
-                    bm |= mk << (8 * a);
-                }
-                S.bm[tid] = bm;
-            }
-        }
-        if (tid == 0) S.qcount = 0;
-        __syncthreads();
-        // Phase A
-        for (int k = 0; k < m; ++k) {
-            const SphereFast& q = S.q[k];
-#pragma unroll 1
-            for (int h = 0; h < 2; ++h) {
-                const int l = tid + h * VOX_THREADS;
-                const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
-                uint32_t n = N_NONE;
-                const uint32_t bm = S.bm[k];
-                if ((bm >> (l >> 6)) & (bm >> (8 + ((l >> 3) & 7))) & (bm >> (16 + (l & 7))) & 1u) {
-                    const float dxf = ((float)X - q.xh[0]) - q.xl[0];
-                    const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
-                    const float dzf = ((float)Z - q.xh[2]) - q.xl[2];
-                    const float distf = (dxf * dxf + dyf * dyf) + dzf * dzf;
-                    const float M = q.margin;
-                    int region;
-                    if (fabsf(distf - q.rp2) <= M || fabsf(distf - q.rm2) <= M)
-                        region = region_exact(X, Y, Z, sph[S.sorted[base + k]]);
-                    else
-                        region = distf > q.rp2 ? 0 : (distf < q.rm2 ? 1 : 2);
-                    if (region == 0) {
-                        n = 0;
-                    } else if (region == 1) {
-                        n = 125;
-                    } else {
-                        n = 0;   // the queued slice counts are added to it
-                        const int pos = atomicAdd(&S.qcount, 1);
-                        if (pos < VOX_QUEUE) {
-                            S.queue[pos] = (uint16_t)((k << 9) | l);
-                        } else {
-                            n = shell_count_direct(dxf, dyf, dzf, q.rsq, M, X, Y, Z, sph[S.sorted[base + k]]);
-                        }
-                    }
-                }
-                set_n(S.n4[k], l, n);
-            }
-        }
-        __syncthreads();
-        // Phase B: five x-slices per queued pair
-        {
-            const int qn = min(S.qcount, VOX_QUEUE);
-            for (int wi = tid; wi < 5 * qn; wi += VOX_THREADS) {
-                const int e = wi / 5, i = wi - 5 * e;
-                const int k = S.queue[e] >> 9, l = S.queue[e] & 511;
-                const SphereFast& q = S.q[k];
-                const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
-                const float dxf = ((float)X - q.xh[0]) - q.xl[0];
-                const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
-                const float dzf = ((float)Z - q.xh[2]) - q.xl[2];
-                bool unsure;
-                int c = slice_count_fast(dxf, dyf, dzf, i, q.rsq, q.margin, &unsure);
-                if (unsure) c = slice_count_resolve(dxf, dyf, dzf, i, q.rsq, q.margin, X, Y, Z, sph[S.sorted[base + k]]);
-                if (c) atomicAdd(&S.n4[k][l >> 2], (uint32_t)c << (8 * (l & 3)));
-            }
-        }
-        __syncthreads();
-        // Phase C: decFlag, src/ibProcessors3D.hh:85-105 (sf > 0.001 <=> n > 0; sf > sf_old <=> n > n_old)
-#pragma unroll 1
-        for (int h = 0; h < 2; ++h) {
-            const int l = tid + h * VOX_THREADS;
-            const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
-            uint32_t nold = S.n[l], idold = S.id[l];
-            T u0 = S.u[0][l], u1 = S.u[1][l], u2 = S.u[2][l];
-            uint32_t fl = S.flags[l];
-            for (int k = 0; k < m; ++k) {
-                const uint32_t n = get_n(S.n4[k], l);
-                if (n == N_NONE) continue;
-                const SphereFast& q = S.q[k];
-                const int dec = (n > 0 ? 1 : 0) + (nold > 0 ? 2 : 0);
-                bool set = false, zero = false;
-                if (dec == 1) set = true;
-                else if (dec == 2) zero = (idold == (uint32_t)q.tag);
-                else if (dec == 3) set = (n > nold) || (idold == (uint32_t)q.tag);
-                // dec == 0 is setToZero on a cell that is already empty
-                if (zero) {
-                    nold = 0; idold = 0; u0 = u1 = u2 = T(0); fl |= 1u;
-                } else if (set) {
-                    // setValues, src/ibProcessors3D.hh:163-174 (com == x for single spheres)
-                    if (sizeof(T) == 8) {
-                        double a0, a1, a2;
-                        surface_velocity(sph[S.sorted[base + k]], X, Y, Z, a0, a1, a2);
-                        u0 = T(a0); u1 = T(a1); u2 = T(a2);
-                    } else {
-                        const float dxf = ((float)X - q.xh[0]) - q.xl[0];
-                        const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
-                        const float dzf = ((float)Z - q.xh[2]) - q.xl[2];
-                        u0 = T(q.v[0] + (q.w[1] * dzf - q.w[2] * dyf));
-                        u1 = T(q.v[1] + (-q.w[0] * dzf + q.w[2] * dxf));
-                        u2 = T(q.v[2] + (q.w[0] * dyf - q.w[1] * dxf));
-                    }
-                    nold = n; idold = (uint32_t)q.tag; fl |= 1u;
-                }
-                if (INIT_VEL && n == 125) {
-                    fl |= 2u;
-                    S.d[0][l] = u0; S.d[1][l] = u1; S.d[2][l] = u2;
-                }
-            }
-            S.n[l] = (uint8_t)nold; S.id[l] = idold; S.flags[l] = (uint8_t)fl;
-            S.u[0][l] = u0; S.u[1][l] = u1; S.u[2][l] = u2;
-        }
-    }
-
-    // write back (each thread its own two cells; no barrier needed)
-#pragma unroll 1
-    for (int h = 0; h < 2; ++h) {
-        const int l = tid + h * VOX_THREADS;
-        const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
-        if (X >= g.nx || Y >= g.ny || Z >= g.nz) continue;
-        const size_t c = ((size_t)X * g.ny + Y) * g.nz + Z;
-        const uint32_t fl = S.flags[l];
-        if (fl & 1u) {
-            vox[c] = (uint32_t)S.n[l] | (S.id[l] << VOX_NBITS);
-            up[c] = S.u[0][l]; up[g.N + c] = S.u[1][l]; up[2 * g.N + c] = S.u[2][l];
-        }
-        if (INIT_VEL && (fl & 2u)) {
-            // f̄_i = feq_i(rhoBar = 0, invRho = 1, j = u)
-            const T d0 = S.d[0][l], d1 = S.d[1][l], d2 = S.d[2][l];
-            const T uSqr = d0 * d0 + d1 * d1 + d2 * d2;
+            // f̄_i = feq_i(rhoBar = 0, invRho = 1, j = u), rounded operation by operation
+            // (no contraction), so that every kernel variant writes the same bits
+            const T uSqr = add_rn(add_rn(mul_rn(d0, d0), mul_rn(d1, d1)), mul_rn(d2, d2));
 #pragma unroll
             for (int i = 0; i < Q; ++i) {
-                const T cu = T(cx(i)) * d0 + T(cy(i)) * d1 + T(cz(i)) * d2;
-                const T e = T(wt(i)) * (T(3) * cu + (T(4.5) * cu * cu - T(1.5) * uSqr));
+                const T cu = add_rn(add_rn(mul_rn(T(cx(i)), d0), mul_rn(T(cy(i)), d1)), mul_rn(T(cz(i)), d2));
+                const T e = mul_rn(T(wt(i)), add_rn(mul_rn(T(3), cu),
+                                                    sub_rn(mul_rn(mul_rn(T(4.5), cu), cu), mul_rn(T(1.5), uSqr))));
                 *pop_slot(f, i, X, Y, Z, phase, g) = e;
             }
         }
     }
+    // write back the changed cells
+#pragma unroll 2
+    for (int j = 0; j < 16; ++j) {
+        const int l = lane + 32 * j;
+        const uint32_t code = S.setter[l];
+        if (code == SETTER_KEEP) continue;
+        const int X = X0 + (j >> 1), Y = Y0 + (lane >> 3) + 4 * (j & 1);
+        const size_t c = ((size_t)X * g.ny + Y) * g.nz + Z;
+        vox[c] = S.w[l];
+        if (up != nullptr) {
+            T u0, u1, u2;
+            setter_velocity<T>(code, sph, fast, X, Y, Z, u0, u1, u2);
+            up[c] = u0; up[g.N + c] = u1; up[2 * g.N + c] = u2;
+        }
+    }
 }
 
-// Persistent voxelization: blocks claim tiles of the work list one at a time
-// (work_n[0] tiles listed, work_n[1] claim counter, work_n[2] finished blocks;
-// the last block to finish zeroes all three for the next voxelization).
+// Persistent voxelization: warps claim tiles of the work list one at a time
+// (work_n[0] tiles listed, work_n[1] claim counter, work_n[2] finished warps;
+// the last warp to finish zeroes all three for the next voxelization).
 // BATCH: a listed tile belongs to the domain d with toff[d] <= tile.
 template <typename T, bool INIT_VEL, bool BATCH>
-__global__ void __launch_bounds__(VOX_THREADS, 4)   // 4 blocks per SM (measured best; a few spills)
+__global__ void __launch_bounds__(VOX_THREADS, INIT_VEL ? 2 : 3)
 k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fast, int nsph,
            int* __restrict__ tile_cnt, const int* __restrict__ bins, const int* __restrict__ work,
            int* __restrict__ work_n, uint32_t* __restrict__ vox, T* __restrict__ up, T* __restrict__ f, int phase,
-           Geom g, unsigned* __restrict__ err, const DomView* __restrict__ doms, const int* __restrict__ toff,
-           int ndom, const int* __restrict__ ncur) {
+           Geom g, const DomView* __restrict__ doms, const int* __restrict__ toff, int ndom,
+           const int* __restrict__ ncur) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
-    VoxSmem<T, INIT_VEL>& S = *reinterpret_cast<VoxSmem<T, INIT_VEL>*>(smem_raw);
-    __shared__ int s_item;
+    WarpVox<INIT_VEL>& S = reinterpret_cast<WarpVox<INIT_VEL>*>(smem_raw)[threadIdx.x >> 5];
+    const int lane = threadIdx.x & 31;
     const int nwork = *(volatile int*)work_n;
     for (;;) {
-        __syncthreads();   // previous tile done with S
-        if (threadIdx.x == 0) s_item = atomicAdd(work_n + 1, 1);
-        __syncthreads();
-        const int w = s_item;
+        int w = 0;
+        if (lane == 0) w = atomicAdd(work_n + 1, 1);
+        w = __shfl_sync(FULL_MASK, w, 0);
         if (w >= nwork) break;
         const int tg = work[w];
         if (BATCH) {
             const int d = find_domain(toff, ndom, tg);
             const DomView& D = doms[d];
             voxelize_tile<T, INIT_VEL>(S, tg - D.t0, sph + D.s0, fast + D.s0, __ldg(ncur + d), tile_cnt + D.t0,
-                                       bins + (size_t)D.t0 * TILE_BIN, vox + D.cell0, up + D.up0, f ? f + D.f0 : f,
-                                       phase, D.g, err);
+                                       bins + (size_t)D.t0 * TILE_BIN, vox + D.cell0, up ? up + D.up0 : up,
+                                       f ? f + D.f0 : f, phase, D.g);
         } else {
-            voxelize_tile<T, INIT_VEL>(S, tg, sph, fast, nsph, tile_cnt, bins, vox, up, f, phase, g, err);
+            voxelize_tile<T, INIT_VEL>(S, tg, sph, fast, nsph, tile_cnt, bins, vox, up, f, phase, g);
         }
+        __syncwarp();
     }
-    if (threadIdx.x == 0) {
+    if (lane == 0) {
         __threadfence();
-        if (atomicAdd(work_n + 2, 1) == (int)gridDim.x - 1) {
+        if (atomicAdd(work_n + 2, 1) == (int)(gridDim.x * VOX_WARPS) - 1) {
             work_n[0] = 0;
             work_n[1] = 0;
             work_n[2] = 0;
@@ -628,7 +630,7 @@ cudaError_t launch_vox(const SphereDev* sph, const SphereFast* fast, int n, int*
                        const int* work, int* work_n, int ntiles, uint32_t* vox, T* up, T* f, int phase, Geom g,
                        unsigned* err, const DomView* doms, const int* toff, int ndom, const int* ncur,
                        cudaStream_t s) {
-    constexpr size_t smem = sizeof(VoxSmem<T, INIT_VEL>);
+    constexpr size_t smem = sizeof(WarpVox<INIT_VEL>) * VOX_WARPS;
     static std::atomic<int> cached[LBDEM_MAX_DEVICES];   // per device: persistent grid size
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -648,9 +650,10 @@ cudaError_t launch_vox(const SphereDev* sph, const SphereFast* fast, int n, int*
         blocks = sms * (per_sm > 0 ? per_sm : 1);
         cached[dev].store(blocks, std::memory_order_relaxed);
     }
-    const int grid = ntiles < blocks ? ntiles : blocks;
+    const int need = (ntiles + VOX_WARPS - 1) / VOX_WARPS;
+    const int grid = need < blocks ? need : blocks;
     k_voxelize<T, INIT_VEL, BATCH><<<grid, VOX_THREADS, smem, s>>>(sph, fast, n, tile_cnt, bins, work, work_n, vox, up,
-                                                                  f, phase, g, err, doms, toff, ndom, ncur);
+                                                                  f, phase, g, doms, toff, ndom, ncur);
     return cudaGetLastError();
 }
 
