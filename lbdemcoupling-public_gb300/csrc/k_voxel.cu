@@ -17,7 +17,7 @@
 //   dist = (dx^2 + dy^2) + dz^2  against (r + sqrt(3.1)/2)^2 and (r - sqrt(3.1)/2)^2,
 //   (xs_i + ys_j) + zs_k < r^2   for the 125 sub-cell centres of shell cells.
 // GB300 executes double arithmetic at two lanes per clock per SM, so each
-// comparison is first made in float with a margin M = 2^-18 (r + 4)^2.  For a
+// comparison is first made in float with a margin M = 2^-19 (r + 4)^2.  For a
 // cell inside the box (|dx| < r + 3, centre split x = xh + xl with |x| < 2^24)
 // the float value differs from the double one by at most 27 u (r + 3.5)^2,
 // u = 2^-24 (sample sums), resp. 22 u (r + 3.2)^2 (dist), so a float result
@@ -119,7 +119,7 @@ __device__ __forceinline__ void prepare_sphere(const double* __restrict__ p, int
     q.rm2 = (float)s.rm2;
     q.rsq = (float)s.rsq;
     const float r4 = (float)s.r + 4.0f;
-    q.margin = ldexpf(r4 * r4, -18);
+    q.margin = ldexpf(r4 * r4, -19);
     for (int d = 0; d < 3; ++d) {
         q.lo[d] = s.valid ? s.lo[d] : 1;
         q.hi[d] = s.valid ? s.hi[d] : 0;
@@ -217,33 +217,55 @@ __device__ __forceinline__ void surface_velocity(const SphereDev& s, int X, int 
     u2 = __dadd_rn(s.v[2], __dsub_rn(__dmul_rn(s.w[0], dy), __dmul_rn(s.w[1], dx)));
 }
 
+// Packed pairs of floats for the sample sums.
+__device__ __forceinline__ unsigned long long pk2(float a, float b) {
+    unsigned long long v;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(v) : "f"(a), "f"(b));
+    return v;
+}
+__device__ __forceinline__ unsigned long long add2(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
+__device__ __forceinline__ unsigned long long sub2(unsigned long long a, unsigned long long b) {
+    unsigned long long d;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+    return d;
+}
 // Sub-cell count of one x-slice (i fixed: 25 of the 125 samples) of a shell
-// cell in float; *unsure is set when a sample falls inside the decision band.
+// cell in float, every operation rounded on its own (the error bound of the
+// header holds for this form): the sums t = (xs + ys_j) + zs_k are formed two
+// at a time in packed f32x2 arithmetic, d = t - r^2 (exact near r^2), and a
+// sample is inside when the sign bit of d is set.  *unsure is set when some
+// |d| <= M (a sample inside the decision band).
 __device__ __forceinline__ int slice_count_fast(float dxf, float dyf, float dzf, int i, float rsq, float M,
                                                 bool* unsure) {
-    const float ax = dxf + sub_delta_f(i);
-    const float xs = ax * ax;
+    const float ax = __fadd_rn(dxf, sub_delta_f(i));
+    const float xs = __fmul_rn(ax, ax);
     float ys[5], zs[5];
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
         const float d = sub_delta_f(j);
-        const float ay = dyf + d; ys[j] = ay * ay;
-        const float az = dzf + d; zs[j] = az * az;
+        const float ay = __fadd_rn(dyf, d); ys[j] = __fmul_rn(ay, ay);
+        const float az = __fadd_rn(dzf, d); zs[j] = __fmul_rn(az, az);
     }
-    const float lo = rsq - M, hi = rsq + M;
-    int n_lo = 0, n_hi = 0;
+    const unsigned long long z01 = pk2(zs[0], zs[1]), z23 = pk2(zs[2], zs[3]), r2 = pk2(rsq, rsq);
+    unsigned neg = 0u;
+    float mind = 3.0e38f;
 #pragma unroll
     for (int j = 0; j < 5; ++j) {
-        const float a = xs + ys[j];
-#pragma unroll
-        for (int k = 0; k < 5; ++k) {
-            const float t = a + zs[k];
-            n_lo += t < lo ? 1 : 0;
-            n_hi += t < hi ? 1 : 0;
-        }
+        const float a = __fadd_rn(xs, ys[j]);
+        const unsigned long long a2 = pk2(a, a);
+        const unsigned long long d01 = sub2(add2(a2, z01), r2), d23 = sub2(add2(a2, z23), r2);
+        const float d4 = __fsub_rn(__fadd_rn(a, zs[4]), rsq);
+        const unsigned u0 = (unsigned)d01, u1 = (unsigned)(d01 >> 32), u2 = (unsigned)d23, u3 = (unsigned)(d23 >> 32);
+        neg += (u0 >> 31) + (u1 >> 31) + (u2 >> 31) + (u3 >> 31) + (__float_as_uint(d4) >> 31);
+        mind = fminf(mind, fminf(fminf(fabsf(__uint_as_float(u0)), fabsf(__uint_as_float(u1))),
+                                 fminf(fminf(fabsf(__uint_as_float(u2)), fabsf(__uint_as_float(u3))), fabsf(d4))));
     }
-    *unsure = n_lo != n_hi;
-    return n_lo;
+    *unsure = !(mind > M);
+    return (int)neg;
 }
 
 // The same slice with the samples inside the band decided by the reference's

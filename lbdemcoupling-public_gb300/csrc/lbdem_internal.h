@@ -144,7 +144,7 @@ struct SphereDev {
 struct SphereFast {
     float xh[3], xl[3];      // centre = xh + xl
     float rp2, rm2, rsq;     // thresholds rounded to float
-    float margin;            // decision band half-width, 2^-18 (r + 4)^2
+    float margin;            // decision band half-width, 2^-19 (r + 4)^2
     int lo[3], hi[3];        // empty box: lo > hi
     int tag;
     float v[3], w[3];        // velocity and angular velocity rounded to float

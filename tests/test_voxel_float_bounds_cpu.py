@@ -4,7 +4,7 @@ decides the reference's double comparisons exactly.
 The kernel evaluates, in float, the cell distance (dx^2 + dy^2) + dz^2 and the
 125 sub-cell sums (xs_i + ys_j) + zs_k from the centre split x = xh + xl, and
 falls back to the reference's double sequence (src/ibProcessors3D.hh:128-155)
-only when a float value lies within M = 2^-18 (r + 4)^2 of its threshold.  This
+only when a float value lies within M = 2^-19 (r + 4)^2 of its threshold.  This
 emulates that float arithmetic in IEEE single precision on the CPU (numpy, one
 rounding per operation; with and without the fused multiply-adds the compiler
 may form) and checks, over random spheres up to r = 32 with centres anywhere in
@@ -18,6 +18,7 @@ import numpy as np
 import pytest
 
 U = 2.0 ** -24
+MARGIN_EXP = -19   # M = 2^MARGIN_EXP (r + 4)^2, SphereFast::margin in the kernel
 SQRT3HALF = 0.8803408430829505
 SUB_D = np.array([-0.4, -0.19999999999999996, 0.0, 0.20000000000000007, 0.4])   # double sub-cell offsets
 SUB_F = np.array([-0.4, -0.2, 0.0, 0.2, 0.4], dtype=np.float32)                   # the kernel's float ones
@@ -68,7 +69,7 @@ def test_distance_band_decides_like_double(fused):
         err = np.abs(dist_f - dist_d).max()
         worst = max(worst, err / bound)
         assert err <= bound
-        Mf = np.ldexp(f32((f32(rad) + f32(4.0)) * (f32(rad) + f32(4.0))), -18)
+        Mf = np.ldexp(f32((f32(rad) + f32(4.0)) * (f32(rad) + f32(4.0))), MARGIN_EXP)
         M = float(Mf)
         rp = rad + SQRT3HALF
         rm = rad - SQRT3HALF
@@ -117,12 +118,20 @@ def test_subcell_band_decides_like_double(fused):
         assert np.abs(t_f - t_d).max() <= bound
         rsq_d = rad * rad
         rsq_f = f32(rsq_d)
-        Mf = np.ldexp(f32((f32(rad) + f32(4.0)) * (f32(rad) + f32(4.0))), -18)
+        Mf = np.ldexp(f32((f32(rad) + f32(4.0)) * (f32(rad) + f32(4.0))), MARGIN_EXP)
         lo, hi = rsq_f - Mf, rsq_f + Mf                                  # float, as the kernel forms them
         assert float(rsq_f) - float(lo) > bound + abs(float(rsq_f) - rsq_d)
         assert float(hi) - float(rsq_f) > bound + abs(float(rsq_f) - rsq_d)
         t32 = t_f.astype(np.float32)
-        inside, outside = t32 < lo, ~(t32 < hi)                            # n_lo / n_hi agree: decided
+        # the resolve routine's rule: t < lo counted, t >= hi not, in between in double
+        inside, outside = t32 < lo, ~(t32 < hi)
         assert np.all(t_d[inside] < rsq_d) and not np.any(t_d[outside] < rsq_d)
+        # the fast count's rule: d = t - r^2 in float (exact near r^2); a slice is
+        # decided when every |d| > M, and a sample is inside when d < 0
+        d32 = (t32 - rsq_f).astype(np.float32)
+        sure = np.abs(d32) > Mf
+        assert np.array_equal((d32 < 0)[sure], (t_d < rsq_d)[sure])
+        near = (t32 >= f32(0.5) * rsq_f) & (t32 <= f32(2.0) * rsq_f)          # Sterbenz: d exact
+        assert np.array_equal(d32[near].astype(np.float64), t32[near].astype(np.float64) - float(rsq_f))
         checked += int(inside.sum() + outside.sum())
     assert checked > 10 ** 6
