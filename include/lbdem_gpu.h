@@ -254,20 +254,28 @@ lbdem_status lbdem_init_profile(lbdem_handle* h, int32_t kind, double rho_hi, do
  *   precision    element type of dev_up (lbdem_precision)
  *   n, dev_rec   particle table in device memory, [n][12] doubles as for
  *                lbdem_set_particles_device; n <= LBDEM_STATIC_MAX_SPHERES,
- *                tags 1..LBDEM_STATIC_MAX_TAG
+ *                tags 1..LBDEM_STATIC_MAX_TAG, radii up to LBDEM_STATIC_MAX_RADIUS
+ *                (a larger radius sets LBDEM_DEVERR_RADIUS and the sphere is
+ *                skipped, as on a handle)
  *   dev_vox      [N] voxel words (count n | tag << 7), read and updated
- *   dev_up       [3][N] particle surface velocity, read and updated
+ *   dev_up       [3][N] particle surface velocity.  FP64: read and updated
+ *                (setValues of the reference).  FP32: written in full with the
+ *                velocity the FP32 form's collision recomputes per cell from the
+ *                owner particle (lbdem_get_field of a handle), the arm taken to
+ *                the nearest image along every axis
  *   dev_err      one device word; LBDEM_DEVERR_* bits are OR-ed into it
  *   cuda_stream  stream of the work (NULL: the legacy default stream)
  * Sizes beyond the limits return LBDEM_ERR_CAPACITY before any GPU work.
- * The work is queued and not synchronized.  The first call on a device, with
- * that device current, resolves the array's device address; make that first
- * call before any stream capture.  Every call uses the same array: calls
- * whose GPU work overlaps (on different streams or threads) race on it.  Each
- * call clears the tile counters and the tag map before using them. */
+ * The work is queued and not synchronized.  Every call looks up the array's
+ * device address on the current device (cudaGetSymbolAddress, no GPU work);
+ * the first call on a device may load the library's device code there, so
+ * make that first call before any stream capture.  Every call uses the same
+ * array: calls whose GPU work overlaps (on different streams or threads) race
+ * on it.  Each call clears the tile counters and the tag map before using them. */
 #define LBDEM_STATIC_MAX_SPHERES 4096
 #define LBDEM_STATIC_MAX_TILES 4096
 #define LBDEM_STATIC_MAX_TAG 65535
+#define LBDEM_STATIC_MAX_RADIUS 1024.0
 #define LBDEM_STATIC_SCRATCH_BYTES (3u << 20)
 lbdem_status lbdem_voxelize_static(int32_t nx, int32_t ny, int32_t nz, int32_t precision, int32_t n,
                                    const double* dev_rec, uint32_t* dev_vox, void* dev_up, uint32_t* dev_err,

@@ -343,7 +343,7 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_step(const AdjointArgs<
                     if (sizeof(T) == 8) {
                         d[0] = T((double)x - p[0]); d[1] = T((double)y - p[1]); d[2] = T((double)z - p[2]);
                     } else {
-                        const float4* q4 = reinterpret_cast<const float4*>(A.xpf) + 2 * (size_t)slot;
+                        const float4* q4 = reinterpret_cast<const float4*>(A.xpf + (size_t)slot * XPF_STRIDE);
                         const float4 hq = q4[0], lq = q4[1];
                         d[0] = T(((float)x - hq.x) - hq.w);
                         d[1] = T(((float)y - hq.y) - lq.x);

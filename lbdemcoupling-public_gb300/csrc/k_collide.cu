@@ -18,16 +18,18 @@
 // One kernel implements the step: persistent CTAs of 128 threads whose warps
 // walk 64-cell z-segments.  The 19 population rows of a segment (plus, in the
 // odd phase, the halo element of every c_z != 0 direction), the voxel words and
-// (single lattice) the particle surface-velocity rows are staged in shared
-// memory, double-buffered, so the next segment's bytes are in flight while the
+// (FP64 form, single lattice) the particle surface-velocity rows are staged in
+// shared memory, double-buffered, so the next segment's bytes are in flight while the
 // current one is collided: per-thread 16-byte cp.async with commit groups for
 // FP32 lattices with 16-byte aligned rows, cp.async.bulk on an mbarrier
 // otherwise; rows that are not 16-byte aligned (nz % 4 != 0) are copied in whole
 // 16-byte chunks around the row.  The staged pre-collision values double as
 // fPre of the PSM update.  The FP32 form collides two cells per thread in packed
-// f32x2 arithmetic (collide_segment_pairs); the FP64 form one cell per thread in
-// the reference's double sequence.  The same kernel steps many independent
-// domains in one launch (batch mode).
+// f32x2 arithmetic (collide_segment_pairs) and recomputes the particle surface
+// velocity of its solid cells from the owner particle's row of the float table
+// (no per-cell velocity field); the FP64 form one cell per thread in the
+// reference's double sequence, with the velocity setValues stored.  The same
+// kernel steps many independent domains in one launch (batch mode).
 #include "lbdem_internal.h"
 
 #include <cstddef>
@@ -493,7 +495,7 @@ __device__ __forceinline__ int cell_force_terms(const CollideArgs<T>& a, uint32_
         dz = T((double)z - __ldg(p + 2));
     } else {
         // centre = hi + lo in float: (x - hi) - lo is the arm to ~1 ulp
-        const float4* p = reinterpret_cast<const float4*>(a.xpf) + 2 * (size_t)slot;
+        const float4* p = reinterpret_cast<const float4*>(a.xpf + (size_t)slot * XPF_STRIDE);
         const float4 h = __ldg(p), l = __ldg(p + 1);
         dx = T(((float)x - h.x) - h.w);
         dy = T(((float)y - h.y) - l.x);
@@ -574,7 +576,7 @@ __device__ __forceinline__ void finish_run(const CollideArgs<float>& a, int tag,
         atomicOr(a.err, 0x8u);   // LBDEM_DEVERR_UNMAPPED_TAG
         return;
     }
-    const float4* p = reinterpret_cast<const float4*>(a.xpf) + 2 * (size_t)slot;
+    const float4* p = reinterpret_cast<const float4*>(a.xpf + (size_t)slot * XPF_STRIDE);
     const float4 h = __ldg(p), l = __ldg(p + 1);
     float dx = ((float)sx - h.x) - h.w;
     float dy = ((float)sy - h.y) - l.x;
@@ -639,6 +641,10 @@ __device__ __forceinline__ int pick(int c, int m, int v, int p) { return c < 0 ?
 constexpr int WARPS = COLLIDE_BLOCK / 32;    // warps per CTA
 constexpr int SEGW = COLLIDE_SEGW;          // cells per warp segment (2 per lane)
 constexpr int WAIT_LIMIT = 1 << 22;         // bounded mbarrier wait (iterations of try_wait)
+
+// Surface-velocity rows are staged by the FP64 form of a single lattice only.
+template <typename T, bool BATCH>
+__host__ __device__ constexpr bool stage_up() { return !BATCH && sizeof(T) == 8; }
 
 // 16-byte aligned, so that every warp's stage (at warp * sizeof) keeps the bulk
 // copies' shared-memory destinations on 16-byte boundaries.
@@ -1044,18 +1050,24 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     // result does not depend on the cell it is paired with.
     const Mom2 m = moments2(f);
     F2 Fx = bc(0.f), Fy = bc(0.f), Fz = bc(0.f);
-    auto up2 = [&](int d) -> F2 {
-        if (!STAGE_UP) {
-            const float* p = a.up + (size_t)d * N + own;
-            return pk(v0 ? __ldg(p + za) : 0.f, v1 ? __ldg(p + zb) : 0.f);
+    // particle surface velocity of the lane's solid cells, recomputed from the
+    // owner particle's row of the float table (one row when both cells belong to
+    // the same particle), read after the BGK arithmetic.  (Looking the owners up
+    // before the moment sums, or prefetching the rows, measured slower.)
+    const int s0 = n0 > 0 ? owner_slot(w0, a.tag2slot, a.max_tag, a.nslot) : -1;
+    const int s1 = n1 > 0 ? owner_slot(w1, a.tag2slot, a.max_tag, a.nslot) : -1;
+    F2 up[3] = {bc(0.f), bc(0.f), bc(0.f)};
+    auto solid_velocity = [&]() {
+        float ua[3] = {0.f, 0.f, 0.f}, ub[3] = {0.f, 0.f, 0.f};
+        const int sl = s0 >= 0 ? s0 : s1;
+        if (sl >= 0) {
+            const TableRow r = load_row(a.xpf, sl);
+            if (s0 >= 0) row_velocity(r, sx, sy, za, g, ua[0], ua[1], ua[2]);
+            if (s1 == sl) row_velocity(r, sx, sy, zb, g, ub[0], ub[1], ub[2]);
         }
-        const int mu = MIS ? (int)((lead >> (40 + 2 * d)) & 3u) : 0;
-        const float* p = &st.up[b][d][mu];
-        if (ADJ) {
-            const float2 t = *reinterpret_cast<const float2*>(p + j0);
-            return pk(t.x, t.y);
-        }
-        return pk(p[j0], p[j1]);
+        if (s1 >= 0 && s1 != sl) row_velocity(load_row(a.xpf, s1), sx, sy, zb, g, ub[0], ub[1], ub[2]);
+#pragma unroll
+        for (int d = 0; d < 3; ++d) up[d] = pk(ua[d], ub[d]);
     };
     // FORCE: the solid correction's momentum is the BGK post-collision one, j + rho g,
     // for the cells that ran BGK
@@ -1063,9 +1075,10 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
         return FORCE ? pk(n0 < 125 ? 1.f : 0.f, n1 < 125 ? 1.f : 0.f) * (bc(1.f) + m.rhoBar) : bc(0.f);
     };
     if constexpr (MIS) {
-        if (__any_sync(FULL, n0 > 0 || n1 > 0))   // one pass; a no-op for the lanes' fluid cells
-            bgk_psm2<FORCE>(f, m, a.omega, a.g3[0], a.g3[1], a.g3[2], hsol(), up2(0), up2(1), up2(2), B, Fx, Fy, Fz);
-        else
+        if (__any_sync(FULL, n0 > 0 || n1 > 0)) {   // one pass; a no-op for the lanes' fluid cells
+            if (n0 > 0 || n1 > 0) solid_velocity();
+            bgk_psm2<FORCE>(f, m, a.omega, a.g3[0], a.g3[1], a.g3[2], hsol(), up[0], up[1], up[2], B, Fx, Fy, Fz);
+        } else
             bgk2<FORCE>(f, m, a.omega, a.g3[0], a.g3[1], a.g3[2]);
     } else {
         bgk2<FORCE>(f, m, a.omega, a.g3[0], a.g3[1], a.g3[2]);
@@ -1073,8 +1086,9 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
             const F2 hs = hsol();
             const F2 sjx = fma2(hs, bc(a.g3[0]), m.jx), sjy = fma2(hs, bc(a.g3[1]), m.jy),
                      sjz = fma2(hs, bc(a.g3[2]), m.jz);
-            if (FORCE) psm2(f, m.rhoBar, sjx, sjy, sjz, m.invRho, up2(0), up2(1), up2(2), B, at2, Fx, Fy, Fz);
-            else psm2(f, m.rhoBar, m.jx, m.jy, m.jz, m.invRho, up2(0), up2(1), up2(2), B, at2, Fx, Fy, Fz);
+            solid_velocity();
+            if (FORCE) psm2(f, m.rhoBar, sjx, sjy, sjz, m.invRho, up[0], up[1], up[2], B, at2, Fx, Fy, Fz);
+            else psm2(f, m.rhoBar, m.jx, m.jy, m.jz, m.invRho, up[0], up[1], up[2], B, at2, Fx, Fy, Fz);
         }
     }
 
@@ -1191,10 +1205,11 @@ __global__ void __launch_bounds__(COLLIDE_BLOCK, sizeof(T) == 4 ? 4 : 2)
 k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* __restrict__ dargs,
                  const int* __restrict__ seg0, int ndom) {
     constexpr int V = WarpStage<T>::V;
-    // surface-velocity rows staged with the populations for a single lattice; the
-    // many short rows of a batch read them directly (three more small copies per
-    // segment cost more there than the loads they replace)
-    constexpr bool STAGE_UP = !BATCH;
+    // FP64 form: surface-velocity rows staged with the populations for a single
+    // lattice; the many short rows of a batch read them directly (three more small
+    // copies per segment cost more there than the loads they replace).  The FP32
+    // form keeps no velocity field (it recomputes the velocity per solid cell).
+    constexpr bool STAGE_UP = stage_up<T, BATCH>();
     // FP32 form, aligned rows of a single lattice: staging by per-thread cp.async
     constexpr bool LSU = sizeof(T) == 4 && !MIS && !BATCH;
     extern __shared__ __align__(16) unsigned char smem_raw[];
@@ -1341,7 +1356,7 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
 template <typename T, bool ODD, bool FORCE, bool PER, bool MIS, bool BATCH>
 cudaError_t launch_staged(const CollideArgs<T>& a, long long nseg, const CollideArgs<T>* dargs,
                           const int* seg0, int ndom, int blocks_per_sm, cudaStream_t s) {
-    constexpr size_t smem = WARPS * sizeof(WarpStage<T, !BATCH>);
+    constexpr size_t smem = WARPS * sizeof(WarpStage<T, stage_up<T, BATCH>()>);
     if (nseg >= (1LL << 31)) return cudaErrorInvalidValue;   // segment indices are split in 32 bits
     // per device: (resident blocks per SM << 16) | SM count, 0 until first use there
     static std::atomic<int> shape[LBDEM_MAX_DEVICES];

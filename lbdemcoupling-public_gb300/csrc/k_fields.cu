@@ -122,6 +122,25 @@ inline unsigned grid_for(size_t n, int threads) {
     return (unsigned)(b < cap ? (b > 0 ? b : 1) : cap);
 }
 
+// Particle surface velocity field of the float form, [3][N]: the velocity the
+// collision uses, recomputed per solid cell from its owner's float-table row
+// (zero in free cells and in cells whose tag has no particle).
+__global__ void k_owner_velocity(const uint32_t* __restrict__ vox, const int* __restrict__ tag2slot, int max_tag,
+                                 int nslot, const float* __restrict__ xpf, Geom g, float* __restrict__ out) {
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < g.N; c += (size_t)gridDim.x * blockDim.x) {
+        float u0 = 0.f, u1 = 0.f, u2 = 0.f;
+        const int slot = owner_slot(vox[c], tag2slot, max_tag, nslot);
+        if (slot >= 0) {
+            int x, y, z;
+            decompose(c, g, x, y, z);
+            table_velocity(xpf + (size_t)slot * XPF_STRIDE, x, y, z, g, u0, u1, u2);
+        }
+        out[c] = u0;
+        out[g.N + c] = u1;
+        out[2 * g.N + c] = u2;
+    }
+}
+
 }  // namespace
 
 template <typename T>
@@ -158,6 +177,11 @@ cudaError_t launch_macro(const T* f, int phase, double* rho, double* u, Geom g, 
 template <typename T>
 cudaError_t launch_mass(const T* f, double* out, Geom g, cudaStream_t s) {
     k_mass<T><<<grid_for((size_t)Q * g.N, MASS_THREADS), MASS_THREADS, 0, s>>>(f, out, g);
+    return cudaGetLastError();
+}
+cudaError_t launch_owner_velocity(const uint32_t* vox, const int* tag2slot, int max_tag, int nslot, const float* xpf,
+                                  Geom g, float* out, cudaStream_t s) {
+    k_owner_velocity<<<grid_for(g.N, 256), 256, 0, s>>>(vox, tag2slot, max_tag, nslot, xpf, g, out);
     return cudaGetLastError();
 }
 cudaError_t launch_vox_fields(const uint32_t* vox, double* sf, int32_t* id, uint8_t* nsub, Geom g, cudaStream_t s) {

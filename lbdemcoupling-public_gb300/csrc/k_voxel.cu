@@ -132,9 +132,11 @@ __device__ __forceinline__ void prepare_sphere(const double* __restrict__ p, int
     q.pad = 0;
     sph[i] = s;
     fast[i] = q;
-    float* xp = xpf + (size_t)i * 8;
-    xp[0] = q.xh[0]; xp[1] = q.xh[1]; xp[2] = q.xh[2]; xp[3] = q.xl[0];
-    xp[4] = q.xl[1]; xp[5] = q.xl[2]; xp[6] = 0.f; xp[7] = 0.f;
+    float4* xp = reinterpret_cast<float4*>(xpf + (size_t)i * XPF_STRIDE);
+    xp[0] = make_float4(q.xh[0], q.xh[1], q.xh[2], q.xl[0]);
+    xp[1] = make_float4(q.xl[1], q.xl[2], q.v[0], q.v[1]);
+    xp[2] = make_float4(q.v[2], q.w[0], q.w[1], q.w[2]);
+    xp[3] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (s.tag >= 1) atomicMin(tag2slot + s.tag, il);
 }
 
@@ -463,7 +465,7 @@ __device__ __forceinline__ void voxelize_tile(WarpVox<INIT_VEL>& S, int t, const
                                               const SphereFast* __restrict__ fast, int nsph,
                                               int* __restrict__ tile_cnt, const int* __restrict__ bins,
                                               uint32_t* __restrict__ vox, T* __restrict__ up, T* __restrict__ f,
-                                              int phase, const Geom& g) {
+                                              int phase, const Geom& g, const OwnerTable& ot) {
     const int lane = threadIdx.x & 31;
     const int tny = tiles_along(g.ny), tnz = tiles_along(g.nz);
     const int tx = t / (tny * tnz);
@@ -544,8 +546,16 @@ __device__ __forceinline__ void voxelize_tile(WarpVox<INIT_VEL>& S, int t, const
             const int X = X0 + (j >> 1), Y = Y0 + (lane >> 3) + 4 * (j & 1);
             const size_t c = ((size_t)X * g.ny + Y) * g.nz + Z;
             T d0, d1, d2;
-            if (code == SETTER_KEEP) {
+            if (code == SETTER_KEEP && up != nullptr) {
                 d0 = up[c]; d1 = up[g.N + c]; d2 = up[2 * g.N + c];
+            } else if (code == SETTER_KEEP) {
+                // no velocity field (float form): the velocity of the cell's
+                // unchanged owner, recomputed as the collision does
+                d0 = d1 = d2 = T(0);
+                if constexpr (sizeof(T) == 4) {
+                    const int slot = owner_slot(vox[c], ot.tag2slot, ot.max_tag, nsph);
+                    if (slot >= 0) table_velocity(ot.xpf + (size_t)slot * XPF_STRIDE, X, Y, Z, g, d0, d1, d2);
+                }
             } else {
                 setter_velocity<T>(code, sph, fast, X, Y, Z, d0, d1, d2);
             }
@@ -588,7 +598,7 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
            int* __restrict__ tile_cnt, const int* __restrict__ bins, const int* __restrict__ work,
            int* __restrict__ work_n, uint32_t* __restrict__ vox, T* __restrict__ up, T* __restrict__ f, int phase,
            Geom g, const DomView* __restrict__ doms, const int* __restrict__ toff, int ndom,
-           const int* __restrict__ ncur) {
+           const int* __restrict__ ncur, OwnerTable ot) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WarpVox<INIT_VEL>& S = reinterpret_cast<WarpVox<INIT_VEL>*>(smem_raw)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
@@ -602,11 +612,12 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
         if (BATCH) {
             const int d = find_domain(toff, ndom, tg);
             const DomView& D = doms[d];
+            const OwnerTable od{ot.xpf + (size_t)XPF_STRIDE * D.s0, ot.tag2slot + D.tag0, ot.max_tag};
             voxelize_tile<T, INIT_VEL>(S, tg - D.t0, sph + D.s0, fast + D.s0, __ldg(ncur + d), tile_cnt + D.t0,
                                        bins + (size_t)D.t0 * TILE_BIN, vox + D.cell0, up ? up + D.up0 : up,
-                                       f ? f + D.f0 : f, phase, D.g);
+                                       f ? f + D.f0 : f, phase, D.g, od);
         } else {
-            voxelize_tile<T, INIT_VEL>(S, tg, sph, fast, nsph, tile_cnt, bins, vox, up, f, phase, g);
+            voxelize_tile<T, INIT_VEL>(S, tg, sph, fast, nsph, tile_cnt, bins, vox, up, f, phase, g, ot);
         }
         __syncwarp();
     }
@@ -650,7 +661,7 @@ namespace {
 template <typename T, bool INIT_VEL, bool BATCH>
 cudaError_t launch_vox(const SphereDev* sph, const SphereFast* fast, int n, int* tile_cnt, const int* bins,
                        const int* work, int* work_n, int ntiles, uint32_t* vox, T* up, T* f, int phase, Geom g,
-                       unsigned* err, const DomView* doms, const int* toff, int ndom, const int* ncur,
+                       const DomView* doms, const int* toff, int ndom, const int* ncur, const OwnerTable& ot,
                        cudaStream_t s) {
     constexpr size_t smem = sizeof(WarpVox<INIT_VEL>) * VOX_WARPS;
     static std::atomic<int> cached[LBDEM_MAX_DEVICES];   // per device: persistent grid size
@@ -675,7 +686,7 @@ cudaError_t launch_vox(const SphereDev* sph, const SphereFast* fast, int n, int*
     const int need = (ntiles + VOX_WARPS - 1) / VOX_WARPS;
     const int grid = need < blocks ? need : blocks;
     k_voxelize<T, INIT_VEL, BATCH><<<grid, VOX_THREADS, smem, s>>>(sph, fast, n, tile_cnt, bins, work, work_n, vox, up,
-                                                                  f, phase, g, doms, toff, ndom, ncur);
+                                                                  f, phase, g, doms, toff, ndom, ncur, ot);
     return cudaGetLastError();
 }
 
@@ -684,34 +695,35 @@ cudaError_t launch_vox(const SphereDev* sph, const SphereFast* fast, int n, int*
 template <typename T>
 cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, int n, int* tile_cnt, const int* bins,
                             const int* work, int* work_n, int ntiles, uint32_t* vox, T* up, T* f, int init_vel,
-                            int odd_phase, Geom g, unsigned* err, cudaStream_t s) {
+                            int odd_phase, Geom g, const OwnerTable& ot, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
     if (init_vel)
         return launch_vox<T, true, false>(sph, fast, n, tile_cnt, bins, work, work_n, ntiles, vox, up, f, odd_phase, g,
-                                          err, nullptr, nullptr, 0, nullptr, s);
+                                          nullptr, nullptr, 0, nullptr, ot, s);
     return launch_vox<T, false, false>(sph, fast, n, tile_cnt, bins, work, work_n, ntiles, vox, up, f, odd_phase, g,
-                                       err, nullptr, nullptr, 0, nullptr, s);
+                                       nullptr, nullptr, 0, nullptr, ot, s);
 }
 
 template <typename T>
 cudaError_t launch_voxelize_batch(const SphereDev* sph, const SphereFast* fast, int* tile_cnt, const int* bins,
                                   const int* work, int* work_n, int ntiles, uint32_t* vox, T* up, T* f, int init_vel,
                                   int odd_phase, const DomView* doms, const int* toff, int ndom, const int* ncur,
-                                  unsigned* err, cudaStream_t s) {
+                                  const OwnerTable& ot, cudaStream_t s) {
     if (ntiles <= 0) return cudaSuccess;
     if (init_vel)
         return launch_vox<T, true, true>(sph, fast, 0, tile_cnt, bins, work, work_n, ntiles, vox, up, f, odd_phase,
-                                         Geom{}, err, doms, toff, ndom, ncur, s);
+                                         Geom{}, doms, toff, ndom, ncur, ot, s);
     return launch_vox<T, false, true>(sph, fast, 0, tile_cnt, bins, work, work_n, ntiles, vox, up, f, odd_phase,
-                                      Geom{}, err, doms, toff, ndom, ncur, s);
+                                      Geom{}, doms, toff, ndom, ncur, ot, s);
 }
 
 #define INST(T)                                                                                                    \
     template cudaError_t launch_voxelize<T>(const SphereDev*, const SphereFast*, int, int*, const int*, const int*, \
-                                            int*, int, uint32_t*, T*, T*, int, int, Geom, unsigned*, cudaStream_t); \
+                                            int*, int, uint32_t*, T*, T*, int, int, Geom, const OwnerTable&,       \
+                                            cudaStream_t);                                                         \
     template cudaError_t launch_voxelize_batch<T>(const SphereDev*, const SphereFast*, int*, const int*,          \
                                                   const int*, int*, int, uint32_t*, T*, T*, int, int,              \
-                                                  const DomView*, const int*, int, const int*, unsigned*,          \
+                                                  const DomView*, const int*, int, const int*, const OwnerTable&,  \
                                                   cudaStream_t);
 INST(float)
 INST(double)

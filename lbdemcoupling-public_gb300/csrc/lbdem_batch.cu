@@ -198,11 +198,11 @@ void fill_dargs(lbdem_batch* b, std::vector<CollideArgs<T>>& out, T* f_base, dou
         a.f = f_base + v.f0;
         a.fo = a.f;
         a.vox = b->vox + v.cell0;
-        a.up = (const T*)b->up + v.up0;
+        a.up = b->up ? (const T*)b->up + v.up0 : nullptr;   // FP64 form only
         a.cf = nullptr;
         a.tag2slot = b->d_tag2slot + v.tag0;
         a.rec = b->d_rec + (size_t)REC_STRIDE * v.s0;
-        a.xpf = b->d_xpf + (size_t)8 * v.s0;
+        a.xpf = b->d_xpf + (size_t)XPF_STRIDE * v.s0;
         a.nslot = b->cap[d];
         a.max_tag = b->cfg.max_tag;
         a.ft = ft_base + (size_t)6 * v.s0;
@@ -258,11 +258,13 @@ cudaError_t enqueue_step(lbdem_batch* b, bool odd, int init_vel) {
     if (b->prec == LBDEM_PREC_FP64)
         e = launch_voxelize_batch<double>(b->d_sph, b->d_fast, b->d_tile_cnt, b->d_bins, b->d_work, b->d_work_n,
                                           b->ntiles, b->vox, (double*)b->up, (double*)b->f, init_vel, P, b->d_views,
-                                          b->d_toff, b->ndom, b->d_ncur, b->d_err, s);
+                                          b->d_toff, b->ndom, b->d_ncur,
+                                          OwnerTable{b->d_xpf, b->d_tag2slot, b->cfg.max_tag}, s);
     else
         e = launch_voxelize_batch<float>(b->d_sph, b->d_fast, b->d_tile_cnt, b->d_bins, b->d_work, b->d_work_n,
-                                         b->ntiles, b->vox, (float*)b->up, (float*)b->f, init_vel, P, b->d_views,
-                                         b->d_toff, b->ndom, b->d_ncur, b->d_err, s);
+                                         b->ntiles, b->vox, nullptr, (float*)b->f, init_vel, P, b->d_views,
+                                         b->d_toff, b->ndom, b->d_ncur,
+                                         OwnerTable{b->d_xpf, b->d_tag2slot, b->cfg.max_tag}, s);
     if (e != cudaSuccess) return e;
     if (b->njobs > 0 && !b->pavg_valid) {
         if ((e = launch_planes(b, P, 0, nullptr, b->d_pavg + (size_t)b->njobs * P)) != cudaSuccess) return e;
@@ -487,7 +489,7 @@ lbdem_status lbdem_batch_create(const lbdem_batch_config* cfg, int32_t ndomains,
     const size_t capn = (size_t)std::max(b->nslots, 1);
     TRY(dalloc(b, &b->f, b->f_elems * b->esz + ALLOC_TAIL));
     TRY(dalloc(b, &b->vox, b->vox_elems * sizeof(uint32_t) + ALLOC_TAIL));
-    TRY(dalloc(b, &b->up, b->up_elems * b->esz + ALLOC_TAIL));
+    if (b->prec == LBDEM_PREC_FP64) TRY(dalloc(b, &b->up, b->up_elems * b->esz + ALLOC_TAIL));
     TRY(dalloc(b, &b->btab, (size_t)126 * ndomains * b->esz));
     b->rec_off = round_up(sizeof(int) * (size_t)ndomains, 16);
     b->stage_bytes = b->rec_off + capn * REC_STRIDE * sizeof(double);
@@ -496,7 +498,7 @@ lbdem_status lbdem_batch_create(const lbdem_batch_config* cfg, int32_t ndomains,
     b->d_rec = (double*)(b->d_stage + b->rec_off);
     TRY(dalloc(b, &b->d_sph, capn * sizeof(SphereDev)));
     TRY(dalloc(b, &b->d_fast, capn * sizeof(SphereFast)));
-    TRY(dalloc(b, &b->d_xpf, capn * 8 * sizeof(float)));
+    TRY(dalloc(b, &b->d_xpf, capn * XPF_STRIDE * sizeof(float)));
     TRY(dalloc(b, &b->d_tag2slot, sizeof(int) * ((size_t)c.max_tag + 1) * ndomains));
     TRY(dalloc(b, &b->d_tile_cnt, sizeof(int) * (size_t)std::max(b->ntiles, 1)));
     TRY(dalloc(b, &b->d_bins, sizeof(int) * TILE_BIN * (size_t)std::max(b->ntiles, 1)));
@@ -517,7 +519,7 @@ lbdem_status lbdem_batch_create(const lbdem_batch_config* cfg, int32_t ndomains,
 
     TRY(cudaMemset(b->f, 0, b->f_elems * b->esz + ALLOC_TAIL));
     TRY(cudaMemset(b->vox, 0, b->vox_elems * sizeof(uint32_t) + ALLOC_TAIL));
-    TRY(cudaMemset(b->up, 0, b->up_elems * b->esz));
+    if (b->up) TRY(cudaMemset(b->up, 0, b->up_elems * b->esz));
     TRY(cudaMemset(b->d_tile_cnt, 0, sizeof(int) * (size_t)std::max(b->ntiles, 1)));
     TRY(cudaMemset(b->d_work_n, 0, sizeof(int) * 4));
     TRY(cudaMemset(b->d_err, 0, sizeof(unsigned)));
@@ -782,7 +784,15 @@ lbdem_status lbdem_batch_get_field(lbdem_batch* b, int32_t domain, int32_t which
             break;
         }
         case LBDEM_FIELD_PARTICLE_VELOCITY:
-            BK(b, cudaMemcpyAsync(host_buf, (char*)b->up + v.up0 * b->esz, 3 * N * b->esz, cudaMemcpyDeviceToHost, s));
+            if (b->up) {
+                BK(b, cudaMemcpyAsync(host_buf, (char*)b->up + v.up0 * b->esz, 3 * N * b->esz, cudaMemcpyDeviceToHost,
+                                      s));
+            } else {   // FP32 form: recomputed from the owner particles of the domain's list
+                BK(b, launch_owner_velocity(b->vox + v.cell0, b->d_tag2slot + v.tag0, b->cfg.max_tag, b->cap[domain],
+                                            b->d_xpf + (size_t)XPF_STRIDE * v.s0, v.g, (float*)b->scratch, s));
+                b->launches += 1;
+                BK(b, cudaMemcpyAsync(host_buf, b->scratch, 3 * N * sizeof(float), cudaMemcpyDeviceToHost, s));
+            }
             break;
         case LBDEM_FIELD_DENSITY:
         case LBDEM_FIELD_VELOCITY: {

@@ -25,7 +25,8 @@ struct lbdem_handle {
 
     void* f = nullptr;          // [19][N] populations
     uint32_t* vox = nullptr;    // [N] n | tag << 7
-    void* up = nullptr;         // [3][N]
+    void* up = nullptr;         // [3][N] particle surface velocity (FP64 form only; the FP32
+                                // form recomputes it from the owner particle)
     void* cf = nullptr;         // [3][N] optional
     double* btab = nullptr;     // [126] B(n), double
     float* btabf = nullptr;     // [126] B(n) rounded to float
@@ -34,7 +35,7 @@ struct lbdem_handle {
     double* d_rec = nullptr;    // [cap][12]
     SphereDev* d_sph = nullptr; // [cap]
     SphereFast* d_fast = nullptr; // [cap]
-    float* d_xpf = nullptr;     // [cap][8]
+    float* d_xpf = nullptr;     // [cap][XPF_STRIDE]
     int* d_tag2slot = nullptr;  // [max_tag + 1]
     int ntiles = 0;
     int* d_tile_cnt = nullptr;  // [ntiles] spheres binned per tile (zero between calls)
@@ -156,6 +157,17 @@ lbdem_status wait_staging(lbdem_handle* h) {
 // caller that the prepare launch copies into h->d_rec as it reads it).
 lbdem_status voxelize(lbdem_handle* h, int n, int init_vel, const double* src) {
     cudaStream_t s = h->stream;
+    // defineVelocity reads the velocity a covered cell held before this pass.  The
+    // FP32 form keeps no velocity field: rebuild it, as the collision saw it, from
+    // the previous list's tables before the prepare launch replaces them.
+    float* up_before = nullptr;
+    if (init_vel && n > 0 && h->prec == LBDEM_PREC_FP32_DEV) {
+        lbdem_status st = ensure_scratch(h, 3 * h->g.N * sizeof(float));
+        if (st != LBDEM_OK) return st;
+        up_before = (float*)h->scratch;
+        CK(h, launch_owner_velocity(h->vox, h->d_tag2slot, h->cfg.max_tag, h->n_cur, h->d_xpf, h->g, up_before, s));
+        h->launches += 1;
+    }
     CK(h, cudaMemsetAsync(h->d_tag2slot, 0x7F, sizeof(int) * ((size_t)h->cfg.max_tag + 1), s));
     if (n > 0) {
         CK(h, launch_prepare_bin(src, n, h->d_sph, h->d_fast, h->d_xpf, h->d_tag2slot, h->d_err, h->g,
@@ -165,12 +177,12 @@ lbdem_status voxelize(lbdem_handle* h, int n, int init_vel, const double* src) {
         const int phase = (int)(h->step & 1);
         if (h->prec == LBDEM_PREC_FP64)
             CK(h, launch_voxelize<double>(h->d_sph, h->d_fast, n, h->d_tile_cnt, h->d_bins, h->d_work, h->d_work_n,
-                                          h->ntiles, h->vox,
-                                          (double*)h->up, (double*)h->f, init_vel, phase, h->g, h->d_err, s));
+                                          h->ntiles, h->vox, (double*)h->up, (double*)h->f, init_vel, phase, h->g,
+                                          OwnerTable{h->d_xpf, h->d_tag2slot, h->cfg.max_tag}, s));
         else
             CK(h, launch_voxelize<float>(h->d_sph, h->d_fast, n, h->d_tile_cnt, h->d_bins, h->d_work, h->d_work_n,
-                                         h->ntiles, h->vox,
-                                         (float*)h->up, (float*)h->f, init_vel, phase, h->g, h->d_err, s));
+                                         h->ntiles, h->vox, up_before, (float*)h->f, init_vel, phase, h->g,
+                                         OwnerTable{h->d_xpf, h->d_tag2slot, h->cfg.max_tag}, s));
         h->launches += 2;
         if (init_vel) h->pavg_valid = false;
     }
@@ -225,7 +237,7 @@ cudaError_t k1_launch(lbdem_handle* h, void* fin, void* fout) {
         return launch_collide_stream<double>(a, odd, force, h->stream);
     }
     CollideArgs<float> a;
-    a.g = h->g; a.f = (float*)fin; a.fo = (float*)fout; a.vox = h->vox; a.up = (const float*)h->up;
+    a.g = h->g; a.f = (float*)fin; a.fo = (float*)fout; a.vox = h->vox; a.up = nullptr;
     a.cf = (float*)h->cf; a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.xpf = h->d_xpf; a.nslot = n;
     a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err; a.btab = h->btabf; a.omega = (float)h->cfg.omega;
     for (int d = 0; d < 3; ++d) a.g3[d] = (float)h->cfg.body_force[d];
@@ -336,7 +348,7 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     TRY(cudaEventCreateWithFlags(&h->ev_staged, cudaEventDisableTiming));
     TRY(dalloc(h, &h->f, (size_t)Q * N * h->esz + ALLOC_TAIL));
     TRY(dalloc(h, &h->vox, N * sizeof(uint32_t) + ALLOC_TAIL));
-    TRY(dalloc(h, &h->up, 3 * N * h->esz + ALLOC_TAIL));
+    if (h->prec == LBDEM_PREC_FP64) TRY(dalloc(h, &h->up, 3 * N * h->esz + ALLOC_TAIL));
     if (c.flags & LBDEM_FLAG_CELL_FORCE) TRY(dalloc(h, &h->cf, 3 * N * h->esz));
     TRY(dalloc(h, &h->btab, 126 * sizeof(double)));
     TRY(dalloc(h, &h->btabf, 126 * sizeof(float)));
@@ -344,7 +356,7 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     TRY(dalloc(h, &h->d_rec, capn * REC_STRIDE * sizeof(double)));
     TRY(dalloc(h, &h->d_sph, capn * sizeof(SphereDev)));
     TRY(dalloc(h, &h->d_fast, capn * sizeof(SphereFast)));
-    TRY(dalloc(h, &h->d_xpf, capn * 8 * sizeof(float)));
+    TRY(dalloc(h, &h->d_xpf, capn * XPF_STRIDE * sizeof(float)));
     TRY(dalloc(h, &h->d_tag2slot, ((size_t)c.max_tag + 1) * sizeof(int)));
     TRY(dalloc(h, &h->d_tile_cnt, (size_t)h->ntiles * sizeof(int)));
     TRY(dalloc(h, &h->d_bins, (size_t)h->ntiles * TILE_BIN * sizeof(int)));
@@ -382,7 +394,7 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     TRY(cudaMemcpy(h->btabf, btf, sizeof(btf), cudaMemcpyHostToDevice));
     TRY(cudaMemset(h->f, 0, (size_t)Q * N * h->esz));   // f̄ = 0: rho = 1, u = 0
     TRY(cudaMemset(h->vox, 0, N * sizeof(uint32_t)));
-    TRY(cudaMemset(h->up, 0, 3 * N * h->esz));
+    if (h->up) TRY(cudaMemset(h->up, 0, 3 * N * h->esz));
     if (h->cf) TRY(cudaMemset(h->cf, 0, 3 * N * h->esz));
     TRY(cudaMemset(h->d_tag2slot, 0x7F, ((size_t)c.max_tag + 1) * sizeof(int)));
     TRY(cudaMemset(h->d_ft, 0, 6 * capn * sizeof(double)));
@@ -598,7 +610,15 @@ lbdem_status lbdem_get_field(lbdem_handle* h, int32_t which, void* host_buf) {
             break;
         }
         case LBDEM_FIELD_PARTICLE_VELOCITY:
-            CK(h, cudaMemcpyAsync(host_buf, h->up, 3 * N * h->esz, cudaMemcpyDeviceToHost, s));
+            if (h->up) {
+                CK(h, cudaMemcpyAsync(host_buf, h->up, 3 * N * h->esz, cudaMemcpyDeviceToHost, s));
+            } else {   // FP32 form: recomputed from the owner particles of the current list
+                if ((st = ensure_scratch(h, 3 * N * sizeof(float))) != LBDEM_OK) return st;
+                CK(h, launch_owner_velocity(h->vox, h->d_tag2slot, h->cfg.max_tag, h->n_cur, h->d_xpf, h->g,
+                                            (float*)h->scratch, s));
+                h->launches += 1;
+                CK(h, cudaMemcpyAsync(host_buf, h->scratch, 3 * N * sizeof(float), cudaMemcpyDeviceToHost, s));
+            }
             break;
         case LBDEM_FIELD_HYDRO_FORCE:
             if (!h->cf) return fail(h, LBDEM_ERR_INVALID_ARG, "get_field: create with LBDEM_FLAG_CELL_FORCE");
@@ -1007,10 +1027,10 @@ lbdem_status lbdem_save_state(lbdem_handle* h, const char* path) {
     if (st != LBDEM_OK) return st;
     std::vector<uint32_t> vox(N);
     std::vector<unsigned char> up(3 * N * h->esz);
+    if ((st = lbdem_get_field(h, LBDEM_FIELD_PARTICLE_VELOCITY, up.data())) != LBDEM_OK) return st;
     {
         DeviceGuard dg(h->device);
         CK(h, cudaMemcpyAsync(vox.data(), h->vox, N * sizeof(uint32_t), cudaMemcpyDeviceToHost, h->stream));
-        CK(h, cudaMemcpyAsync(up.data(), h->up, 3 * N * h->esz, cudaMemcpyDeviceToHost, h->stream));
         CK(h, cudaStreamSynchronize(h->stream));
     }
     CheckpointHeader hd{};
@@ -1055,7 +1075,9 @@ lbdem_status lbdem_load_state(lbdem_handle* h, const char* path) {
     if (st != LBDEM_OK) return st;
     DeviceGuard dg(h->device);
     CK(h, cudaMemcpyAsync(h->vox, vox.data(), N * sizeof(uint32_t), cudaMemcpyHostToDevice, h->stream));
-    CK(h, cudaMemcpyAsync(h->up, up.data(), 3 * N * h->esz, cudaMemcpyHostToDevice, h->stream));
+    // the FP32 form keeps no velocity field: it recomputes the velocity from the
+    // particle list of the next lbdem_set_particles
+    if (h->up) CK(h, cudaMemcpyAsync(h->up, up.data(), 3 * N * h->esz, cudaMemcpyHostToDevice, h->stream));
     CK(h, cudaStreamSynchronize(h->stream));
     h->pavg_valid = false;
     return LBDEM_OK;

@@ -17,6 +17,7 @@ constexpr int TILE_CELLS = TILE * TILE * TILE;
 constexpr int TILE_BIN = 64;            // sphere slots per tile bin
 constexpr int TILE_LIST_MAX = 1024;     // spheres per tile when a bin overflows (shared memory)
 constexpr int REC_STRIDE = 12;          // doubles per particle record {x3, v3, w3, r, tag, 0}
+constexpr int XPF_STRIDE = 16;          // floats per particle of the float table (xpf, see below)
 constexpr int VOX_NBITS = 7;            // voxel word: sub-cell count n (7 bits) | tag << 7
 constexpr uint32_t VOX_NMASK = (1u << VOX_NBITS) - 1u;
 constexpr int32_t MAX_TAG_LIMIT = (1 << 25) - 1;
@@ -120,7 +121,7 @@ struct CollideArgs {
     T* cf;                   // [3][N] per-cell force (nullptr: not kept)
     const int* tag2slot;     // [max_tag + 1] lowest particle index per tag
     const double* rec;       // [n][12] particle records (positions for the torque arm)
-    const float* xpf;        // [n][8] centre split into float hi/lo (float form's torque arm)
+    const float* xpf;        // [n][XPF_STRIDE] float table: centre hi/lo, v, omega (float form)
     int nslot;               // particles in the current list
     int max_tag;             // tag2slot has max_tag + 1 entries
     double* ft;              // [6][n]: F (3n) then T (3n)
@@ -130,6 +131,58 @@ struct CollideArgs {
     T g3[3];                 // Guo body-force acceleration
     DivMagic dz, dy;         // division by the z-segments per row and by ny (set by the launchers)
 };
+
+// Float table of a particle list, one row of XPF_STRIDE floats per particle:
+//   {xh0, xh1, xh2, xl0 | xl1, xl2, v0, v1 | v2, w0, w1, w2 | 0, 0, 0, 0},
+// centre = xh + xl (hi/lo split), velocity and angular velocity rounded to float.
+// It gives the float form its torque arms and its particle surface velocities.
+struct TableRow {
+    float4 a, b, c;
+};
+__device__ __forceinline__ TableRow load_row(const float* __restrict__ xpf, int slot) {
+    const float4* p = reinterpret_cast<const float4*>(xpf + (size_t)slot * XPF_STRIDE);
+    return TableRow{__ldg(p), __ldg(p + 1), __ldg(p + 2)};
+}
+//
+// Particle surface velocity of cell (x, y, z) in the float form, recomputed from
+// the owner particle's row instead of being stored per cell: v + omega x arm,
+// arm = cell - centre taken to the nearest image along periodic axes with the
+// minimum-image rule of the force sum (integer half extent,
+// src/ibProcessors3D.hh:230-243).  setValues (src/ibProcessors3D.hh:163-174)
+// stores the same velocity from the image that set the cell; ghost images
+// carry their owner's v and omega, and the nearest image is the one that set
+// the cell whenever the periodic extent exceeds the sphere's diameter plus
+// two cells.  Every operation is rounded on its own, so that all kernels
+// that form this velocity agree bit for bit.
+__host__ __device__ __forceinline__ float min_image_f(float d, int n, int per) {
+    if (!per) return d;
+    const int h = n / 2;
+    if (d > (float)h) return d - (float)n;
+    if (d < (float)-h) return d + (float)n;
+    return d;
+}
+__device__ __forceinline__ void row_velocity(const TableRow& r, int x, int y, int z, const Geom& g, float& u0,
+                                             float& u1, float& u2) {
+    const float dx = min_image_f(__fsub_rn(__fsub_rn((float)x, r.a.x), r.a.w), g.nx, g.per[0]);
+    const float dy = min_image_f(__fsub_rn(__fsub_rn((float)y, r.a.y), r.b.x), g.ny, g.per[1]);
+    const float dz = min_image_f(__fsub_rn(__fsub_rn((float)z, r.a.z), r.b.y), g.nz, g.per[2]);
+    // v = (b.z, b.w, c.x), omega = (c.y, c.z, c.w)
+    u0 = __fadd_rn(r.b.z, __fsub_rn(__fmul_rn(r.c.z, dz), __fmul_rn(r.c.w, dy)));
+    u1 = __fadd_rn(r.b.w, __fsub_rn(__fmul_rn(r.c.w, dx), __fmul_rn(r.c.y, dz)));
+    u2 = __fadd_rn(r.c.x, __fsub_rn(__fmul_rn(r.c.y, dy), __fmul_rn(r.c.z, dx)));
+}
+__device__ __forceinline__ void table_velocity(const float* __restrict__ row, int x, int y, int z, const Geom& g,
+                                               float& u0, float& u1, float& u2) {
+    const float4* p = reinterpret_cast<const float4*>(row);
+    row_velocity(TableRow{__ldg(p), __ldg(p + 1), __ldg(p + 2)}, x, y, z, g, u0, u1, u2);
+}
+// The owner slot of a voxel word (-1: no solid fraction, or a tag with no particle).
+__device__ __forceinline__ int owner_slot(uint32_t w, const int* __restrict__ tag2slot, int max_tag, int nslot) {
+    if ((w & VOX_NMASK) == 0u) return -1;
+    const int tag = (int)(w >> VOX_NBITS);
+    const int slot = tag <= max_tag ? __ldg(tag2slot + tag) : -1;
+    return (slot >= 0 && slot < nslot) ? slot : -1;
+}
 
 // Exact (double) description of one sphere of the list, for the decisions
 // that need the reference's double arithmetic.
@@ -201,10 +254,18 @@ cudaError_t launch_prepare_bin(const double* rec, int n, SphereDev* sph, SphereF
                                int* tag2slot, unsigned* err, Geom g, int max_tag, double max_radius,
                                double* ft_zero, double* rec_copy, int* tile_cnt, int* bins, int* work, int* work_n,
                                cudaStream_t s);
+// The float table and tag map of the list being voxelized (the prepare launch
+// fills both); used by defineVelocity in the float form, which keeps no
+// surface-velocity field (up == nullptr).
+struct OwnerTable {
+    const float* xpf;
+    const int* tag2slot;
+    int max_tag;
+};
 template <typename T>
 cudaError_t launch_voxelize(const SphereDev* sph, const SphereFast* fast, int n, int* tile_cnt, const int* bins,
                             const int* work, int* work_n, int ntiles, uint32_t* vox, T* up, T* f, int init_vel,
-                            int odd_phase, Geom g, unsigned* err, cudaStream_t s);
+                            int odd_phase, Geom g, const OwnerTable& ot, cudaStream_t s);
 
 // Batch forms: particle slots and tiles of all domains in one index space;
 // soff[d] = doms[d].s0, toff[d] = doms[d].t0 (ascending); ncur[d] particles of
@@ -219,7 +280,7 @@ template <typename T>
 cudaError_t launch_voxelize_batch(const SphereDev* sph, const SphereFast* fast, int* tile_cnt, const int* bins,
                                   const int* work, int* work_n, int ntiles, uint32_t* vox, T* up, T* f, int init_vel,
                                   int odd_phase, const DomView* doms, const int* toff, int ndom, const int* ncur,
-                                  unsigned* err, cudaStream_t s);
+                                  const OwnerTable& ot, cudaStream_t s);
 
 // Field helpers.  phase: number of completed steps mod 2 (storage layout).
 template <typename T>
@@ -234,6 +295,10 @@ template <typename T>
 cudaError_t launch_mass(const T* f, double* out, Geom g, cudaStream_t s);
 cudaError_t launch_vox_fields(const uint32_t* vox, double* sf, int32_t* id, uint8_t* nsub, Geom g,
                               cudaStream_t s);
+// Float form: the particle surface velocity of every cell, [3][N], as the
+// collision recomputes it (owner rows of the float table; zero in free cells).
+cudaError_t launch_owner_velocity(const uint32_t* vox, const int* tag2slot, int max_tag, int nslot, const float* xpf,
+                                  Geom g, float* out, cudaStream_t s);
 
 // One plane (box) of the periodic pressure drop: average density of the box and,
 // optionally, the Zhang rescale of the populations entering it.
@@ -268,7 +333,7 @@ struct AdjointArgs {
     const int* tag2slot;
     int max_tag, nslot;
     const double* rec;       // [nslot][12] particle records of the step
-    const float* xpf;        // [nslot][8] centres split into float hi/lo (float form's arm)
+    const float* xpf;        // [nslot][XPF_STRIDE] float table (float form's arm)
     const double* w;         // [nslot][6] dL/dF, dL/dT of the step
     double* gvel;            // [nslot][6] += dL/dv, dL/domega of the step
     double* gglob;           // [4] += dL/dg, dL/dtau

@@ -30,7 +30,7 @@ constexpr size_t up_align(size_t b) { return (b + ALIGN - 1) / ALIGN * ALIGN; }
 constexpr size_t OFF_SPH = 0;
 constexpr size_t OFF_FAST = OFF_SPH + up_align(sizeof(SphereDev) * LBDEM_STATIC_MAX_SPHERES);
 constexpr size_t OFF_XPF = OFF_FAST + up_align(sizeof(SphereFast) * LBDEM_STATIC_MAX_SPHERES);
-constexpr size_t OFF_TAG = OFF_XPF + up_align(sizeof(float) * 8 * LBDEM_STATIC_MAX_SPHERES);
+constexpr size_t OFF_TAG = OFF_XPF + up_align(sizeof(float) * XPF_STRIDE * LBDEM_STATIC_MAX_SPHERES);
 constexpr size_t OFF_CNT = OFF_TAG + up_align(sizeof(int) * ((size_t)LBDEM_STATIC_MAX_TAG + 1));
 constexpr size_t OFF_BINS = OFF_CNT + up_align(sizeof(int) * LBDEM_STATIC_MAX_TILES);
 constexpr size_t OFF_WORK = OFF_BINS + up_align(sizeof(int) * TILE_BIN * (size_t)LBDEM_STATIC_MAX_TILES);
@@ -43,9 +43,6 @@ static_assert(SCRATCH_BYTES <= LBDEM_STATIC_SCRATCH_BYTES, "static scratch regio
 // address comes from cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_scratch[LBDEM_STATIC_SCRATCH_BYTES];
 
-// Device address of g_scratch per device ordinal, resolved by the first call
-// made with that device current.
-void* g_scratch_addr[STATIC_MAX_DEVICES] = {};
 
 }  // namespace
 
@@ -67,15 +64,15 @@ extern "C" lbdem_status lbdem_voxelize_static(int32_t nx, int32_t ny, int32_t nz
         return LBDEM_ERR_NO_DEVICE;
     }
     if (dev < 0 || dev >= STATIC_MAX_DEVICES) return LBDEM_ERR_NO_DEVICE;
-    if (!g_scratch_addr[dev]) {
-        void* p = nullptr;
-        if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) {
-            cudaGetLastError();
-            return LBDEM_ERR_CUDA;
-        }
-        g_scratch_addr[dev] = p;
+    // The array's device address on the current device, looked up on every call
+    // (a host-side lookup, no GPU work): nothing is cached that a device reset
+    // or a second thread could invalidate.
+    void* addr = nullptr;
+    if (cudaGetSymbolAddress(&addr, g_scratch) != cudaSuccess || !addr) {
+        cudaGetLastError();
+        return LBDEM_ERR_CUDA;
     }
-    unsigned char* base = static_cast<unsigned char*>(g_scratch_addr[dev]);
+    unsigned char* base = static_cast<unsigned char*>(addr);
     SphereDev* sph = reinterpret_cast<SphereDev*>(base + OFF_SPH);
     SphereFast* fast = reinterpret_cast<SphereFast*>(base + OFF_FAST);
     float* xpf = reinterpret_cast<float*>(base + OFF_XPF);
@@ -98,15 +95,22 @@ extern "C" lbdem_status lbdem_voxelize_static(int32_t nx, int32_t ny, int32_t nz
         cudaMemsetAsync(tag2slot, 0x7F, sizeof(int) * ((size_t)LBDEM_STATIC_MAX_TAG + 1), s) != cudaSuccess)
         return LBDEM_ERR_CUDA;
     if (n == 0) return LBDEM_OK;   // no sphere touches a cell (as in the reference)
-    cudaError_t e = launch_prepare_bin(dev_rec, n, sph, fast, xpf, tag2slot, dev_err, g, LBDEM_STATIC_MAX_TAG, 1024.0,
-                                       nullptr, nullptr, tile_cnt, bins, work, work_n, s);
+    cudaError_t e = launch_prepare_bin(dev_rec, n, sph, fast, xpf, tag2slot, dev_err, g, LBDEM_STATIC_MAX_TAG,
+                                       LBDEM_STATIC_MAX_RADIUS, nullptr, nullptr, tile_cnt, bins, work, work_n, s);
+    const OwnerTable ot{xpf, tag2slot, LBDEM_STATIC_MAX_TAG};
     if (e == cudaSuccess) {
-        if (precision == LBDEM_PREC_FP64)
+        if (precision == LBDEM_PREC_FP64) {
             e = launch_voxelize<double>(sph, fast, n, tile_cnt, bins, work, work_n, (int)ntiles, dev_vox,
-                                        static_cast<double*>(dev_up), nullptr, 0, 0, g, dev_err, s);
-        else
-            e = launch_voxelize<float>(sph, fast, n, tile_cnt, bins, work, work_n, (int)ntiles, dev_vox,
-                                       static_cast<float*>(dev_up), nullptr, 0, 0, g, dev_err, s);
+                                        static_cast<double*>(dev_up), nullptr, 0, 0, g, ot, s);
+        } else {
+            // FP32 form: the velocity field is the one the handle's collision
+            // recomputes from the owner particles (lbdem_get_field)
+            e = launch_voxelize<float>(sph, fast, n, tile_cnt, bins, work, work_n, (int)ntiles, dev_vox, nullptr,
+                                       nullptr, 0, 0, g, ot, s);
+            if (e == cudaSuccess)
+                e = launch_owner_velocity(dev_vox, tag2slot, LBDEM_STATIC_MAX_TAG, n, xpf, g,
+                                          static_cast<float*>(dev_up), s);
+        }
     }
     return e == cudaSuccess ? LBDEM_OK : LBDEM_ERR_CUDA;
 }
