@@ -106,6 +106,19 @@ lbdem_status lbdem_destroy(lbdem_handle* h);
 const char* lbdem_last_error(const lbdem_handle* h);
 const char* lbdem_status_string(lbdem_status s);
 
+/* BGK relaxation frequency of every cell, 0 < omega < 2: what
+ * defineDynamics(lattice, lattice.getBoundingBox(), new IBcompositeDynamics<T,D>(
+ * new BGKdynamics<T,D>(omega))) sets in the reference's case drivers
+ * (examples/sedimentingSphere/sedimentingSphere.cpp:181).  Waits for the
+ * handle's queued work. */
+lbdem_status lbdem_set_omega(lbdem_handle* h, double omega);
+
+/* Periodicity per axis (1 periodic, 0 half-way bounce-back walls): Palabos'
+ * lattice.periodicity().toggle(d, flag) / toggleAll(flag)
+ * (sedimentingSphere.cpp:183, showcaseRectChannel.cpp:201).  Not allowed
+ * while a pressure drop is set.  Waits for the handle's queued work. */
+lbdem_status lbdem_set_periodic(lbdem_handle* h, const int32_t periodic[3]);
+
 /* Orders the handle's GPU work on the given cudaStream_t (NULL: back to the
  * handle's own stream). */
 lbdem_status lbdem_set_stream(lbdem_handle* h, void* cuda_stream);

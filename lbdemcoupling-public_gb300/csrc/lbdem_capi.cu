@@ -190,6 +190,25 @@ lbdem_status voxelize(lbdem_handle* h, int n, int init_vel, const double* src) {
     return LBDEM_OK;
 }
 
+// B(n) = sf ooo / ((1 - sf) + ooo), sf = n/125, ooo = 1/omega - 1/2
+// (src/ibCompositeDynamics3D.hh:178-179); n = 125 is the full-solid branch, B = 1.
+// Synchronous copies of the handle's omega into both tables.
+cudaError_t upload_btab(lbdem_handle* h) {
+    double bt[126];
+    const double ooo = 1. / h->cfg.omega - 0.5;
+    for (int n = 0; n < 126; ++n) {
+        const double sf = (1. / 125.) * (double)n;
+        bt[n] = sf * ooo / ((1. - sf) + ooo);
+    }
+    bt[0] = 0.0;
+    bt[125] = 1.0;
+    cudaError_t e = cudaMemcpy(h->btab, bt, sizeof(bt), cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) return e;
+    float btf[126];
+    for (int n = 0; n < 126; ++n) btf[n] = (float)bt[n];
+    return cudaMemcpy(h->btabf, btf, sizeof(btf), cudaMemcpyHostToDevice);
+}
+
 bool box_ok(const lbdem_handle* h, const int32_t* b) {
     const int ext[3] = {h->g.nx, h->g.ny, h->g.nz};
     for (int d = 0; d < 3; ++d)
@@ -378,20 +397,7 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     TRY(cudaMemset(h->d_pavg, 0, 8 * sizeof(double)));
     TRY(cudaMallocHost((void**)&h->h_pavg, sizeof(double)));
 
-    // B(n) = sf ooo / ((1 - sf) + ooo), sf = n/125, ooo = 1/omega - 1/2
-    // (src/ibCompositeDynamics3D.hh:178-179); n = 125 is the full-solid branch, B = 1.
-    double bt[126];
-    const double ooo = 1. / c.omega - 0.5;
-    for (int n = 0; n < 126; ++n) {
-        const double sf = (1. / 125.) * (double)n;
-        bt[n] = sf * ooo / ((1. - sf) + ooo);
-    }
-    bt[0] = 0.0;
-    bt[125] = 1.0;
-    TRY(cudaMemcpy(h->btab, bt, sizeof(bt), cudaMemcpyHostToDevice));
-    float btf[126];
-    for (int n = 0; n < 126; ++n) btf[n] = (float)bt[n];
-    TRY(cudaMemcpy(h->btabf, btf, sizeof(btf), cudaMemcpyHostToDevice));
+    TRY(upload_btab(h));
     TRY(cudaMemset(h->f, 0, (size_t)Q * N * h->esz));   // f̄ = 0: rho = 1, u = 0
     TRY(cudaMemset(h->vox, 0, N * sizeof(uint32_t)));
     if (h->up) TRY(cudaMemset(h->up, 0, 3 * N * h->esz));
@@ -748,6 +754,28 @@ lbdem_status lbdem_set_pressure_drop(lbdem_handle* h, const lbdem_pressure_drop*
     h->pdrop_bpj = plane_blocks(std::max(box_cells(d->inlet), box_cells(d->outlet)));
     h->pdrop_on = true;
     h->pavg_valid = false;
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_set_omega(lbdem_handle* h, double omega) {
+    if (!h) return LBDEM_ERR_INVALID_ARG;
+    if (!(omega > 0.0 && omega < 2.0)) return fail(h, LBDEM_ERR_INVALID_ARG, "set_omega: omega outside (0, 2)");
+    DeviceGuard dg(h->device);
+    CK(h, cudaStreamSynchronize(h->stream));   // queued steps use the old tables
+    h->cfg.omega = omega;
+    CK(h, upload_btab(h));
+    return LBDEM_OK;
+}
+
+lbdem_status lbdem_set_periodic(lbdem_handle* h, const int32_t periodic[3]) {
+    if (!h || !periodic) return LBDEM_ERR_INVALID_ARG;
+    for (int d = 0; d < 3; ++d)
+        if (periodic[d] != 0 && periodic[d] != 1) return fail(h, LBDEM_ERR_INVALID_ARG, "set_periodic: 0 or 1");
+    if (h->pdrop_on)
+        return fail(h, LBDEM_ERR_INVALID_ARG, "set_periodic: set the periodicity before the pressure drop");
+    DeviceGuard dg(h->device);
+    CK(h, cudaStreamSynchronize(h->stream));
+    for (int d = 0; d < 3; ++d) h->cfg.periodic[d] = h->g.per[d] = periodic[d];
     return LBDEM_OK;
 }
 

@@ -56,7 +56,7 @@ int main(int argc, char** argv) {
                 plb::applyZhangPeriodicPressure(lattice, inlet, rhoHi, rhoAvgOut, 0, 1);
                 plb::applyZhangPeriodicPressure(lattice, outlet, rhoLo, rhoAvgIn, 0, -1);
             }
-            plb::getForcesFromLattice<LAMMPS_NS::FixLbCouplingOnetoone>(lattice, wrapper, units);
+            plb::getForcesFromLattice(lattice, wrapper, units);
         }
         const size_t N = (size_t)nx * ny * nz;
         std::vector<double> u(3 * N);

@@ -55,7 +55,7 @@ int main(int argc, char** argv) {
         for (long iT = 0; iT < steps; ++iT) {
             plb::setSpheresOnLattice(lattice, wrapper, units, false);
             lattice.collideAndStream();
-            plb::getForcesFromLattice<LAMMPS_NS::FixLbCouplingOnetoone>(lattice, wrapper, units);
+            plb::getForcesFromLattice(lattice, wrapper, units);
             wrapper.run(demSubsteps);
             if (iT % every == 0)
                 std::fprintf(out, "%ld %.17g %.17g %.17g\n", iT, units.getLbPosition(wrapper.atom.x[0][2]),

@@ -85,6 +85,8 @@ SIGNATURES = {
     "lbdem_last_error": (C.c_char_p, [_P]),
     "lbdem_status_string": (C.c_char_p, [C.c_int]),
     "lbdem_set_stream": (C.c_int, [_P, _P]),
+    "lbdem_set_omega": (C.c_int, [_P, C.c_double]),
+    "lbdem_set_periodic": (C.c_int, [_P, C.POINTER(_I)]),
     "lbdem_synchronize": (C.c_int, [_P]),
     "lbdem_init_equilibrium": (C.c_int, [_P, C.c_double, _D]),
     "lbdem_set_populations": (C.c_int, [_P, _P]),
@@ -234,6 +236,13 @@ class Lattice:
             raise LbdemError(st, self.lib.lbdem_last_error(self.h).decode())
 
     # -- state ------------------------------------------------------------
+    def set_omega(self, omega):
+        self._check(self.lib.lbdem_set_omega(self.h, float(omega)))
+
+    def set_periodic(self, periodic):
+        p = (_I * 3)(*[int(x) for x in periodic])
+        self._check(self.lib.lbdem_set_periodic(self.h, p))
+
     def init_equilibrium(self, rho_bar=0.0, u=(0.0, 0.0, 0.0)):
         uu = _c64(u)
         self._check(self.lib.lbdem_init_equilibrium(self.h, float(rho_bar), _dptr(uu)))

@@ -116,11 +116,10 @@ def test_division_by_invariant_divisor():
                     assert ((n * m) >> 32) >> s == n // d, (d, n)
 
 
-def test_integration_binding_snippet_compiles(tmp_path):
-    """The C++ binding INTEGRATION.md shows a maintainer adding on the reference side
-    compiles against the C ABI header, the PhysUnits3D shim and the LIGGGHTS stand-in
-    of the example programs (its templates instantiated with double)."""
-    import re
+def test_integration_binding_snippet_compiles():
+    """The C++ binding a maintainer adds on the reference side (tests/integration_binding.cpp,
+    quoted in INTEGRATION.md) compiles against the C ABI header, the PhysUnits3D shim and
+    the LIGGGHTS stand-in of the example programs (its templates instantiated with double)."""
     import shutil
     import subprocess
     from pathlib import Path
@@ -128,19 +127,8 @@ def test_integration_binding_snippet_compiles(tmp_path):
     if cxx is None:
         pytest.skip("no C++ compiler")
     root = Path(__file__).resolve().parents[1]
-    text = (root / "INTEGRATION.md").read_text()
-    blocks = re.findall(r"```cpp\n(.*?)```", text, flags=re.S)
-    snippet = next(b for b in blocks if "struct GpuLattice" in b)
-    src = tmp_path / "binding.cpp"
-    src.write_text(
-        "#include <algorithm>\n#include <cstdint>\n#include <stdexcept>\n#include <vector>\n"
-        '#include "dem_standin.h"\n#include "physunits_gpu.h"\n'
-        "namespace plb { typedef long plint; }\nusing namespace plb;\n"
-        + snippet
-        + "\nvoid instantiate(GpuLattice& lat, LiggghtsCouplingWrapper& w, PhysUnits3D<double> const& u,\n"
-          "                 std::vector<plint>& ex) {\n"
-          "  setSpheresOnLattice(lat, w, u, ex, true);\n  getForcesFromLattice(lat, w, u);\n}\n")
     pkg = root / "lbdemcoupling-public_gb300"
     r = subprocess.run([cxx, "-std=c++17", "-fsyntax-only", "-Wall", f"-I{root / 'include'}", f"-I{pkg / 'plb'}",
-                        f"-I{pkg / 'examples'}", str(src)], capture_output=True, text=True)
+                        f"-I{pkg / 'examples'}", str(root / "tests" / "integration_binding.cpp")],
+                       capture_output=True, text=True)
     assert r.returncode == 0, r.stderr
