@@ -78,6 +78,13 @@ typedef enum {
 /* Keep the per-cell hydrodynamic force field (for export).  Off by default: the
  * force/torque sum is fused into the collide-stream kernel and needs no field. */
 #define LBDEM_FLAG_CELL_FORCE 0x1
+/* Failure-path test hook: in every collide-stream step of the handle, each warp's
+ * first wait for its staged data waits on a barrier that nothing completes
+ * (bounded), so the step takes the path of a copy that never lands: the kernel
+ * sets LBDEM_DEVERR_TIMEOUT, lets its copies in flight land and returns early
+ * (the step's populations are then not valid).  Applies to the FP64 form and to
+ * rows that are not 16-byte aligned (the staging that waits on barriers). */
+#define LBDEM_FLAG_PROBE_TIMEOUT 0x2
 
 typedef struct {
     int32_t nx, ny, nz;       /* lattice extent in cells                              */
@@ -94,6 +101,12 @@ typedef struct {
 } lbdem_config;
 
 typedef struct lbdem_handle lbdem_handle;
+
+/* Failure-path test hook: the nth device or pinned allocation made by
+ * lbdem_create or lbdem_batch_create from now on (process-wide) reports failure
+ * without being made; nth <= 0 switches the hook off.  A creation that meets it
+ * returns LBDEM_ERR_OUT_OF_MEMORY after releasing what it had allocated. */
+void lbdem_debug_fail_allocation(int32_t nth);
 
 /* Fills cfg with defaults: 32^3 periodic, omega 1, FP64, device 0,
  * 1024 particles, max_tag 1<<20, max_radius 16. */

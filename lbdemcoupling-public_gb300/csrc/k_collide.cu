@@ -641,6 +641,7 @@ __device__ __forceinline__ int pick(int c, int m, int v, int p) { return c < 0 ?
 constexpr int WARPS = COLLIDE_BLOCK / 32;    // warps per CTA
 constexpr int SEGW = COLLIDE_SEGW;          // cells per warp segment (2 per lane)
 constexpr int WAIT_LIMIT = 1 << 22;         // bounded mbarrier wait (iterations of try_wait)
+constexpr int PROBE_WAIT = 64;              // the timeout test hook's wait (iterations)
 
 // Surface-velocity rows are staged by the FP64 form of a single lattice only.
 template <typename T, bool BATCH>
@@ -692,9 +693,9 @@ __device__ __forceinline__ bool mbar_try_wait(unsigned long long* bar, uint32_t 
         : "memory");
     return ok != 0;
 }
-// Bounded wait: false if the phase did not complete within WAIT_LIMIT tries.
-__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
-    for (int k = 0; k < WAIT_LIMIT; ++k)
+// Bounded wait: false if the phase did not complete within `limit` tries.
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity, int limit = WAIT_LIMIT) {
+    for (int k = 0; k < limit; ++k)
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
@@ -1216,9 +1217,11 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     WarpStage<T, STAGE_UP>& st = reinterpret_cast<WarpStage<T, STAGE_UP>*>(smem_raw)[warp];
+    __shared__ unsigned long long probe[WARPS];   // the test hook's barrier (never completes)
     if (lane == 0) {
         mbar_init(&st.bar[0], 1);
         mbar_init(&st.bar[1], 1);
+        mbar_init(&probe[warp], 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncwarp();
@@ -1239,6 +1242,7 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
     };
     T hcur = issue(0, seg);
     uint32_t phase = 0;   // bit b: parity expected next on buffer b
+    bool first = true;
     int b = 0;
     for (; seg < nseg; seg += stride, b ^= 1) {
         const long long next = seg + stride;
@@ -1250,11 +1254,21 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
             else cp_wait<0>();
             __syncwarp();   // and every other lane's
         } else {
-            const bool ok = mbar_wait(&st.bar[b], (phase >> b) & 1u);
+            const uint32_t pb = (phase >> b) & 1u;
+            bool ok;
+            if (!BATCH && a1.probe_timeout && first) {
+                // test hook: wait on a barrier nothing arrives on, as for a copy that never lands
+                ok = mbar_wait(&probe[warp], 0u, PROBE_WAIT);
+            } else {
+                ok = mbar_wait(&st.bar[b], pb);
+            }
             phase ^= 1u << b;
+            first = false;
             if (__any_sync(FULL, !ok)) {
-                // a copy did not land: report, let in-flight copies finish, leave
+                // a copy did not land: report, let this warp's copies in flight land
+                // (both buffers, bounded), leave
                 if (lane == 0) atomicOr(BATCH ? dargs[0].err : a1.err, 0x20u);   // LBDEM_DEVERR_TIMEOUT
+                mbar_wait(&st.bar[b], pb);
                 if (next < nseg) mbar_wait(&st.bar[b ^ 1], (phase >> (b ^ 1)) & 1u);
                 return;
             }

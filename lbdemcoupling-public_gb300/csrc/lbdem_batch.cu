@@ -125,6 +125,7 @@ lbdem_status fail_cuda(lbdem_batch* b, const char* what, cudaError_t e) {
 template <typename P>
 cudaError_t dalloc(lbdem_batch* b, P** p, size_t bytes) {
     void* q = nullptr;
+    if (alloc_should_fail()) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMalloc(&q, bytes == 0 ? 16 : bytes);
     if (e == cudaSuccess) {
         *p = (P*)q;
@@ -512,9 +513,9 @@ lbdem_status lbdem_batch_create(const lbdem_batch_config* cfg, int32_t ndomains,
     TRY(dalloc(b, &b->d_seg0, sizeof(int) * ndomains));
     TRY(dalloc(b, &b->d_dargs, (b->prec == LBDEM_PREC_FP64 ? sizeof(CollideArgs<double>) : sizeof(CollideArgs<float>)) *
                                    ndomains));
-    TRY(cudaMallocHost((void**)&b->h_stage, b->stage_bytes));
-    TRY(cudaMallocHost((void**)&b->h_ft, sizeof(double) * 6 * capn));
-    TRY(cudaMallocHost((void**)&b->h_err, sizeof(unsigned)));
+    TRY(alloc_should_fail() ? cudaErrorMemoryAllocation : cudaMallocHost((void**)&b->h_stage, b->stage_bytes));
+    TRY(alloc_should_fail() ? cudaErrorMemoryAllocation : cudaMallocHost((void**)&b->h_ft, sizeof(double) * 6 * capn));
+    TRY(alloc_should_fail() ? cudaErrorMemoryAllocation : cudaMallocHost((void**)&b->h_err, sizeof(unsigned)));
     std::memset(b->h_stage, 0, b->stage_bytes);
 
     TRY(cudaMemset(b->f, 0, b->f_elems * b->esz + ALLOC_TAIL));

@@ -14,6 +14,19 @@
 
 using namespace lbdem;
 
+namespace lbdem {
+std::atomic<int> g_alloc_fail_countdown{0};
+}
+
+namespace {
+// Pinned host allocation through the allocation-failure test hook.
+template <typename P>
+cudaError_t halloc(P** p, size_t bytes) {
+    if (alloc_should_fail()) return cudaErrorMemoryAllocation;
+    return cudaMallocHost((void**)p, bytes);
+}
+}  // namespace
+
 struct lbdem_handle {
     lbdem_config cfg{};
     Geom g{};
@@ -111,6 +124,7 @@ lbdem_status fail_cuda(lbdem_handle* h, const char* what, cudaError_t e) {
 template <typename P>
 cudaError_t dalloc(lbdem_handle* h, P** p, size_t bytes) {
     void* q = nullptr;
+    if (alloc_should_fail()) return cudaErrorMemoryAllocation;
     cudaError_t e = cudaMalloc(&q, bytes == 0 ? 16 : bytes);
     if (e == cudaSuccess) {
         *p = (P*)q;
@@ -252,6 +266,7 @@ cudaError_t k1_launch(lbdem_handle* h, void* fin, void* fout) {
         a.g = h->g; a.f = (double*)fin; a.fo = (double*)fout; a.vox = h->vox; a.up = (const double*)h->up;
         a.cf = (double*)h->cf; a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.xpf = h->d_xpf; a.nslot = n;
         a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err; a.btab = h->btab; a.omega = h->cfg.omega;
+        a.probe_timeout = (h->cfg.flags & LBDEM_FLAG_PROBE_TIMEOUT) ? 1 : 0;
         for (int d = 0; d < 3; ++d) a.g3[d] = h->cfg.body_force[d];
         return launch_collide_stream<double>(a, odd, force, h->stream);
     }
@@ -259,6 +274,7 @@ cudaError_t k1_launch(lbdem_handle* h, void* fin, void* fout) {
     a.g = h->g; a.f = (float*)fin; a.fo = (float*)fout; a.vox = h->vox; a.up = nullptr;
     a.cf = (float*)h->cf; a.tag2slot = h->d_tag2slot; a.rec = h->d_rec; a.xpf = h->d_xpf; a.nslot = n;
     a.max_tag = h->cfg.max_tag; a.ft = h->d_ft; a.err = h->d_err; a.btab = h->btabf; a.omega = (float)h->cfg.omega;
+    a.probe_timeout = (h->cfg.flags & LBDEM_FLAG_PROBE_TIMEOUT) ? 1 : 0;
     for (int d = 0; d < 3; ++d) a.g3[d] = (float)h->cfg.body_force[d];
     return launch_collide_stream<float>(a, odd, force, h->stream);
 }
@@ -275,6 +291,8 @@ cudaError_t plane_launch(lbdem_handle* h, const PlaneJob* jobs, int njobs, int b
 }  // namespace
 
 extern "C" {
+
+void lbdem_debug_fail_allocation(int32_t nth) { g_alloc_fail_countdown.store(nth > 0 ? nth : 0); }
 
 void lbdem_config_default(lbdem_config* c) {
     if (!c) return;
@@ -386,16 +404,16 @@ lbdem_status lbdem_create(const lbdem_config* cfg, lbdem_handle** out) {
     TRY(dalloc(h, &h->d_ft, 6 * capn * sizeof(double)));
     TRY(dalloc(h, &h->d_err, sizeof(unsigned)));
     TRY(dalloc(h, &h->d_mass, sizeof(double)));
-    TRY(cudaMallocHost((void**)&h->h_rec, capn * REC_STRIDE * sizeof(double)));
-    TRY(cudaMallocHost((void**)&h->h_ft, 6 * capn * sizeof(double)));
-    TRY(cudaMallocHost((void**)&h->h_err, sizeof(unsigned)));
+    TRY(halloc(&h->h_rec, capn * REC_STRIDE * sizeof(double)));
+    TRY(halloc(&h->h_ft, 6 * capn * sizeof(double)));
+    TRY(halloc(&h->h_err, sizeof(unsigned)));
     TRY(dalloc(h, &h->d_jobs, 3 * sizeof(PlaneJob)));
     TRY(dalloc(h, &h->d_pavg, 8 * sizeof(double)));
     TRY(dalloc(h, &h->d_ppart, 3 * PLANE_BLOCKS_MAX * sizeof(double)));
     TRY(dalloc(h, &h->d_pcount, 3 * sizeof(unsigned)));
     TRY(cudaMemset(h->d_pcount, 0, 3 * sizeof(unsigned)));
     TRY(cudaMemset(h->d_pavg, 0, 8 * sizeof(double)));
-    TRY(cudaMallocHost((void**)&h->h_pavg, sizeof(double)));
+    TRY(halloc(&h->h_pavg, sizeof(double)));
 
     TRY(upload_btab(h));
     TRY(cudaMemset(h->f, 0, (size_t)Q * N * h->esz));   // f̄ = 0: rho = 1, u = 0

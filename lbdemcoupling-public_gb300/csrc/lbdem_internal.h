@@ -130,6 +130,7 @@ struct CollideArgs {
     T omega;                 // BGK relaxation frequency
     T g3[3];                 // Guo body-force acceleration
     DivMagic dz, dy;         // division by the z-segments per row and by ny (set by the launchers)
+    int probe_timeout;       // test hook: the first wait of every warp runs out (LBDEM_FLAG_PROBE_TIMEOUT)
 };
 
 // Float table of a particle list, one row of XPF_STRIDE floats per particle:
@@ -232,6 +233,18 @@ __device__ __forceinline__ int find_domain(const int* __restrict__ off, int n, i
 // past their end: the staged collide kernel copies whole 16-byte chunks around
 // unaligned rows.
 constexpr size_t ALLOC_TAIL = 64;
+
+// Test hook of lbdem_debug_fail_allocation: when positive, the allocation that
+// brings it to zero reports failure without being made (device and pinned
+// allocations of lbdem_create and lbdem_batch_create).
+extern std::atomic<int> g_alloc_fail_countdown;
+inline bool alloc_should_fail() {
+    int c = g_alloc_fail_countdown.load(std::memory_order_relaxed);
+    while (c > 0) {
+        if (g_alloc_fail_countdown.compare_exchange_weak(c, c - 1, std::memory_order_relaxed)) return c == 1;
+    }
+    return false;
+}
 
 // Launchers (return cudaGetLastError() of the launch).
 template <typename T>

@@ -25,6 +25,7 @@ LIB_PATH = _PKG / "_build" / "liblbdem_gb300.so"
 PREC_FP64 = 0
 PREC_FP32_DEV = 1
 FLAG_CELL_FORCE = 0x1
+FLAG_PROBE_TIMEOUT = 0x2
 
 FIELD_POPULATIONS = 0
 FIELD_SOLID_FRACTION = 1
@@ -39,6 +40,7 @@ DEVERR_TILE_LIST = 0x1
 DEVERR_TAG_RANGE = 0x4
 DEVERR_UNMAPPED_TAG = 0x8
 DEVERR_RADIUS = 0x10
+DEVERR_TIMEOUT = 0x20
 
 STATUS = {0: "LBDEM_OK", 1: "LBDEM_ERR_INVALID_ARG", 2: "LBDEM_ERR_CUDA", 3: "LBDEM_ERR_OUT_OF_MEMORY",
           4: "LBDEM_ERR_CAPACITY", 5: "LBDEM_ERR_DEVICE", 6: "LBDEM_ERR_NO_DEVICE"}
@@ -80,6 +82,7 @@ PROFILE_POISEUILLE = 1
 
 SIGNATURES = {
     "lbdem_config_default": (None, [C.POINTER(Config)]),
+    "lbdem_debug_fail_allocation": (None, [_I]),
     "lbdem_create": (C.c_int, [C.POINTER(Config), C.POINTER(_P)]),
     "lbdem_destroy": (C.c_int, [_P]),
     "lbdem_last_error": (C.c_char_p, [_P]),
@@ -131,6 +134,11 @@ SIGNATURES = {
     "lbdem_batch_get_tuning": (C.c_int, [_P, C.POINTER(_I), C.POINTER(C.c_float)]),
     "lbdem_batch_set_tuning": (C.c_int, [_P, _I]),
 }
+
+def debug_fail_allocation(nth: int):
+    """lbdem_debug_fail_allocation: the nth allocation of a creation from now on fails (0: off)."""
+    load().lbdem_debug_fail_allocation(int(nth))
+
 
 # Limits of lbdem_voxelize_static (include/lbdem_gpu.h).
 STATIC_MAX_SPHERES = 4096
