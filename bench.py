@@ -49,7 +49,7 @@ for _p in (str(ROOT), str(PKG)):
         sys.path.insert(0, _p)
 
 METRIC = "coupled PSM MLUPS & %HBM roofline, FP32 vs FP64 form at force err ≤1e-4"
-SHAPE = (256, 256, 256)
+SHAPE = (256, 256, 256)   # --edge changes it (profiling runs on smaller cubes)
 TAU = 0.55
 SEED = 2024
 WORKLOAD = "monodisperse suspension, periodic 256^3, 2000 spheres r=8, tau=0.55, prescribed kinematics"
@@ -66,18 +66,25 @@ def peaks():
 
 
 def profiled_traffic():
-    """DRAM bytes per collide-stream launch from the committed ncu summary."""
+    """Per collide-stream launch, from the committed ncu summary
+    (profiles/collide_stream_traffic.txt): DRAM bytes ("fp32", "fp64") and the FP64
+    form's double-precision thread instructions ("fp64_dp_ops")."""
     p = ROOT / "profiles" / "collide_stream_traffic.txt"
     out = {}
     if p.exists():
         for line in p.read_text().splitlines():
             parts = line.split()
-            if len(parts) >= 2 and parts[0] in ("fp32", "fp64"):
+            if len(parts) >= 2 and parts[0] in ("fp32", "fp64", "fp64_dp_ops", "fp64_pipe_active"):
                 try:
                     out[parts[0]] = float(parts[1])
                 except ValueError:
                     pass
     return out
+
+
+def sm_count(device):
+    import torch
+    return int(torch.cuda.get_device_properties(device).multi_processor_count)
 
 
 class ClockSampler:
@@ -131,11 +138,22 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def particles():
+    """The benchmark's spheres: workloads.monodisperse_256 at 256^3; on a smaller cube
+    (--edge) the same construction with the sphere count scaled to the volume
+    (the same solid fraction)."""
+    import workloads as W
+    if SHAPE == (256, 256, 256):
+        return W.monodisperse_256(SEED)[1]
+    n = int(round(2000 * float(np.prod(SHAPE)) / 256 ** 3))
+    return W.suspension(SHAPE, n_max=n, radius=8.0, seed=SEED)
+
+
 def build_tables(n_steps: int):
     """Per-step particle tables (ghost images included) for prescribed kinematics."""
     import workloads as W
     import lbdem
-    _, p = W.monodisperse_256(SEED)
+    p = particles()
     recs, host = [], []
     for _ in range(n_steps):
         g = W.with_ghosts(p, SHAPE)
@@ -390,9 +408,16 @@ def main():
     ap.add_argument("--no-batched", action="store_true", help="skip the batched-channels leg")
     ap.add_argument("--batched-steps", type=int, default=60)
     ap.add_argument("--no-adjoint", action="store_true", help="skip the adjoint-window leg")
+    ap.add_argument("--edge", type=int, default=256,
+                    help="cube edge of the workload (profiling on smaller cases; the benchmark is 256)")
     args = ap.parse_args()
     if args.warmup < 3:
         ap.error("--warmup must be >= 3")
+    global SHAPE, WORKLOAD
+    if args.edge != 256:
+        SHAPE = (args.edge,) * 3
+        WORKLOAD = WORKLOAD.replace("256^3", f"{args.edge}^3").replace(
+            "2000 spheres", f"{int(round(2000 * args.edge ** 3 / 256 ** 3))} spheres")
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -404,7 +429,7 @@ def main():
         if rank != 0:
             return
         import workloads as W
-        _, p = W.monodisperse_256(SEED)
+        p = particles()
         tables = []
         q = p
         for _ in range(min(args.warmup + args.steps, 64)):
@@ -473,6 +498,24 @@ def main():
     v64 = world * N * args.steps / (t64 * 1e-3) / 1e6
     ach32 = BYTES_PER_CELL["fp32"] * N / (r32["k1_ms"] * 1e-3) / 1e9
     ach64 = BYTES_PER_CELL["fp64"] * N / (r64["k1_ms"] * 1e-3) / 1e9 if r64 else None
+    # the coupled step against the same bytes: K1's algorithmic bytes per whole step
+    step32 = BYTES_PER_CELL["fp32"] * N / (t32 / args.steps * 1e-3) / 1e9
+    # FP64 form against its own ceiling: double-precision lanes per clock per SM (2 on
+    # GB300) x SMs x the median SM clock sampled during its run
+    fp64_pipe = None
+    if r64 and traffic.get("fp64_dp_ops") and r64["clocks"].get("sm_mhz"):
+        ops = traffic["fp64_dp_ops"]
+        rate = ops / (r64["k1_ms"] * 1e-3) / 1e12
+        peak_dp = 2.0 * sm_count(device) * r64["clocks"]["sm_mhz"] * 1e6 / 1e12
+        fp64_pipe = {"bound": "fp64", "achieved": rate, "peak": peak_dp, "unit": "T DP lane-ops/s",
+                     "frac": rate / peak_dp, "dp_ops_per_launch": ops, "dp_ops_per_cell": ops / N,
+                     "peak_source": "2 FP64 lanes per clock per SM x SMs x median SM clock of the FP64 run",
+                     "pipe_active_frac": (traffic["fp64_pipe_active"] / 100.0) if traffic.get("fp64_pipe_active")
+                                         else None,
+                     "pipe_note": "achieved/peak counts add/mul/fma only; pipe_active_frac (ncu) counts every "
+                                  "FP64-pipe instruction (conversions, compares, the reciprocal sequence)",
+                     "ops_source": "ncu smsp__sass_thread_inst_executed_op_d{add,mul,fma}_pred_on.sum, "
+                                   "profiles/collide_stream_traffic.txt"}
     ferr = None
     if r64:
         F32, F64 = r32["F"], r64["F"]
@@ -503,13 +546,20 @@ def main():
         "roofline": {"bound": "hbm", "achieved": ach32, "peak": peak, "unit": "GB/s", "frac": ach32 / peak,
                      "traffic": traffic.get("fp32"), "kernel": "k_collide_staged<float> (all axes periodic)",
                      "bytes_per_cell": BYTES_PER_CELL["fp32"], "peak_source": peak_kind,
-                     "k1_ms": r32["k1_ms"], "k2_voxelize_ms": r32["k2_ms"]},
+                     "k1_ms": r32["k1_ms"], "k2_voxelize_ms": r32["k2_ms"],
+                     "step_achieved": step32, "step_frac": step32 / peak,
+                     "step_note": "K1's algorithmic bytes per coupling step / ms_per_step (voxelization, "
+                                  "collide-stream and force sums all inside the step)"},
         "fp64": None if r64 is None else {
             "value": v64, "unit": "MLUPS", "ms_per_step": t64 / args.steps,
-            "roofline": {"bound": "hbm", "achieved": ach64, "peak": peak, "unit": "GB/s", "frac": ach64 / peak,
-                         "traffic": traffic.get("fp64"), "kernel": "k_collide_staged<double> (all axes periodic)",
-                         "bytes_per_cell": BYTES_PER_CELL["fp64"], "k1_ms": r64["k1_ms"],
-                         "k2_voxelize_ms": r64["k2_ms"]}},
+            "vs_cpu": (v64 / cpu["value"]) if cpu else None,
+            "vs_cpu_note": "FP64 form against the FP64 CPU oracle of cpu_baseline (same precision)",
+            "clocks": r64["clocks"],
+            "roofline": fp64_pipe if fp64_pipe else {"bound": "fp64", "achieved": None, "frac": None},
+            "hbm": {"achieved": ach64, "peak": peak, "unit": "GB/s", "frac": ach64 / peak,
+                    "traffic": traffic.get("fp64"), "kernel": "k_collide_staged<double> (all axes periodic)",
+                    "bytes_per_cell": BYTES_PER_CELL["fp64"]},
+            "k1_ms": r64["k1_ms"], "k2_voxelize_ms": r64["k2_ms"]},
         "force_rel_err_fp32_vs_fp64": ferr,
         "batched": batched,
         "adjoint": adjoint,

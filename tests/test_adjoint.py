@@ -241,3 +241,69 @@ def test_fp32_checkpoint_interval_on_aligned_rows(gpu, oracle):
         assert rel_err(o["grad_vel"], outs[0]["grad_vel"]) <= 1e-12
         assert rel_err(o["grad_body_force"], outs[0]["grad_body_force"]) <= 1e-12
         assert abs(o["grad_tau"] - outs[0]["grad_tau"]) <= 1e-12 * abs(outs[0]["grad_tau"])
+
+
+# ---- GPU adjoint as a torch.autograd.Function (check harness) ------------------------------------
+
+class GpuPSMWindow(torch.autograd.Function):
+    """The loss of a window of GPU PSM steps, L = sum_t sum_p w[t][p] . (F_p(t), T_p(t)),
+    as a differentiable torch function of the initial populations f0, the per-step
+    particle velocities and angular velocities vel [nsteps][n][6], the body force g
+    and tau.  forward() runs lbdem_adjoint_window, which returns the loss together
+    with every gradient (forward pass, checkpointed recomputation, hand-written
+    reverse steps); backward() scales them by the incoming gradient.  Positions,
+    radii and tags (rec_base) and the weights are constants."""
+
+    @staticmethod
+    def forward(ctx, f0, vel, g, tau, lb, shape, periodic, rec_base, weights, K, prec):
+        rec = rec_base.copy()
+        rec[:, :, 3:9] = vel.detach().cpu().numpy()
+        with lb.Lattice(*shape, 1.0 / float(tau), periodic=periodic, precision=prec,
+                        body_force=tuple(float(x) for x in g.detach().cpu()), max_particles=64, max_tag=64,
+                        max_radius=8) as L:
+            L.set_populations(f0.detach().cpu().numpy())
+            out = L.adjoint_window(rec, weights, K, want_f0=True)
+        ctx.grads = (torch.from_numpy(np.ascontiguousarray(out["grad_f0"], dtype=np.float64)).reshape(f0.shape),
+                     torch.from_numpy(out["grad_vel"].copy()), torch.from_numpy(out["grad_body_force"].copy()),
+                     torch.tensor(out["grad_tau"], dtype=torch.float64))
+        return torch.tensor(out["loss"], dtype=torch.float64)
+
+    @staticmethod
+    def backward(ctx, gout):
+        gf0, gvel, gg, gtau = ctx.grads
+        return gout * gf0, gout * gvel, gout * gg, gout * gtau, None, None, None, None, None, None, None
+
+
+@pytest.mark.gpu
+def test_autograd_function_backward_matches_full_tape(gpu, oracle):
+    """loss.backward() through GpuPSMWindow, inside a larger graph (the velocities
+    are a scaled copy of a base table, tau and g derived tensors), against the
+    float64 torch model's full tape on the same graph: loss 1e-12, every leaf
+    gradient 1e-10."""
+    c = case((16, 14, 18), (1, 0, 0), 3, 11, 12)
+    ol = initial_state(oracle, c)
+    f0_np = ol.get_populations().astype(np.float64)
+    vel_np = np.concatenate([c["rec"][:, :, 3:6], c["rec"][:, :, 6:9]], axis=2)
+    model = torch_model(ol, c)
+    grads = []
+    for use_gpu in (True, False):
+        f0 = torch.tensor(f0_np, requires_grad=True)
+        base = torch.tensor(vel_np, requires_grad=True)
+        scale = torch.tensor(1.3, dtype=torch.float64, requires_grad=True)
+        lt = torch.tensor(np.log(TAU), dtype=torch.float64, requires_grad=True)
+        g = torch.tensor(c["g"], dtype=torch.float64, requires_grad=True)
+        vel, tau = scale * base, torch.exp(lt)
+        if use_gpu:
+            loss = GpuPSMWindow.apply(f0, vel, g, tau, gpu, c["shape"], c["periodic"], c["rec"], c["weights"], 4, 0)
+        else:
+            loss, _ = model.window(f0.reshape(19, -1), vel, torch.tensor(c["weights"]), tau, g)
+        (2.0 * loss).backward()
+        grads.append({"loss": float(loss.detach()), "f0": f0.grad.numpy().reshape(19, -1), "base": base.grad.numpy(),
+                      "scale": float(scale.grad), "lt": float(lt.grad), "g": g.grad.numpy()})
+    got, ref = grads
+    assert abs(got["loss"] - ref["loss"]) <= 1e-12 * abs(ref["loss"])
+    for k in ("f0", "base", "g"):
+        assert rel_err(got[k], ref[k]) <= 1e-10, k
+    for k in ("scale", "lt"):
+        assert abs(got[k] - ref[k]) <= 1e-10 * abs(ref[k]), k
+    assert abs(ref["scale"]) > 0 and abs(ref["lt"]) > 0
