@@ -1063,8 +1063,9 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
         const int sl = s0 >= 0 ? s0 : s1;
         if (sl >= 0) {
             const TableRow r = load_row(a.xpf, sl);
-            if (s0 >= 0) row_velocity(r, sx, sy, za, g, ua[0], ua[1], ua[2]);
-            if (s1 == sl) row_velocity(r, sx, sy, zb, g, ub[0], ub[1], ub[2]);
+            const RowPart rp = row_part(r, sx, sy, g);
+            if (s0 >= 0) cell_part(r, rp, za, g, ua[0], ua[1], ua[2]);
+            if (s1 == sl) cell_part(r, rp, zb, g, ub[0], ub[1], ub[2]);
         }
         if (s1 >= 0 && s1 != sl) row_velocity(load_row(a.xpf, s1), sx, sy, zb, g, ub[0], ub[1], ub[2]);
 #pragma unroll

@@ -162,15 +162,28 @@ __host__ __device__ __forceinline__ float min_image_f(float d, int n, int per) {
     if (d < (float)-h) return d + (float)n;
     return d;
 }
-__device__ __forceinline__ void row_velocity(const TableRow& r, int x, int y, int z, const Geom& g, float& u0,
-                                             float& u1, float& u2) {
+// The row part (x, y fixed) of the velocity: c = v + omega x (dx, dy, 0).
+struct RowPart {
+    float c0, c1, c2;
+};
+__device__ __forceinline__ RowPart row_part(const TableRow& r, int x, int y, const Geom& g) {
     const float dx = min_image_f(__fsub_rn(__fsub_rn((float)x, r.a.x), r.a.w), g.nx, g.per[0]);
     const float dy = min_image_f(__fsub_rn(__fsub_rn((float)y, r.a.y), r.b.x), g.ny, g.per[1]);
-    const float dz = min_image_f(__fsub_rn(__fsub_rn((float)z, r.a.z), r.b.y), g.nz, g.per[2]);
     // v = (b.z, b.w, c.x), omega = (c.y, c.z, c.w)
-    u0 = __fadd_rn(r.b.z, __fsub_rn(__fmul_rn(r.c.z, dz), __fmul_rn(r.c.w, dy)));
-    u1 = __fadd_rn(r.b.w, __fsub_rn(__fmul_rn(r.c.w, dx), __fmul_rn(r.c.y, dz)));
-    u2 = __fadd_rn(r.c.x, __fsub_rn(__fmul_rn(r.c.y, dy), __fmul_rn(r.c.z, dx)));
+    return RowPart{__fsub_rn(r.b.z, __fmul_rn(r.c.w, dy)), __fadd_rn(r.b.w, __fmul_rn(r.c.w, dx)),
+                   __fadd_rn(r.c.x, __fsub_rn(__fmul_rn(r.c.y, dy), __fmul_rn(r.c.z, dx)))};
+}
+// ... plus the z part omega x (0, 0, dz)
+__device__ __forceinline__ void cell_part(const TableRow& r, const RowPart& p, int z, const Geom& g, float& u0,
+                                          float& u1, float& u2) {
+    const float dz = min_image_f(__fsub_rn(__fsub_rn((float)z, r.a.z), r.b.y), g.nz, g.per[2]);
+    u0 = __fadd_rn(p.c0, __fmul_rn(r.c.z, dz));
+    u1 = __fsub_rn(p.c1, __fmul_rn(r.c.y, dz));
+    u2 = p.c2;
+}
+__device__ __forceinline__ void row_velocity(const TableRow& r, int x, int y, int z, const Geom& g, float& u0,
+                                             float& u1, float& u2) {
+    cell_part(r, row_part(r, x, y, g), z, g, u0, u1, u2);
 }
 __device__ __forceinline__ void table_velocity(const float* __restrict__ row, int x, int y, int z, const Geom& g,
                                                float& u0, float& u1, float& u2) {
