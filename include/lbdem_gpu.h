@@ -52,7 +52,8 @@ typedef enum {
 } lbdem_status;
 
 /* Bits of the device error word (lbdem_get_device_errors). */
-#define LBDEM_DEVERR_TILE_LIST     0x1u  /* an 8^3-cell tile is overlapped by > 1024 spheres */
+#define LBDEM_DEVERR_TILE_LIST     0x1u  /* kept for compatibility; no longer raised (a tile's
+                                            spheres are re-collected without a limit)        */
 #define LBDEM_DEVERR_TAG_RANGE     0x4u  /* a particle tag is < 1 or > max_tag              */
 #define LBDEM_DEVERR_UNMAPPED_TAG  0x8u  /* a solid cell names a tag with no particle       */
 #define LBDEM_DEVERR_RADIUS        0x10u /* a radius is not finite, <= 0 or > max_radius    */
