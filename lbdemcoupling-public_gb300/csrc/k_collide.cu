@@ -27,8 +27,9 @@
 // fPre of the PSM update.  The FP32 form collides two cells per thread in packed
 // f32x2 arithmetic (collide_segment_pairs) and recomputes the particle surface
 // velocity of its solid cells from the owner particle's row of the float table
-// (no per-cell velocity field); the FP64 form one cell per thread in the
-// reference's double sequence, with the velocity setValues stored.  The same
+// (no per-cell velocity field); the FP64 form one cell per thread in double,
+// BGK and solid correction in one pass (collide_cell_fp64; with a body force
+// collide_cell), with the velocity setValues stored.  The same
 // kernel steps many independent domains in one launch (batch mode).
 #include "lbdem_internal.h"
 
@@ -204,6 +205,119 @@ __device__ __forceinline__ void collide_cell(const CollideArgs<T>& a, T (&f)[Q],
 }
 
 // ---------------------------------------------------------------------------
+// FP64 form without a body force: the base BGK (src/ibCompositeDynamics3D.hh:139-140)
+// and the solid correction (:150-200) of a cell in one pass over the opposite
+// pairs (i = 1..9, k = i + 9, c_k = -c_i), written around the non-equilibrium
+// parts g = fPre - feq.  With the solid equilibrium feqS at P = (1 + rhoBar) uPart
+// (:154), Dl = feq - feqS and alpha = omega (1 - B) + B, the reference's
+//   out = fPre + (1 - B)(fBGK - fPre) + bb,  fBGK = fPre - omega g,
+// becomes
+//   out_i = fPre_i - alpha g_i + B (g_k - Dl_i),   out_k = fPre_k - alpha g_k + B (g_i - Dl_k),
+//   out_0 = fPre_0 - omega (1 - B) g_0 + B Dl_0     (the rest-population sign, :161, :185),
+//   F -= c_i (bb - bbOpp) = c_k 2 B ((fPre_k - fPre_i) - 3 t c_k.(j + P))   (:172-174),
+// where, with cj = c_k.j and cP = c_k.P,
+//   feq_{k,i} = C +/- 3 t cj,  C = t (rhoBar + invRho (4.5 cj^2 - 1.5 j.j)),
+//   Dl_{k,i} = Qd +/- 3 t (cj - cP),  Qd = t invRho (4.5 (cj - cP)(cj + cP) - 1.5 (j.j - P.P)),
+//   Dl_0 = t_0 (-1.5 invRho (j.j - P.P)).
+// n = 125 gives B = 1 (no BGK, alpha = 1), n = 0 gives B = 0 (the BGK result).
+// The moments are those of fPre: without a body force BGK conserves them, and the
+// reference's post-collision recomputation (:146-148) differs by rounding only.
+// SOLID false (a warp without solid cells) leaves out the solid terms; a fluid
+// cell gets the same bits either way, so results do not depend on which cells
+// share a warp.
+template <int AX>
+__device__ __forceinline__ double pair_sum(const double (&d)[9]) {
+    // sum_k c_k[AX] d[k - 10] over the directions k = 10..18 with c_k[AX] != 0, in k order
+    double r = 0.0;
+    bool any = false;
+#pragma unroll
+    for (int k = 10; k < Q; ++k) {
+        const int c = AX == 0 ? cx(k) : (AX == 1 ? cy(k) : cz(k));
+        if (c == 0) continue;
+        const double v = d[k - 10];
+        r = any ? (c > 0 ? r + v : r - v) : (c > 0 ? v : -v);
+        any = true;
+    }
+    return r;
+}
+
+template <bool SOLID>
+__device__ __forceinline__ void collide_cell_fp64(double (&f)[Q], double omega, double B, double up0, double up1,
+                                                  double up2, double& Fx, double& Fy, double& Fz) {
+    double d[9];
+    double rhoBar;
+    {
+        double s[9];
+#pragma unroll
+        for (int i = 1; i <= 9; ++i) {
+            s[i - 1] = f[i] + f[i + 9];
+            d[i - 1] = f[i + 9] - f[i];
+        }
+        rhoBar = f[0] + ((((s[0] + s[1]) + (s[2] + s[3])) + ((s[4] + s[5]) + (s[6] + s[7]))) + s[8]);
+    }
+    const double jx = pair_sum<0>(d), jy = pair_sum<1>(d), jz = pair_sum<2>(d);
+    const double invRho = recip(1.0 + rhoBar);
+    const double jSqr = fma(jz, jz, fma(jy, jy, jx * jx));
+    const double m15 = -1.5 * invRho;
+    const double base = fma(m15, jSqr, rhoBar);
+    double Px = 0.0, Py = 0.0, Pz = 0.0, dd = 0.0, alpha = omega, om1B = omega;
+    if (SOLID) {
+        const double rho = 1.0 + rhoBar;
+        Px = up0 * rho; Py = up1 * rho; Pz = up2 * rho;
+        const double PSqr = fma(Pz, Pz, fma(Py, Py, Px * Px));
+        dd = m15 * (jSqr - PSqr);
+        alpha = fma(B, 1.0 - omega, omega);
+        om1B = omega * (1.0 - B);
+    }
+    {
+        const double g0 = f[0] - wt(0) * base;
+        f[0] = SOLID ? fma(B, wt(0) * dd, fma(-om1B, g0, f[0])) : fma(-omega, g0, f[0]);
+    }
+    double Ex = 0.0, Ey = 0.0, Ez = 0.0;
+    bool fx0 = false, fy0 = false, fz0 = false;
+#pragma unroll
+    for (int k = 10; k < Q; ++k) {
+        const int i = k - 9;
+        const double t = wt(k), t3 = 3.0 * wt(k);
+        const double a45 = (4.5 * wt(k)) * invRho;
+        const double cj = cdot(k, jx, jy, jz);
+        const double C = fma(a45 * cj, cj, t * base);
+        const double Lj = t3 * cj;
+        const double gi = (f[i] - C) + Lj;
+        const double gk = (f[k] - C) - Lj;
+        if (SOLID) {
+            const double cP = cdot(k, Px, Py, Pz);
+            const double m = cj - cP, p = cj + cP;
+            const double Qd = fma(a45 * m, p, t * dd);
+            const double L = t3 * m;
+            const double e = d[i - 1] - t3 * p;
+            f[i] = fma(B, (gk - Qd) + L, fma(-alpha, gi, f[i]));
+            f[k] = fma(B, (gi - Qd) - L, fma(-alpha, gk, f[k]));
+            if (cx(k) != 0) { Ex = fx0 ? (cx(k) > 0 ? Ex + e : Ex - e) : (cx(k) > 0 ? e : -e); fx0 = true; }
+            if (cy(k) != 0) { Ey = fy0 ? (cy(k) > 0 ? Ey + e : Ey - e) : (cy(k) > 0 ? e : -e); fy0 = true; }
+            if (cz(k) != 0) { Ez = fz0 ? (cz(k) > 0 ? Ez + e : Ez - e) : (cz(k) > 0 ? e : -e); fz0 = true; }
+        } else {
+            f[i] = fma(-omega, gi, f[i]);
+            f[k] = fma(-omega, gk, f[k]);
+        }
+    }
+    const double B2 = B + B;
+    Fx = SOLID ? B2 * Ex : 0.0;
+    Fy = SOLID ? B2 * Ey : 0.0;
+    Fz = SOLID ? B2 * Ez : 0.0;
+}
+
+// Per-cell force and torque added to the particle's sums (FP64 form): six
+// double atomics per solid cell, resolved in L2 instead of a warp scan on the
+// FP64 pipe.
+__device__ __forceinline__ void add_cell_force(const CollideArgs<double>& a, int slot, const double (&v)[6]) {
+    double* Fp = a.ft + 3 * (size_t)slot;
+    double* Tp = a.ft + 3 * (size_t)a.nslot + 3 * (size_t)slot;
+    atomicAdd(Fp + 0, v[0]); atomicAdd(Fp + 1, v[1]); atomicAdd(Fp + 2, v[2]);
+    atomicAdd(Tp + 0, v[3]); atomicAdd(Tp + 1, v[4]); atomicAdd(Tp + 2, v[5]);
+}
+
+// ---------------------------------------------------------------------------
 // FP32 form: two cells per thread in packed f32x2 arithmetic (sm_100 family
 // add/sub/mul/fma .f32x2), the cells z and z + 1 of one row.  The same update as
 // collide_cell, arranged per opposite pair around the direction k = i + 9 (every
@@ -214,8 +328,7 @@ __device__ __forceinline__ void collide_cell(const CollideArgs<T>& a, T (&f)[Q],
 //     cell runs it for both without a select;
 //   * with the Guo force the solid correction's momentum is the BGK post-collision
 //     momentum j + rho g (exact in arithmetic) instead of a second moment sum.
-// Rounding differs from collide_cell at the float level; the FP64 form keeps
-// collide_cell and the reference's double sequence.
+// Rounding differs from the FP64 form at the float level.
 struct F2 {
     unsigned long long r;
 };
@@ -1315,12 +1428,16 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
             // FP32 form: packed pairs of cells
             collide_segment_pairs<ODD, FORCE, PER, MIS, STAGE_UP>(a, st, b, sx, sy, z0, len, srcrow, lead);
         } else {
-            // FP64 form: one cell per lane at a time, the reference's double sequence
+            // FP64 form: one cell per lane at a time; force and torque per cell with
+            // double atomics
             const int vlead = MIS ? (int)((lead >> 38) & 3u) : 0;
 #pragma unroll 1
             for (int j = lane; j < SEGW; j += 32) {
                 int key = -1;
                 T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+                const uint32_t w = j < len ? st.vox[b][vlead + j] : 0u;
+                // warp-uniform: the solid terms run only in warps that hold a solid cell
+                const bool any_solid = __any_sync(FULL, (w & VOX_NMASK) != 0u);
                 if (j < len) {
                     const int z = z0 + j;
                     const size_t c = own + z;
@@ -1334,14 +1451,24 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
                     T f[Q];
 #pragma unroll
                     for (int i = 0; i < Q; ++i) f[i] = at(i);
-                    const uint32_t w = st.vox[b][vlead + j];
                     T Fx, Fy, Fz;
                     auto upv = [&](int d) -> T {
                         if (!STAGE_UP) return __ldg(a.up + (size_t)d * N + c);
                         const int m = MIS ? (int)((lead >> (40 + 2 * d)) & 3u) : 0;
                         return st.up[b][d][m + j];
                     };
-                    collide_cell<T, FORCE>(a, f, w, [&](int i) { return at(i); }, upv, Fx, Fy, Fz);
+                    if constexpr (!FORCE) {
+                        const int n = min((int)(w & VOX_NMASK), 125);
+                        if (any_solid) {
+                            const bool s = n > 0;   // a fluid cell's velocity slot is not read
+                            collide_cell_fp64<true>(f, a.omega, __ldg(a.btab + n), s ? upv(0) : T(0),
+                                                    s ? upv(1) : T(0), s ? upv(2) : T(0), Fx, Fy, Fz);
+                        } else {
+                            collide_cell_fp64<false>(f, a.omega, T(0), T(0), T(0), T(0), Fx, Fy, Fz);
+                        }
+                    } else {
+                        collide_cell<T, FORCE>(a, f, w, [&](int i) { return at(i); }, upv, Fx, Fy, Fz);
+                    }
                     if (!ODD) {
 #pragma unroll
                         for (int i = 0; i < Q; ++i) F[(size_t)opp(i) * N + c] = f[i];
@@ -1359,8 +1486,8 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
                     }
                     if (a.cf) { a.cf[c] = Fx; a.cf[N + c] = Fy; a.cf[2 * N + c] = Fz; }
                     key = cell_force_terms(a, w, sx, sy, z, Fx, Fy, Fz, v);
+                    if (key >= 0) add_cell_force(a, key, v);
                 }
-                reduce_forces(a, key, v);
             }
         }
         __syncwarp();   // buffer b is free for the segment after next

@@ -346,6 +346,7 @@ struct alignas(16) WarpVox {
     uint32_t defv[INIT_VEL ? TILE_CELLS : 1];
     uint32_t cnt4[TILE_CELLS / 4];                  // shell sub-cell counts, one byte per cell
     uint16_t queue[TILE_CELLS];                     // shell cells of the current sphere
+    uint8_t items[5 * 32];                          // x-slices left to count: (cell in chunk) << 3 | slice
 };
 
 // decFlag, src/ibProcessors3D.hh:85-105 (sf > 0.001 <=> n > 0; sf > sf_old <=>
@@ -404,7 +405,6 @@ __device__ __noinline__ void apply_sphere(WarpVox<INIT_VEL>& S, const SphereFast
         const unsigned bal = __ballot_sync(FULL_MASK, region == 2);
         if (region == 2) {
             S.queue[qn + __popc(bal & below)] = (uint16_t)l;
-            cnt8[l] = 0;
         } else if (region >= 0) {
             fold_cell(S, l, region == 1 ? 125u : 0u, tag, m);
         }
@@ -412,20 +412,66 @@ __device__ __noinline__ void apply_sphere(WarpVox<INIT_VEL>& S, const SphereFast
     }
     if (qn == 0) return;
     __syncwarp();
-    // 2: counts of the queued cells by x-slice
-    for (int u = lane; u < 5 * qn; u += 32) {
-        const int e = u / 5, i = u - 5 * e;
-        const int l = S.queue[e];
-        const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
-        const float dxf = ((float)X - q.xh[0]) - q.xl[0];
-        const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
-        const float dzq = ((float)Z - q.xh[2]) - q.xl[2];
-        bool unsure;
-        int cs = slice_count_fast(dxf, dyf, dzq, i, q.rsq, M, &unsure);
-        if (unsure) cs = slice_count_resolve(dxf, dyf, dzq, i, q.rsq, M, X, Y, Z, sph[m]);
-        if (cs) atomicAdd(&S.cnt4[l >> 2], (uint32_t)cs << (8 * (l & 3)));
+    // 2: counts of the queued cells, 32 at a time.  Lane `lane` takes queued
+    // cell c0 + lane and decides each x-slice from its largest and smallest
+    // sample sums, (xs_i + max ys) + max zs and (xs_i + min ys) + min zs: these
+    // are samples of the slice, and the rounded sums are monotone in every term,
+    // so a bound farther than M from r^2 decides all 25 samples as the
+    // per-sample rule would (25 inside, or none).  The slices left are queued
+    // and counted sample by sample, one slice per lane.
+    for (int c0 = 0; c0 < qn; c0 += 32) {
+        uint32_t mixed = 0u;
+        if (c0 + lane < qn) {
+            const int l = S.queue[c0 + lane];
+            const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
+            const float dxf = ((float)X - q.xh[0]) - q.xl[0];
+            const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
+            const float dzq = ((float)Z - q.xh[2]) - q.xl[2];
+            float ymin = 3.0e38f, ymax = 0.f, zmin = 3.0e38f, zmax = 0.f;
+#pragma unroll
+            for (int j = 0; j < 5; ++j) {
+                const float d = sub_delta_f(j);
+                const float ay = __fadd_rn(dyf, d), az = __fadd_rn(dzq, d);
+                const float ys = __fmul_rn(ay, ay), zs = __fmul_rn(az, az);
+                ymin = fminf(ymin, ys); ymax = fmaxf(ymax, ys);
+                zmin = fminf(zmin, zs); zmax = fmaxf(zmax, zs);
+            }
+            int inside = 0;
+#pragma unroll
+            for (int i = 0; i < 5; ++i) {
+                const float ax = __fadd_rn(dxf, sub_delta_f(i));
+                const float xs = __fmul_rn(ax, ax);
+                const float hi = __fsub_rn(__fadd_rn(__fadd_rn(xs, ymax), zmax), q.rsq);
+                const float lo = __fsub_rn(__fadd_rn(__fadd_rn(xs, ymin), zmin), q.rsq);
+                if (hi < -M) inside += 25;
+                else if (!(lo > M)) mixed |= 1u << i;
+            }
+            cnt8[l] = (uint8_t)inside;
+        }
+        const int k = __popc(mixed);
+        int incl = k;
+#pragma unroll
+        for (int d = 1; d < 32; d <<= 1) {
+            const int o = __shfl_up_sync(FULL_MASK, incl, d);
+            if (lane >= d) incl += o;
+        }
+        const int total = __shfl_sync(FULL_MASK, incl, 31);
+        for (int pos = incl - k; mixed; mixed &= mixed - 1u) S.items[pos++] = (uint8_t)((lane << 3) | (__ffs(mixed) - 1));
+        __syncwarp();
+        for (int u = lane; u < total; u += 32) {
+            const int it = S.items[u];
+            const int l = S.queue[c0 + (it >> 3)], i = it & 7;
+            const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
+            const float dxf = ((float)X - q.xh[0]) - q.xl[0];
+            const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
+            const float dzq = ((float)Z - q.xh[2]) - q.xl[2];
+            bool unsure;
+            int cs = slice_count_fast(dxf, dyf, dzq, i, q.rsq, M, &unsure);
+            if (unsure) cs = slice_count_resolve(dxf, dyf, dzq, i, q.rsq, M, X, Y, Z, sph[m]);
+            if (cs) atomicAdd(&S.cnt4[l >> 2], (uint32_t)cs << (8 * (l & 3)));
+        }
+        __syncwarp();
     }
-    __syncwarp();
     // 3
     for (int e = lane; e < qn; e += 32) {
         const int l = S.queue[e];
