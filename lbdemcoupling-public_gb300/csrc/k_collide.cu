@@ -307,6 +307,24 @@ __device__ __forceinline__ void collide_cell_fp64(double (&f)[Q], double omega, 
     Fz = SOLID ? B2 * Ez : 0.0;
 }
 
+// Position of the k-th set bit (k = 0: the lowest) of m; k < popc(m).
+__device__ __forceinline__ int nth_bit(unsigned m, int k) {
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const unsigned lo = m & ((1u << w) - 1u);
+        const int c = __popc(lo);
+        if (k >= c) {
+            k -= c;
+            m >>= w;
+            pos += w;
+        } else {
+            m = lo;
+        }
+    }
+    return pos;
+}
+
 // Per-cell force and torque added to the particle's sums (FP64 form): six
 // double atomics per solid cell, resolved in L2 instead of a warp scan on the
 // FP64 pipe.
@@ -1429,16 +1447,31 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
             collide_segment_pairs<ODD, FORCE, PER, MIS, STAGE_UP>(a, st, b, sx, sy, z0, len, srcrow, lead);
         } else {
             // FP64 form: one cell per lane at a time; force and torque per cell with
-            // double atomics
+            // double atomics.  The segment's solid cells are taken first (pass 0
+            // holds as many of them as fit): a pass whose warp holds a solid cell
+            // runs the solid terms for every lane, so gathering them leaves more
+            // passes on the BGK-only path.  A cell's result does not depend on
+            // its pass.
+            static_assert(SEGW == 64, "two passes of 32 cells per segment");
             const int vlead = MIS ? (int)((lead >> 38) & 3u) : 0;
+            const uint32_t wl0 = lane < len ? st.vox[b][vlead + lane] : 0u;
+            const uint32_t wl1 = lane + 32 < len ? st.vox[b][vlead + lane + 32] : 0u;
+            const unsigned sol0 = __ballot_sync(FULL, (wl0 & VOX_NMASK) != 0u);
+            const unsigned sol1 = __ballot_sync(FULL, (wl1 & VOX_NMASK) != 0u);
+            const unsigned flu0 = __ballot_sync(FULL, lane < len) & ~sol0;
+            const unsigned flu1 = __ballot_sync(FULL, lane + 32 < len) & ~sol1;
+            const int ns0 = __popc(sol0), ns = ns0 + __popc(sol1);
+            const int nf0 = __popc(flu0), nf = nf0 + __popc(flu1);
 #pragma unroll 1
-            for (int j = lane; j < SEGW; j += 32) {
-                int key = -1;
+            for (int p = 0; p < 2; ++p) {
+                const int slot = 32 * p + lane;
+                int j = -1;   // the cell this lane takes in pass p
+                if (slot < ns) j = slot < ns0 ? nth_bit(sol0, slot) : 32 + nth_bit(sol1, slot - ns0);
+                else if (slot - ns < nf) j = slot - ns < nf0 ? nth_bit(flu0, slot - ns) : 32 + nth_bit(flu1, slot - ns - nf0);
+                const bool any_solid = ns > 32 * p;   // warp-uniform
                 T v[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-                const uint32_t w = j < len ? st.vox[b][vlead + j] : 0u;
-                // warp-uniform: the solid terms run only in warps that hold a solid cell
-                const bool any_solid = __any_sync(FULL, (w & VOX_NMASK) != 0u);
-                if (j < len) {
+                if (j >= 0) {
+                    const uint32_t w = st.vox[b][vlead + j];
                     const int z = z0 + j;
                     const size_t c = own + z;
                     // smem index of direction i: V + lead_i + j - shift_i, shift_i = c_z,i
@@ -1485,7 +1518,7 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
                         }
                     }
                     if (a.cf) { a.cf[c] = Fx; a.cf[N + c] = Fy; a.cf[2 * N + c] = Fz; }
-                    key = cell_force_terms(a, w, sx, sy, z, Fx, Fy, Fz, v);
+                    const int key = cell_force_terms(a, w, sx, sy, z, Fx, Fy, Fz, v);
                     if (key >= 0) add_cell_force(a, key, v);
                 }
             }
