@@ -75,10 +75,14 @@ struct CellAdj {
 // Reverse of one cell.  f: pre-collision populations; mu: adjoint of the
 // post-collision populations; a: adjoint of the cell force.  Accumulates
 // d/duP, d/dtau, d/dg and returns the scalars lambda is built from.
+// general (warp-uniform: the warp holds a solid cell): a fluid cell takes the
+// solid cells' path too, with B = 0, where it yields B = 0, sB = 1 and zero
+// grbs, gjs, guP, so phi = mu and the same bits as the fluid path; the warp
+// then runs one path instead of both.
 template <typename T>
-__device__ __forceinline__ CellAdj<T> adjoint_cell(const T (&f)[Q], const T (&mu)[Q], int n, T B, T dBdtau,
-                                                   const T (&uP)[3], const T (&a)[3], T omega, const T (&g)[3],
-                                                   T (&guP)[3], T& gtau, T (&gg)[3]) {
+__device__ __forceinline__ CellAdj<T> adjoint_cell(const T (&f)[Q], const T (&mu)[Q], int n, bool general, T B,
+                                                   T dBdtau, const T (&uP)[3], const T (&a)[3], T omega,
+                                                   const T (&g)[3], T (&guP)[3], T& gtau, T (&gg)[3]) {
     CellAdj<T> R;
     // pre-collision moments
     T rb = T(0), j0 = T(0), j1 = T(0), j2 = T(0);
@@ -98,7 +102,7 @@ __device__ __forceinline__ CellAdj<T> adjoint_cell(const T (&f)[Q], const T (&mu
 
     R.B = T(0); R.sB = T(1); R.grbs = T(0); R.gjs0 = T(0); R.gjs1 = T(0); R.gjs2 = T(0);
     guP[0] = guP[1] = guP[2] = T(0);
-    if (n > 0) {
+    if (n > 0 || general) {
         // moments of f* and S1 = sum mu_k f*_k
         T rbs = T(0), js0 = T(0), js1 = T(0), js2 = T(0), S1 = T(0);
         if (n == 125) {
@@ -197,7 +201,7 @@ __device__ __forceinline__ CellAdj<T> adjoint_cell(const T (&f)[Q], const T (&mu
             if (Y && Z) myz += Y * Z > 0 ? wp : -wp;
         }
     };
-    if (n == 0) moments([&](int k) { return mu[k]; });   // fluid cell: phi = mu
+    if (!general) moments([&](int k) { return mu[k]; });   // fluid cells only: phi = mu
     else moments([&](int k) { return R.sB * mu[k] + R.grbs + cdotT<T>(k, R.gjs0, R.gjs1, R.gjs2); });
     // m2 applied to J, u, g
     const T aJ0 = mxx * J0 + mxy * J1 + mxz * J2v, aJ1 = mxy * J0 + myy * J1 + myz * J2v,
@@ -267,8 +271,9 @@ __device__ __forceinline__ void reduce6(int key, T (&v)[6], double* __restrict__
         for (int q = 0; q < 6; ++q) atomicAdd(out + 6 * (size_t)key + q, (double)v[q]);
 }
 
-template <typename T>
-__global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_step(const AdjointArgs<T> A) {
+// PER: every axis periodic (no wall cases in the neighbour lookups).
+template <typename T, bool PER>
+__global__ void __launch_bounds__(ADJ_THREADS, sizeof(T) == 4 ? 2 : 1) k_adjoint_step(const AdjointArgs<T> A) {
     __shared__ double s_red[ADJ_THREADS / 32][4];
     const Geom g = A.g;
     const size_t N = g.N;
@@ -285,25 +290,28 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_step(const AdjointArgs<
         const int z = (qi - row * nzc) * 32 + lane;
         int key = -1;
         T pv[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+        // warp-uniform: some cell of the run is solid
+        const bool general = __any_sync(FULLMASK, z < g.nz && (A.vox[(size_t)row * g.nz + z] & VOX_NMASK) != 0u);
         if (z < g.nz) {
             const int x = row / g.ny;
             const int y = row - x * g.ny;
             const size_t c = (size_t)row * g.nz + z;
             // neighbour coordinates (-1 beyond a wall) and the nine row offsets
-            const int xs[3] = {x > 0 ? x - 1 : (g.per[0] ? g.nx - 1 : -1), x, x < g.nx - 1 ? x + 1 : (g.per[0] ? 0 : -1)};
-            const int ys[3] = {y > 0 ? y - 1 : (g.per[1] ? g.ny - 1 : -1), y, y < g.ny - 1 ? y + 1 : (g.per[1] ? 0 : -1)};
-            const int zs[3] = {z > 0 ? z - 1 : (g.per[2] ? g.nz - 1 : -1), z, z < g.nz - 1 ? z + 1 : (g.per[2] ? 0 : -1)};
+            const bool p0 = PER || g.per[0], p1 = PER || g.per[1], p2 = PER || g.per[2];
+            const int xs[3] = {x > 0 ? x - 1 : (p0 ? g.nx - 1 : -1), x, x < g.nx - 1 ? x + 1 : (p0 ? 0 : -1)};
+            const int ys[3] = {y > 0 ? y - 1 : (p1 ? g.ny - 1 : -1), y, y < g.ny - 1 ? y + 1 : (p1 ? 0 : -1)};
+            const int zs[3] = {z > 0 ? z - 1 : (p2 ? g.nz - 1 : -1), z, z < g.nz - 1 ? z + 1 : (p2 ? 0 : -1)};
             long long rowoff[9];
 #pragma unroll
             for (int a = 0; a < 3; ++a)
 #pragma unroll
                 for (int b = 0; b < 3; ++b)
-                    rowoff[3 * a + b] = (xs[a] >= 0 && ys[b] >= 0) ? ((long long)xs[a] * g.ny + ys[b]) * g.nz : -1;
+                    rowoff[3 * a + b] = (PER || (xs[a] >= 0 && ys[b] >= 0)) ? ((long long)xs[a] * g.ny + ys[b]) * g.nz : -1;
             // cell x + (dx, dy, dz) as a linear index, or -1 beyond a wall
             auto nb = [&](int dx, int dy, int dz) -> long long {
                 const long long r = rowoff[3 * (dx + 1) + dy + 1];
                 const int zz = zs[dz + 1];
-                return (r >= 0 && zz >= 0) ? r + zz : -1;
+                return (PER || (r >= 0 && zz >= 0)) ? r + zz : -1;
             };
             T f[Q], mu[Q];
             if (A.phase == 0) {
@@ -377,17 +385,18 @@ __global__ void __launch_bounds__(ADJ_THREADS) k_adjoint_step(const AdjointArgs<
             if (n > 0 && slot < 0) n = 0;
             T guP[3];
             const T gvec[3] = {A.g3[0], A.g3[1], A.g3[2]};
-            const CellAdj<T> R = adjoint_cell<T>(f, mu, n, B, dBdtau, uP, a, A.omega, gvec, guP, gtau, gg);
+            const CellAdj<T> R = adjoint_cell<T>(f, mu, n, general, B, dBdtau, uP, a, A.omega, gvec, guP, gtau, gg);
             const T om1 = n == 125 ? T(1) : T(1) - A.omega;
-            if (n == 0) {   // fluid cell: phi = mu, no solid terms
+            if (!general) {   // fluid cells only: phi = mu, no solid terms
 #pragma unroll
                 for (int k = 0; k < Q; ++k)
                     A.lam_out[(size_t)k * N + c] = om1 * mu[k] + (R.grb + cdotT<T>(k, R.gJ0, R.gJ1, R.gJ2));
             } else {
+                // the fluid path's expression plus the solid terms (exactly zero for a fluid cell)
 #pragma unroll
                 for (int k = 0; k < Q; ++k) {
                     const T phi = R.sB * mu[k] + R.grbs + cdotT<T>(k, R.gjs0, R.gjs1, R.gjs2);
-                    T l = om1 * phi + R.grb + cdotT<T>(k, R.gJ0, R.gJ1, R.gJ2);
+                    T l = om1 * phi + (R.grb + cdotT<T>(k, R.gJ0, R.gJ1, R.gJ2));
                     l += R.B * mu[opp(k)] + T(2) * R.B * cdotT<T>(k, a[0], a[1], a[2]);
                     A.lam_out[(size_t)k * N + c] = l;
                 }
@@ -453,14 +462,17 @@ cudaError_t launch_adjoint_step(const AdjointArgs<T>& a, cudaStream_t s) {
         int sms = 0, per_sm = 0;
         e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         if (e == cudaSuccess)
-            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adjoint_step<T>, ADJ_THREADS, 0);
+            e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_adjoint_step<T, false>, ADJ_THREADS, 0);
         if (e != cudaSuccess) return e;
         blocks = sms * (per_sm > 0 ? per_sm : 1);
         cached[dev].store(blocks, std::memory_order_relaxed);
     }
     const size_t need = (a.g.N + ADJ_THREADS - 1) / ADJ_THREADS;
     const unsigned grid = (unsigned)(need < (size_t)blocks ? (need > 0 ? need : 1) : (size_t)blocks);
-    k_adjoint_step<T><<<grid, ADJ_THREADS, 0, s>>>(a);
+    if (a.g.per[0] && a.g.per[1] && a.g.per[2])
+        k_adjoint_step<T, true><<<grid, ADJ_THREADS, 0, s>>>(a);
+    else
+        k_adjoint_step<T, false><<<grid, ADJ_THREADS, 0, s>>>(a);
     return cudaGetLastError();
 }
 

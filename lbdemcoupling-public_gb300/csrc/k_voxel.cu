@@ -386,29 +386,43 @@ __device__ __noinline__ void apply_sphere(WarpVox<INIT_VEL>& S, const SphereFast
     uint8_t* cnt8 = reinterpret_cast<uint8_t*>(S.cnt4);
     const unsigned below = (1u << lane) - 1u;
     int qn = 0;
-    // 1: the half-planes j = 2 x + (0 | 1) of the box's x range whose rows meet its y range
-    for (int j = 2 * bx0; j <= 2 * bx1 + 1; ++j) {
-        const int yh = 4 * (j & 1);
-        if (yh > by1 || yh + 3 < by0) continue;
-        const int x = j >> 1, y = yl + yh;
-        int region = -1;
-        if (zin && y >= by0 && y <= by1) {
-            const float dxf = ((float)(X0 + x) - q.xh[0]) - q.xl[0];
-            const float dyf = ((float)(Y0 + y) - q.xh[1]) - q.xl[1];
-            const float distf = (dxf * dxf + dyf * dyf) + dzf * dzf;
-            if (fabsf(distf - rp2) <= M || fabsf(distf - rm2) <= M)
-                region = region_exact(X0 + x, Y0 + y, Z0 + z, sph[m]);
-            else
-                region = distf > rp2 ? 0 : (distf < rm2 ? 1 : 2);
+    // 1: the box's cells of the tile, x-plane by x-plane in the half-planes h
+    // (rows y = yl + 4 h) that meet the box's y range.  The squared distance is
+    // formed as dx^2 + (dy^2 + dz^2), every rounding explicit, the x-free part
+    // once per lane and half-plane.
+    const float dz2 = __fmul_rn(dzf, dzf);
+    float sh[2];
+    bool inh[2], meet[2];
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+        const int y = yl + 4 * h;
+        const float dyf = ((float)(Y0 + y) - q.xh[1]) - q.xl[1];
+        sh[h] = __fmaf_rn(dyf, dyf, dz2);
+        inh[h] = zin && y >= by0 && y <= by1;
+        meet[h] = !(4 * h > by1 || 4 * h + 3 < by0);   // warp-uniform
+    }
+    for (int x = bx0; x <= bx1; ++x) {
+        const float dxf = ((float)(X0 + x) - q.xh[0]) - q.xl[0];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+            if (!meet[h]) continue;
+            int region = -1;
+            if (inh[h]) {
+                const float distf = __fmaf_rn(dxf, dxf, sh[h]);
+                if (fabsf(distf - rp2) <= M || fabsf(distf - rm2) <= M)
+                    region = region_exact(X0 + x, Y0 + yl + 4 * h, Z0 + z, sph[m]);
+                else
+                    region = distf > rp2 ? 0 : (distf < rm2 ? 1 : 2);
+            }
+            const int l = lane + 64 * x + 32 * h;
+            const unsigned bal = __ballot_sync(FULL_MASK, region == 2);
+            if (region == 2) {
+                S.queue[qn + __popc(bal & below)] = (uint16_t)l;
+            } else if (region >= 0) {
+                fold_cell(S, l, region == 1 ? 125u : 0u, tag, m);
+            }
+            qn += __popc(bal);
         }
-        const int l = lane + 32 * j;
-        const unsigned bal = __ballot_sync(FULL_MASK, region == 2);
-        if (region == 2) {
-            S.queue[qn + __popc(bal & below)] = (uint16_t)l;
-        } else if (region >= 0) {
-            fold_cell(S, l, region == 1 ? 125u : 0u, tag, m);
-        }
-        qn += __popc(bal);
     }
     if (qn == 0) return;
     __syncwarp();

@@ -1,8 +1,9 @@
 """The float fast path of the voxelization (lbdemcoupling-public_gb300/csrc/k_voxel.cu)
 decides the reference's double comparisons exactly.
 
-The kernel evaluates, in float, the cell distance (dx^2 + dy^2) + dz^2 and the
-125 sub-cell sums (xs_i + ys_j) + zs_k from the centre split x = xh + xl, and
+The kernel evaluates, in float, the cell distance dx^2 + (dy^2 + dz^2) (two
+fused multiply-adds) and the 125 sub-cell sums (xs_i + ys_j) + zs_k from the
+centre split x = xh + xl, and
 falls back to the reference's double sequence (src/ibProcessors3D.hh:128-155)
 only when a float value lies within M = 2^-19 (r + 4)^2 of its threshold.  This
 emulates that float arithmetic in IEEE single precision on the CPU (numpy, one
@@ -31,8 +32,10 @@ def _fma(a, b, c):
     return (a.astype(np.float64) * b.astype(np.float64) + c.astype(np.float64)).astype(np.float32)
 
 
-def _dist_f(dxf, dyf, dzf, fused):
-    if not fused:
+def _dist_f(dxf, dyf, dzf, form):
+    if form == "kernel":   # k_voxel.cu: __fmaf_rn(dx, dx, __fmaf_rn(dy, dy, __fmul_rn(dz, dz)))
+        return _fma(dxf, dxf, _fma(dyf, dyf, dzf * dzf))
+    if form == "plain":
         return (dxf * dxf + dyf * dyf) + dzf * dzf
     return _fma(dzf, dzf, _fma(dyf, dyf, dxf * dxf))
 
@@ -51,8 +54,8 @@ def _spheres(seed, n):
     return x, r
 
 
-@pytest.mark.parametrize("fused", [False, True])
-def test_distance_band_decides_like_double(fused):
+@pytest.mark.parametrize("form", ["kernel", "plain", "fused"])
+def test_distance_band_decides_like_double(form):
     x, r = _spheres(3, 40)
     worst = 0.0
     for c, rad in zip(x, r):
@@ -64,7 +67,7 @@ def test_distance_band_decides_like_double(fused):
         dist_d = (dd[:, 0] * dd[:, 0] + dd[:, 1] * dd[:, 1]) + dd[:, 2] * dd[:, 2]
         xh, xl = _split(c)
         df = (P.astype(np.float32) - xh) - xl                                # ((float)X - xh) - xl
-        dist_f = _dist_f(df[:, 0], df[:, 1], df[:, 2], fused).astype(np.float64)
+        dist_f = _dist_f(df[:, 0], df[:, 1], df[:, 2], form).astype(np.float64)
         bound = 22 * U * (rad + 3.2) ** 2
         err = np.abs(dist_f - dist_d).max()
         worst = max(worst, err / bound)
