@@ -278,139 +278,162 @@ __global__ void __launch_bounds__(ADJ_THREADS, sizeof(T) == 4 ? 2 : 1) k_adjoint
     const Geom g = A.g;
     const size_t N = g.N;
     T gtau = T(0), gg[3] = {T(0), T(0), T(0)};   // per-thread sums, widened once
-    // one warp per 32-cell run of a z-row: rows * runs < 2^31 (nx * ny < 2^31 is
-    // checked at creation), so all index arithmetic stays in 32 bits
+    // one warp per 64-cell run of a z-row, in two passes of 32 cells: rows * runs
+    // < 2^31 (nx * ny < 2^31 is checked at creation), so all index arithmetic
+    // stays in 32 bits.  The run's solid cells are taken first (pass 0 holds as
+    // many as fit): a pass with a solid cell runs the solid cells' path for every
+    // lane, so gathering them leaves more passes on the fluid path.  A cell's
+    // result does not depend on its pass.
     const int lane = threadIdx.x & 31;
-    const int nzc = (g.nz + 31) >> 5;
+    const int nzc = (g.nz + 63) >> 6;
     const long long nchunks = (long long)g.nx * g.ny * nzc;
     const long long wstride = (long long)gridDim.x * (ADJ_THREADS / 32);
     for (long long q = (long long)blockIdx.x * (ADJ_THREADS / 32) + (threadIdx.x >> 5); q < nchunks; q += wstride) {
-        const int qi = (int)q;   // runs of 32 cells: < 2^31 for any lattice that fits in memory
+        const int qi = (int)q;   // runs of 64 cells: < 2^31 for any lattice that fits in memory
         const int row = qi / nzc;
-        const int z = (qi - row * nzc) * 32 + lane;
-        int key = -1;
-        T pv[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
-        // warp-uniform: some cell of the run is solid
-        const bool general = __any_sync(FULLMASK, z < g.nz && (A.vox[(size_t)row * g.nz + z] & VOX_NMASK) != 0u);
-        if (z < g.nz) {
-            const int x = row / g.ny;
-            const int y = row - x * g.ny;
-            const size_t c = (size_t)row * g.nz + z;
-            // neighbour coordinates (-1 beyond a wall) and the nine row offsets
-            const bool p0 = PER || g.per[0], p1 = PER || g.per[1], p2 = PER || g.per[2];
-            const int xs[3] = {x > 0 ? x - 1 : (p0 ? g.nx - 1 : -1), x, x < g.nx - 1 ? x + 1 : (p0 ? 0 : -1)};
-            const int ys[3] = {y > 0 ? y - 1 : (p1 ? g.ny - 1 : -1), y, y < g.ny - 1 ? y + 1 : (p1 ? 0 : -1)};
-            const int zs[3] = {z > 0 ? z - 1 : (p2 ? g.nz - 1 : -1), z, z < g.nz - 1 ? z + 1 : (p2 ? 0 : -1)};
-            long long rowoff[9];
+        const int zb = (qi - row * nzc) * 64;
+        const int len = min(64, g.nz - zb);
+        const size_t rowc = (size_t)row * g.nz + zb;
+        const uint32_t wl0 = lane < len ? A.vox[rowc + lane] : 0u;
+        const uint32_t wl1 = lane + 32 < len ? A.vox[rowc + lane + 32] : 0u;
+        const unsigned sol0 = __ballot_sync(FULLMASK, (wl0 & VOX_NMASK) != 0u);
+        const unsigned sol1 = __ballot_sync(FULLMASK, (wl1 & VOX_NMASK) != 0u);
+        const unsigned flu0 = __ballot_sync(FULLMASK, lane < len) & ~sol0;
+        const unsigned flu1 = __ballot_sync(FULLMASK, lane + 32 < len) & ~sol1;
+        const int ns0 = __popc(sol0), ns = ns0 + __popc(sol1);
+        const int nf0 = __popc(flu0), nf = nf0 + __popc(flu1);
+#pragma unroll 1
+        for (int pass = 0; pass < 2; ++pass) {
+            const int slot_l = 32 * pass + lane;
+            int jr = -1;   // the cell of the run this lane takes in this pass
+            if (slot_l < ns) jr = slot_l < ns0 ? nth_bit(sol0, slot_l) : 32 + nth_bit(sol1, slot_l - ns0);
+            else if (slot_l - ns < nf)
+                jr = slot_l - ns < nf0 ? nth_bit(flu0, slot_l - ns) : 32 + nth_bit(flu1, slot_l - ns - nf0);
+            const bool general = ns > 32 * pass;   // warp-uniform: the pass holds a solid cell
+            const int z = zb + jr;
+            int key = -1;
+            T pv[6] = {T(0), T(0), T(0), T(0), T(0), T(0)};
+            if (jr >= 0) {
+                const int x = row / g.ny;
+                const int y = row - x * g.ny;
+                const size_t c = (size_t)row * g.nz + z;
+                // neighbour coordinates (-1 beyond a wall) and the nine row offsets
+                const bool p0 = PER || g.per[0], p1 = PER || g.per[1], p2 = PER || g.per[2];
+                const int xs[3] = {x > 0 ? x - 1 : (p0 ? g.nx - 1 : -1), x, x < g.nx - 1 ? x + 1 : (p0 ? 0 : -1)};
+                const int ys[3] = {y > 0 ? y - 1 : (p1 ? g.ny - 1 : -1), y, y < g.ny - 1 ? y + 1 : (p1 ? 0 : -1)};
+                const int zs[3] = {z > 0 ? z - 1 : (p2 ? g.nz - 1 : -1), z, z < g.nz - 1 ? z + 1 : (p2 ? 0 : -1)};
+                long long rowoff[9];
 #pragma unroll
-            for (int a = 0; a < 3; ++a)
+                for (int a = 0; a < 3; ++a)
 #pragma unroll
-                for (int b = 0; b < 3; ++b)
-                    rowoff[3 * a + b] = (PER || (xs[a] >= 0 && ys[b] >= 0)) ? ((long long)xs[a] * g.ny + ys[b]) * g.nz : -1;
-            // cell x + (dx, dy, dz) as a linear index, or -1 beyond a wall
-            auto nb = [&](int dx, int dy, int dz) -> long long {
-                const long long r = rowoff[3 * (dx + 1) + dy + 1];
-                const int zz = zs[dz + 1];
-                return (PER || (r >= 0 && zz >= 0)) ? r + zz : -1;
-            };
-            T f[Q], mu[Q];
-            if (A.phase == 0) {
+                    for (int b = 0; b < 3; ++b)
+                        rowoff[3 * a + b] =
+                            (PER || (xs[a] >= 0 && ys[b] >= 0)) ? ((long long)xs[a] * g.ny + ys[b]) * g.nz : -1;
+                // cell x + (dx, dy, dz) as a linear index, or -1 beyond a wall
+                auto nb = [&](int dx, int dy, int dz) -> long long {
+                    const long long r = rowoff[3 * (dx + 1) + dy + 1];
+                    const int zz = zs[dz + 1];
+                    return (PER || (r >= 0 && zz >= 0)) ? r + zz : -1;
+                };
+                T f[Q], mu[Q];
+                if (A.phase == 0) {
 #pragma unroll
-                for (int k = 0; k < Q; ++k) f[k] = A.f[(size_t)k * N + c];
-            } else {
-                // odd layout: f_k(x) in slot (opp k, x - c_k), or (k, x) when x - c_k is beyond a wall
-                f[0] = A.f[c];
-#pragma unroll
-                for (int k = 1; k < Q; ++k) {
-                    const long long s2 = nb(-cx(k), -cy(k), -cz(k));
-                    f[k] = s2 >= 0 ? A.f[(size_t)opp(k) * N + (size_t)s2] : A.f[(size_t)k * N + c];
-                }
-            }
-            // transpose of push streaming: mu_k = lambda_k(x + c_k), or lambda_opp k(x) beyond a wall
-#pragma unroll
-            for (int k = 0; k < Q; ++k) {
-                const long long s2 = k == 0 ? (long long)c : nb(cx(k), cy(k), cz(k));
-                mu[k] = s2 >= 0 ? A.lam_in[(size_t)k * N + (size_t)s2] : A.lam_in[(size_t)opp(k) * N + c];
-            }
-            const uint32_t w = A.vox[c];
-            int n = min((int)(w & VOX_NMASK), 125);
-            T uP[3] = {T(0), T(0), T(0)}, a[3] = {T(0), T(0), T(0)}, d[3] = {T(0), T(0), T(0)};
-            T B = T(0), dBdtau = T(0);
-            int slot = -1;
-            if (n > 0) {
-                const int tag = (int)(w >> VOX_NBITS);
-                slot = tag <= A.max_tag ? A.tag2slot[tag] : -1;
-                if (slot < 0 || slot >= A.nslot) {
-                    atomicOr(A.err, 0x8u);   // LBDEM_DEVERR_UNMAPPED_TAG
-                    slot = -1;
+                    for (int k = 0; k < Q; ++k) f[k] = A.f[(size_t)k * N + c];
                 } else {
-                    const double* p = A.rec + (size_t)slot * REC_STRIDE;
-                    // arm d = cell - centre, minimum image as in the force arm
-                    // (src/ibProcessors3D.hh:230-243); the float form takes the
-                    // centre's hi/lo split as the forward pass does
-                    if (sizeof(T) == 8) {
-                        d[0] = T((double)x - p[0]); d[1] = T((double)y - p[1]); d[2] = T((double)z - p[2]);
-                    } else {
-                        const float4* q4 = reinterpret_cast<const float4*>(A.xpf + (size_t)slot * XPF_STRIDE);
-                        const float4 hq = q4[0], lq = q4[1];
-                        d[0] = T(((float)x - hq.x) - hq.w);
-                        d[1] = T(((float)y - hq.y) - lq.x);
-                        d[2] = T(((float)z - hq.z) - lq.y);
-                    }
-                    const int ext[3] = {g.nx, g.ny, g.nz};
+                    // odd layout: f_k(x) in slot (opp k, x - c_k), or (k, x) when x - c_k is beyond a wall
+                    f[0] = A.f[c];
 #pragma unroll
-                    for (int q = 0; q < 3; ++q) {
-                        const int h = ext[q] / 2;
-                        if (d[q] > T(h)) d[q] -= T(ext[q]);
-                        else if (d[q] < T(-h)) d[q] += T(ext[q]);
+                    for (int k = 1; k < Q; ++k) {
+                        const long long s2 = nb(-cx(k), -cy(k), -cz(k));
+                        f[k] = s2 >= 0 ? A.f[(size_t)opp(k) * N + (size_t)s2] : A.f[(size_t)k * N + c];
                     }
-                    const T v0 = T(p[3]), v1 = T(p[4]), v2 = T(p[5]);
-                    const T w0 = T(p[6]), w1 = T(p[7]), w2 = T(p[8]);
-                    // uP = v + w x d (setValues, src/ibProcessors3D.hh:163-174)
-                    uP[0] = v0 + (w1 * d[2] - w2 * d[1]);
-                    uP[1] = v1 + (-w0 * d[2] + w2 * d[0]);
-                    uP[2] = v2 + (w0 * d[1] - w1 * d[0]);
-                    const double* wgt = A.w + (size_t)slot * 6;
-                    const T wf0 = T(wgt[0]), wf1 = T(wgt[1]), wf2 = T(wgt[2]);
-                    const T wt0 = T(wgt[3]), wt1 = T(wgt[4]), wt2 = T(wgt[5]);
-                    // dL/dF_cell = w_F + w_T x d
-                    a[0] = wf0 + (wt1 * d[2] - wt2 * d[1]);
-                    a[1] = wf1 + (wt2 * d[0] - wt0 * d[2]);
-                    a[2] = wf2 + (wt0 * d[1] - wt1 * d[0]);
-                    B = A.btab[n];
-                    const T sf = T(1.0 / 125.0) * T(n), den = (T(1) - sf) + (A.tauT - T(0.5));
-                    dBdtau = n < 125 ? sf * (T(1) - sf) / (den * den) : T(0);
                 }
-            }
-            if (n > 0 && slot < 0) n = 0;
-            T guP[3];
-            const T gvec[3] = {A.g3[0], A.g3[1], A.g3[2]};
-            const CellAdj<T> R = adjoint_cell<T>(f, mu, n, general, B, dBdtau, uP, a, A.omega, gvec, guP, gtau, gg);
-            const T om1 = n == 125 ? T(1) : T(1) - A.omega;
-            if (!general) {   // fluid cells only: phi = mu, no solid terms
-#pragma unroll
-                for (int k = 0; k < Q; ++k)
-                    A.lam_out[(size_t)k * N + c] = om1 * mu[k] + (R.grb + cdotT<T>(k, R.gJ0, R.gJ1, R.gJ2));
-            } else {
-                // the fluid path's expression plus the solid terms (exactly zero for a fluid cell)
+                // transpose of push streaming: mu_k = lambda_k(x + c_k), or lambda_opp k(x) beyond a wall
 #pragma unroll
                 for (int k = 0; k < Q; ++k) {
-                    const T phi = R.sB * mu[k] + R.grbs + cdotT<T>(k, R.gjs0, R.gjs1, R.gjs2);
-                    T l = om1 * phi + (R.grb + cdotT<T>(k, R.gJ0, R.gJ1, R.gJ2));
-                    l += R.B * mu[opp(k)] + T(2) * R.B * cdotT<T>(k, a[0], a[1], a[2]);
-                    A.lam_out[(size_t)k * N + c] = l;
+                    const long long s2 = k == 0 ? (long long)c : nb(cx(k), cy(k), cz(k));
+                    mu[k] = s2 >= 0 ? A.lam_in[(size_t)k * N + (size_t)s2] : A.lam_in[(size_t)opp(k) * N + c];
+                }
+                const uint32_t w = A.vox[c];
+                int n = min((int)(w & VOX_NMASK), 125);
+                T uP[3] = {T(0), T(0), T(0)}, a[3] = {T(0), T(0), T(0)}, d[3] = {T(0), T(0), T(0)};
+                T B = T(0), dBdtau = T(0);
+                int slot = -1;
+                if (n > 0) {
+                    const int tag = (int)(w >> VOX_NBITS);
+                    slot = tag <= A.max_tag ? A.tag2slot[tag] : -1;
+                    if (slot < 0 || slot >= A.nslot) {
+                        atomicOr(A.err, 0x8u);   // LBDEM_DEVERR_UNMAPPED_TAG
+                        slot = -1;
+                    } else {
+                        const double* p = A.rec + (size_t)slot * REC_STRIDE;
+                        // arm d = cell - centre, minimum image as in the force arm
+                        // (src/ibProcessors3D.hh:230-243); the float form takes the
+                        // centre's hi/lo split as the forward pass does
+                        if (sizeof(T) == 8) {
+                            d[0] = T((double)x - p[0]); d[1] = T((double)y - p[1]); d[2] = T((double)z - p[2]);
+                        } else {
+                            const float4* q4 = reinterpret_cast<const float4*>(A.xpf + (size_t)slot * XPF_STRIDE);
+                            const float4 hq = q4[0], lq = q4[1];
+                            d[0] = T(((float)x - hq.x) - hq.w);
+                            d[1] = T(((float)y - hq.y) - lq.x);
+                            d[2] = T(((float)z - hq.z) - lq.y);
+                        }
+                        const int ext[3] = {g.nx, g.ny, g.nz};
+#pragma unroll
+                        for (int q = 0; q < 3; ++q) {
+                            const int h = ext[q] / 2;
+                            if (d[q] > T(h)) d[q] -= T(ext[q]);
+                            else if (d[q] < T(-h)) d[q] += T(ext[q]);
+                        }
+                        const T v0 = T(p[3]), v1 = T(p[4]), v2 = T(p[5]);
+                        const T w0 = T(p[6]), w1 = T(p[7]), w2 = T(p[8]);
+                        // uP = v + w x d (setValues, src/ibProcessors3D.hh:163-174)
+                        uP[0] = v0 + (w1 * d[2] - w2 * d[1]);
+                        uP[1] = v1 + (-w0 * d[2] + w2 * d[0]);
+                        uP[2] = v2 + (w0 * d[1] - w1 * d[0]);
+                        const double* wgt = A.w + (size_t)slot * 6;
+                        const T wf0 = T(wgt[0]), wf1 = T(wgt[1]), wf2 = T(wgt[2]);
+                        const T wt0 = T(wgt[3]), wt1 = T(wgt[4]), wt2 = T(wgt[5]);
+                        // dL/dF_cell = w_F + w_T x d
+                        a[0] = wf0 + (wt1 * d[2] - wt2 * d[1]);
+                        a[1] = wf1 + (wt2 * d[0] - wt0 * d[2]);
+                        a[2] = wf2 + (wt0 * d[1] - wt1 * d[0]);
+                        B = A.btab[n];
+                        const T sf = T(1.0 / 125.0) * T(n), den = (T(1) - sf) + (A.tauT - T(0.5));
+                        dBdtau = n < 125 ? sf * (T(1) - sf) / (den * den) : T(0);
+                    }
+                }
+                if (n > 0 && slot < 0) n = 0;
+                T guP[3];
+                const T gvec[3] = {A.g3[0], A.g3[1], A.g3[2]};
+                const CellAdj<T> R = adjoint_cell<T>(f, mu, n, general, B, dBdtau, uP, a, A.omega, gvec, guP, gtau, gg);
+                const T om1 = n == 125 ? T(1) : T(1) - A.omega;
+                if (!general) {   // fluid cells only: phi = mu, no solid terms
+#pragma unroll
+                    for (int k = 0; k < Q; ++k)
+                        A.lam_out[(size_t)k * N + c] = om1 * mu[k] + (R.grb + cdotT<T>(k, R.gJ0, R.gJ1, R.gJ2));
+                } else {
+                    // the fluid path's expression plus the solid terms (exactly zero for a fluid cell)
+#pragma unroll
+                    for (int k = 0; k < Q; ++k) {
+                        const T phi = R.sB * mu[k] + R.grbs + cdotT<T>(k, R.gjs0, R.gjs1, R.gjs2);
+                        T l = om1 * phi + (R.grb + cdotT<T>(k, R.gJ0, R.gJ1, R.gJ2));
+                        l += R.B * mu[opp(k)] + T(2) * R.B * cdotT<T>(k, a[0], a[1], a[2]);
+                        A.lam_out[(size_t)k * N + c] = l;
+                    }
+                }
+                if (slot >= 0) {
+                    key = slot;
+                    pv[0] = guP[0]; pv[1] = guP[1]; pv[2] = guP[2];
+                    // d/dw of w x d: d x guP
+                    pv[3] = d[1] * guP[2] - d[2] * guP[1];
+                    pv[4] = d[2] * guP[0] - d[0] * guP[2];
+                    pv[5] = d[0] * guP[1] - d[1] * guP[0];
                 }
             }
-            if (slot >= 0) {
-                key = slot;
-                pv[0] = guP[0]; pv[1] = guP[1]; pv[2] = guP[2];
-                // d/dw of w x d: d x guP
-                pv[3] = d[1] * guP[2] - d[2] * guP[1];
-                pv[4] = d[2] * guP[0] - d[0] * guP[2];
-                pv[5] = d[0] * guP[1] - d[1] * guP[0];
-            }
+            reduce6(key, pv, A.gvel);
         }
-        reduce6(key, pv, A.gvel);
     }
     // block sums of d/dg and d/dtau, one atomic per block and value
     const int warp = threadIdx.x >> 5;

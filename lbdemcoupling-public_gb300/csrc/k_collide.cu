@@ -307,24 +307,6 @@ __device__ __forceinline__ void collide_cell_fp64(double (&f)[Q], double omega, 
     Fz = SOLID ? B2 * Ez : 0.0;
 }
 
-// Position of the k-th set bit (k = 0: the lowest) of m; k < popc(m).
-__device__ __forceinline__ int nth_bit(unsigned m, int k) {
-    int pos = 0;
-#pragma unroll
-    for (int w = 16; w >= 1; w >>= 1) {
-        const unsigned lo = m & ((1u << w) - 1u);
-        const int c = __popc(lo);
-        if (k >= c) {
-            k -= c;
-            m >>= w;
-            pos += w;
-        } else {
-            m = lo;
-        }
-    }
-    return pos;
-}
-
 // Per-cell force and torque added to the particle's sums (FP64 form): six
 // double atomics per solid cell, resolved in L2 instead of a warp scan on the
 // FP64 pipe.

@@ -533,23 +533,31 @@ __device__ __forceinline__ void voxelize_tile(WarpVox<INIT_VEL>& S, int t, const
     const int ty = rem / tnz;
     const int tz = rem - ty * tnz;
     const int X0 = tx * TILE, Y0 = ty * TILE, Z0 = tz * TILE;
+    // The tile's count, both bin slots of the lane (read whatever the count; the
+    // slots past it are ignored) and its 16 voxel words are independent loads,
+    // issued together so that the tile waits for one memory latency, not four.
     const int cnt = tile_cnt[t];
-    int a = INT_MAX, b = INT_MAX;      // the lane's bin entries (list indices)
-    if (cnt <= TILE_BIN) {
-        if (lane < cnt) a = bins[(size_t)t * TILE_BIN + lane];
-        if (lane + 32 < cnt) b = bins[(size_t)t * TILE_BIN + lane + 32];
-    }
+    const int a0 = bins[(size_t)t * TILE_BIN + lane];
+    const int b0 = bins[(size_t)t * TILE_BIN + lane + 32];
     // cell state; a lane's cells share z and, per plane half, the row
     const int z = lane & 7, Z = Z0 + z;
     const bool zok = Z < g.nz;
-#pragma unroll 4
+    uint32_t wv[16];
+#pragma unroll
+    for (int j = 0; j < 16; ++j) {
+        const int X = X0 + (j >> 1), Y = Y0 + (lane >> 3) + 4 * (j & 1);
+        wv[j] = (zok && X < g.nx && Y < g.ny) ? vox[((size_t)X * g.ny + Y) * g.nz + Z] : 0u;
+    }
+#pragma unroll
     for (int j = 0; j < 16; ++j) {
         const int l = lane + 32 * j;
-        const int X = X0 + (j >> 1), Y = Y0 + (lane >> 3) + 4 * (j & 1);
-        S.w[l] = (zok && X < g.nx && Y < g.ny) ? vox[((size_t)X * g.ny + Y) * g.nz + Z] : 0u;
+        S.w[l] = wv[j];
         S.setter[l] = SETTER_KEEP;
         if (INIT_VEL) S.defv[l] = DEFV_NONE;
     }
+    // the lane's bin entries (list indices)
+    int a = (cnt <= TILE_BIN && lane < cnt) ? a0 : INT_MAX;
+    int b = (cnt <= TILE_BIN && lane + 32 < cnt) ? b0 : INT_MAX;
     if (cnt <= 0) return;
     if (lane == 0) tile_cnt[t] = 0;    // the bins are reused by the next voxelization
     constexpr int W4 = (int)(sizeof(SphereFast) / 16);
@@ -663,12 +671,17 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
     WarpVox<INIT_VEL>& S = reinterpret_cast<WarpVox<INIT_VEL>*>(smem_raw)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
     const int nwork = *(volatile int*)work_n;
-    for (;;) {
+    // the next tile is claimed and its index read while the current one is worked on
+    auto claim = [&]() -> int {
         int w = 0;
         if (lane == 0) w = atomicAdd(work_n + 1, 1);
         w = __shfl_sync(FULL_MASK, w, 0);
-        if (w >= nwork) break;
-        const int tg = work[w];
+        return w < nwork ? work[w] : -1;
+    };
+    int next = claim();
+    while (next >= 0) {
+        const int tg = next;
+        next = claim();
         if (BATCH) {
             const int d = find_domain(toff, ndom, tg);
             const DomView& D = doms[d];

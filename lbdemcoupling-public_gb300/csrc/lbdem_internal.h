@@ -82,6 +82,24 @@ __device__ __forceinline__ size_t slot_index(int i, int x, int y, int z, int pha
     return (size_t)opp(i) * g.N + ((size_t)X * g.ny + Y) * g.nz + Z;
 }
 
+// Position of the k-th set bit (k = 0: the lowest) of m; k < popc(m).
+__device__ __forceinline__ int nth_bit(unsigned m, int k) {
+    int pos = 0;
+#pragma unroll
+    for (int w = 16; w >= 1; w >>= 1) {
+        const unsigned lo = m & ((1u << w) - 1u);
+        const int c = __popc(lo);
+        if (k >= c) {
+            k -= c;
+            m >>= w;
+            pos += w;
+        } else {
+            m = lo;
+        }
+    }
+    return pos;
+}
+
 // Arguments of one collide-stream launch.
 // Launch shapes cached per device (the SM count, the resident blocks of a kernel
 // and its dynamic shared-memory opt-in are properties of one device).
