@@ -24,7 +24,8 @@ with CUDA events on the launching stream.  `fp64` carries the FP64 drop-in
 form on the same inputs, and `force_rel_err_fp32_vs_fp64` the per-particle
 force error between the two after the run.  `e2e` is the FP32 form through
 the C ABI (lbdem_cycle) with host buffers: the particle table copy in, the
-forces copy out and the per-step synchronisation are inside the timed region.
+forces copy out and the per-step synchronisation are inside the timed region;
+`fp64.e2e` is the same for the FP64 form over a bounded number of cycles.
 
 `--impl reference` times the CPU oracle (a restatement of the reference's
 path; the reference itself needs Palabos, LIGGGHTS and MPI) on the host cores.
@@ -54,6 +55,7 @@ TAU = 0.55
 SEED = 2024
 WORKLOAD = "monodisperse suspension, periodic 256^3, 2000 spheres r=8, tau=0.55, prescribed kinematics"
 WINDOW = 300   # steps between returns of the lattice to rest (see the module docstring)
+E2E_FP64_STEPS = 100   # cycles of the FP64 form's end-to-end leg (about 0.8 s at 256^3)
 BYTES_PER_CELL = {"fp32": 2 * 19 * 4 + 4, "fp64": 2 * 19 * 8 + 4}  # 19 loads + 19 stores + voxel word
 
 
@@ -224,11 +226,19 @@ def run_device(prec_name: str, table, offs, steps: int, warmup: int, max_n: int,
             "device_errors": errs}
 
 
-def run_e2e(host_tables, steps: int, warmup: int, max_n: int, max_tag: int, device: int):
-    """FP32 form through lbdem_cycle with host buffers (copies and sync in the timed region)."""
+def run_e2e(host_tables, steps: int, warmup: int, max_n: int, max_tag: int, device: int, prec: str = "fp32"):
+    """One form through the C ABI's lbdem_cycle with host buffers: the particle
+    table copy in, the kernels, the force/torque copy out and the synchronisation
+    are inside the timed region.  The ctypes argument tuples of every step are
+    built before it, so the region holds the C-ABI calls themselves and not the
+    Python binding's per-call argument marshalling (which a C or C++ caller of
+    the ABI does not have)."""
+    import ctypes as C
+
     import lbdem
-    lat = lbdem.Lattice(*SHAPE, 1.0 / TAU, precision=lbdem.PREC_FP32_DEV, max_particles=max_n,
-                        max_tag=max_tag, max_radius=8.0, device=device)
+    lat = lbdem.Lattice(*SHAPE, 1.0 / TAU,
+                        precision=lbdem.PREC_FP32_DEV if prec == "fp32" else lbdem.PREC_FP64,
+                        max_particles=max_n, max_tag=max_tag, max_radius=8.0, device=device)
     F = np.zeros((max_n, 3))
     T = np.zeros((max_n, 3))
     for s in range(warmup):
@@ -236,15 +246,27 @@ def run_e2e(host_tables, steps: int, warmup: int, max_n: int, max_tag: int, devi
         if s > 0 and s % WINDOW == 0:
             lat.init_equilibrium()
         lat.cycle(g.x, g.v, g.w, g.r, g.tag, F=F[: g.n], T=T[: g.n])
+    dp = C.POINTER(C.c_double)
+    keep, calls = [], []
+    for k in range(steps):
+        g = host_tables[warmup + k]
+        arrs = [np.ascontiguousarray(a, dtype=np.float64) for a in (g.x, g.v, g.w, g.r)]
+        tag = np.ascontiguousarray(g.tag, dtype=np.int32)
+        keep.append((arrs, tag))
+        calls.append((lat.h, g.n, *[a.ctypes.data_as(dp) for a in arrs],
+                      tag.ctypes.data_as(C.POINTER(C.c_int32)), 0, F.ctypes.data_as(dp), T.ctypes.data_as(dp)))
+    cycle = lat.lib.lbdem_cycle
     h2d = d2h = 0
     t0 = time.perf_counter()
     for k in range(steps):
-        g = host_tables[warmup + k]
         if (warmup + k) % WINDOW == 0:
             lat.init_equilibrium()
-        lat.cycle(g.x, g.v, g.w, g.r, g.tag, F=F[: g.n], T=T[: g.n])
-        h2d += g.n * 12 * 8
-        d2h += g.n * 6 * 8 + 4
+        st = cycle(*calls[k])
+        if st != 0:
+            lat._check(st)
+        n = calls[k][1]
+        h2d += n * 12 * 8
+        d2h += n * 6 * 8 + 4
     dt = time.perf_counter() - t0
     lat.close()
     return dt, h2d / steps, d2h / steps
@@ -478,14 +500,20 @@ def main():
         ap.error("--forms must include fp32 (the headline form)")
     r32 = run_device("fp32", table, offs, args.steps, args.warmup, max_n, max_tag, device)
     r64 = run_device("fp64", table, offs, args.steps, args.warmup, max_n, max_tag, device) if "fp64" in forms else None
+    # the FP64 form's end-to-end leg runs a bounded number of the same cycles
+    steps64_e2e = min(args.steps, E2E_FP64_STEPS)
     if args.no_e2e:
         e2e_s, h2d, d2h = float("nan"), 0, 0
+        e2e64_s = float("nan")
     else:
         e2e_s, h2d, d2h = run_e2e(host, args.steps, args.warmup, max_n, max_tag, device)
+        e2e64_s = (run_e2e(host, steps64_e2e, args.warmup, max_n, max_tag, device, "fp64")[0] if r64
+                   else float("nan"))
 
     t32 = r32["total_ms"]
     if dist:
-        t32, t64, e2e_s = max_over_ranks([t32, r64["total_ms"] if r64 else 0.0, e2e_s], dist, f"cuda:{device}")
+        t32, t64, e2e_s, e2e64_s = max_over_ranks([t32, r64["total_ms"] if r64 else 0.0, e2e_s, e2e64_s], dist,
+                                                   f"cuda:{device}")
     else:
         t64 = r64["total_ms"] if r64 else float("nan")
     if rank != 0:
@@ -559,7 +587,12 @@ def main():
             "hbm": {"achieved": ach64, "peak": peak, "unit": "GB/s", "frac": ach64 / peak,
                     "traffic": traffic.get("fp64"), "kernel": "k_collide_staged<double> (all axes periodic)",
                     "bytes_per_cell": BYTES_PER_CELL["fp64"]},
-            "k1_ms": r64["k1_ms"], "k2_voxelize_ms": r64["k2_ms"]},
+            "k1_ms": r64["k1_ms"], "k2_voxelize_ms": r64["k2_ms"],
+            "e2e": None if args.no_e2e else {
+                "value": world * N * steps64_e2e / e2e64_s / 1e6, "unit": "MLUPS", "steps": steps64_e2e,
+                "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "vs_cpu": (world * N * steps64_e2e / e2e64_s / 1e6 / cpu["value"]) if cpu else None,
+                "note": "FP64 form through lbdem_cycle with host buffers, against the FP64 CPU oracle"}},
         "force_rel_err_fp32_vs_fp64": ferr,
         "batched": batched,
         "adjoint": adjoint,
