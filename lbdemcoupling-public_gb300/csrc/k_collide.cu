@@ -489,9 +489,10 @@ __device__ __forceinline__ void psm2(F2 (&f)[Q], F2 rhoBar, F2 jx, F2 jy, F2 jz,
 
 // bgk2 followed by psm2 in one pass over the opposite pairs (the same operations
 // in the same order, so the same bits): the pre-collision pair is still in
-// registers when its correction is applied, so fPre is not re-read.  Used for
-// unaligned rows (batch); aligned rows keep the two passes, which measured faster
-// there.  Per pair k = i + 9 (c_k = -c_i), with the solid
+// registers when its correction is applied, so fPre is not re-read.  Used with a
+// body force for unaligned rows (batch); aligned rows keep the two passes, which
+// measured faster there (without a body force both take collide_g2).  Per pair
+// k = i + 9 (c_k = -c_i), with the solid
 // equilibrium at P = (1 + rhoBar) uPart and fb the BGK result:
 //   A = t (dB + 4.5 invRho ((c_k.P)^2 - (c_k.j)^2)),  S = 3 t c_k.(j + P),
 //   E = (fPre_k - fPre_i) - S,
@@ -574,6 +575,68 @@ __device__ __forceinline__ void bgk_psm2(F2 (&f)[Q], const Mom2& m, float omega,
     pair(std::integral_constant<int, 14>{}); pair(std::integral_constant<int, 15>{});
     pair(std::integral_constant<int, 16>{}); pair(std::integral_constant<int, 17>{});
     pair(std::integral_constant<int, 18>{});
+}
+
+// FP32 form without a body force: BGK and the solid correction of both cells
+// in one pass, the formulation of collide_cell_fp64 in packed pairs (around
+// g = fPre - feq; alpha = omega (1 - B) + B; see there).  fPre is f itself on
+// entry, so nothing is re-read from the stage.  SOLID false (no solid cell in
+// the warp) leaves out the solid terms; a fluid cell (B = 0, uP = 0) gets the
+// same bits either way.
+template <bool SOLID>
+__device__ __forceinline__ void collide_g2(F2 (&f)[Q], const Mom2& m, float omega, F2 up0, F2 up1, F2 up2, F2 B,
+                                           F2& Fx, F2& Fy, F2& Fz) {
+    const F2 invRho = m.invRho;
+    const F2 jSqr = fma2(m.jz, m.jz, fma2(m.jy, m.jy, m.jx * m.jx));
+    const F2 m15 = bc(-1.5f) * invRho;
+    const F2 base = fma2(m15, jSqr, m.rhoBar);
+    const F2 nom = bc(-omega);
+    F2 Px = bc(0.f), Py = bc(0.f), Pz = bc(0.f), dd = bc(0.f), nalpha = nom, nom1B = nom;
+    if (SOLID) {
+        const F2 rho = bc(1.f) + m.rhoBar;
+        Px = up0 * rho; Py = up1 * rho; Pz = up2 * rho;
+        const F2 PSqr = fma2(Pz, Pz, fma2(Py, Py, Px * Px));
+        dd = m15 * (jSqr - PSqr);
+        nalpha = fma2(B, bc(omega - 1.f), nom);     // -(omega (1 - B) + B)
+        nom1B = fma2(B, bc(omega), nom);            // -omega (1 - B)
+    }
+    {
+        const F2 g0 = f[0] - bc((float)wt(0)) * base;
+        f[0] = SOLID ? fma2(B, bc((float)wt(0)) * dd, fma2(nom1B, g0, f[0])) : fma2(nom, g0, f[0]);
+    }
+    F2 Ex = bc(0.f), Ey = bc(0.f), Ez = bc(0.f);
+    auto pair = [&](auto kc) {
+        constexpr int k = decltype(kc)::value, i = k - 9;
+        const F2 t = bc((float)wt(k)), t3 = bc(3.f * (float)wt(k));
+        const F2 a45 = bc(4.5f * (float)wt(k)) * invRho;
+        const F2 cj = cdotk<k>(m.jx, m.jy, m.jz);
+        const F2 C = fma2(a45 * cj, cj, t * base);
+        const F2 Lj = t3 * cj;
+        const F2 gi = (f[i] - C) + Lj;
+        const F2 gk = (f[k] - C) - Lj;
+        if (SOLID) {
+            const F2 cP = cdotk<k>(Px, Py, Pz);
+            const F2 mm = cj - cP, pp = cj + cP;
+            const F2 Qd = fma2(a45 * mm, pp, t * dd);
+            const F2 L = t3 * mm;
+            const F2 e = (f[k] - f[i]) - t3 * pp;
+            f[i] = fma2(B, (gk - Qd) + L, fma2(nalpha, gi, f[i]));
+            f[k] = fma2(B, (gi - Qd) - L, fma2(nalpha, gk, f[k]));
+            if constexpr (cx(k) > 0) Ex = Ex + e;
+            if constexpr (cy(k) > 0) Ey = Ey + e; else if constexpr (cy(k) < 0) Ey = Ey - e;
+            if constexpr (cz(k) > 0) Ez = Ez + e; else if constexpr (cz(k) < 0) Ez = Ez - e;
+        } else {
+            f[i] = fma2(nom, gi, f[i]);
+            f[k] = fma2(nom, gk, f[k]);
+        }
+    };
+    pair(std::integral_constant<int, 10>{}); pair(std::integral_constant<int, 11>{});
+    pair(std::integral_constant<int, 12>{}); pair(std::integral_constant<int, 13>{});
+    pair(std::integral_constant<int, 14>{}); pair(std::integral_constant<int, 15>{});
+    pair(std::integral_constant<int, 16>{}); pair(std::integral_constant<int, 17>{});
+    pair(std::integral_constant<int, 18>{});
+    const F2 B2 = B + B;
+    Fx = B2 * Ex; Fy = B2 * Ey; Fz = B2 * Ez;
 }
 
 // float -> double by bit manipulation (exact for normal numbers; subnormal
@@ -1189,7 +1252,15 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     auto hsol = [&]() -> F2 {
         return FORCE ? pk(n0 < 125 ? 1.f : 0.f, n1 < 125 ? 1.f : 0.f) * (bc(1.f) + m.rhoBar) : bc(0.f);
     };
-    if constexpr (MIS) {
+    if constexpr (!FORCE) {
+        // one pass; the solid terms only in warps that hold a solid cell
+        if (__any_sync(FULL, n0 > 0 || n1 > 0)) {
+            if (n0 > 0 || n1 > 0) solid_velocity();
+            collide_g2<true>(f, m, a.omega, up[0], up[1], up[2], B, Fx, Fy, Fz);
+        } else {
+            collide_g2<false>(f, m, a.omega, up[0], up[1], up[2], B, Fx, Fy, Fz);
+        }
+    } else if constexpr (MIS) {
         if (__any_sync(FULL, n0 > 0 || n1 > 0)) {   // one pass; a no-op for the lanes' fluid cells
             if (n0 > 0 || n1 > 0) solid_velocity();
             bgk_psm2<FORCE>(f, m, a.omega, a.g3[0], a.g3[1], a.g3[2], hsol(), up[0], up[1], up[2], B, Fx, Fy, Fz);
