@@ -735,23 +735,19 @@ __device__ __forceinline__ void reduce_forces(const CollideArgs<T>& a, int key, 
 }
 
 // FP32 form: force and torque of the cells of one row segment, reduced per run
-// of equal owner tag with the owner looked up once per run.  Every cell of a
+// of equal owner (keyed by the owner's particle slot, which the cells' surface
+// velocity already looked up).  Every cell of a
 // particle lies within its radius of the particle's nearest image, so along a
 // row the minimum-image arm of cell z is arm(zc) + (z - zc) e_z for any point
 // zc of the segment, and
 //   sum_cells arm x F = arm(zc) x sum F + sum (z - zc) e_z x F,
 // with e_z x F = (-F_y, F_x, 0).  Per cell the kernel accumulates
 // v = (F, -(z - zc) F_y, (z - zc) F_x); the lane that ends a run (the last
-// lane of a run of equal tags, or the first solid lane when one tag covers the
-// warp) maps the tag to the particle slot, takes the arm of its own cell zr,
+// lane of a run of equal slots, or the first solid lane when one slot covers the
+// warp) takes the arm of its own cell zr from the particle's row,
 // arm(zc) = arm(zr) - (zr - zc) e_z, and adds F and arm(zc) x F + (v3, v4, 0).
-__device__ __forceinline__ void finish_run(const CollideArgs<float>& a, int tag, const float (&v)[5], int sx, int sy,
+__device__ __forceinline__ void finish_run(const CollideArgs<float>& a, int slot, const float (&v)[5], int sx, int sy,
                                            int zr, int zc) {
-    const int slot = tag <= a.max_tag ? __ldg(a.tag2slot + tag) : -1;
-    if (slot < 0 || slot >= a.nslot) {
-        atomicOr(a.err, 0x8u);   // LBDEM_DEVERR_UNMAPPED_TAG
-        return;
-    }
     const float4* p = reinterpret_cast<const float4*>(a.xpf + (size_t)slot * XPF_STRIDE);
     const float4 h = __ldg(p), l = __ldg(p + 1);
     float dx = ((float)sx - h.x) - h.w;
@@ -772,7 +768,7 @@ __device__ __forceinline__ void finish_run(const CollideArgs<float>& a, int tag,
     atomicAdd(Tp + 2, (double)(dx * v[1] - dy * v[0]));
 }
 
-// Warp reduction of v over runs of equal key (owner tag, -1: no solid cell);
+// Warp reduction of v over runs of equal key (owner slot, -1: no solid cell);
 // zr is a cell of the lane's run.  Must be reached by all 32 lanes.
 __device__ __forceinline__ void reduce_runs(const CollideArgs<float>& a, int key, float (&v)[5], int zr, int sx,
                                             int sy, int zc) {
@@ -1359,10 +1355,13 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
         whole_row_forces(a, w0, w1, v0, v1, sx, sy, za, zb, fx, fy, fz);
         return;
     }
-    // runs of equal owner tag, arms from the segment's middle point zc
+    // runs of equal owner, arms from the segment's middle point zc
     const int zc = z0 + SEGW / 2;
-    const int ka = (v0 && (w0 & VOX_NMASK)) ? (int)(w0 >> VOX_NBITS) : -1;
-    const int kb = (v1 && (w1 & VOX_NMASK)) ? (int)(w1 >> VOX_NBITS) : -1;
+    // keys: the owners' particle slots; a solid cell whose tag names no particle is
+    // reported and left out
+    const int ka = v0 ? s0 : -1;
+    const int kb = v1 ? s1 : -1;
+    if ((v0 && n0 > 0 && s0 < 0) || (v1 && n1 > 0 && s1 < 0)) atomicOr(a.err, 0x8u);   // LBDEM_DEVERR_UNMAPPED_TAG
     const float da = (float)(za - zc), db = (float)(zb - zc);
     float va[5] = {fx.x, fy.x, fz.x, -da * fy.x, da * fx.x};
     float vb[5] = {fx.y, fy.y, fz.y, -db * fy.y, db * fx.y};
