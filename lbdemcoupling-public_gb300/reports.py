@@ -3,7 +3,7 @@
     python reports.py adjoint      # periodic 128^3, 64 spheres r = 6, 200 steps, checkpoint every 20
     python reports.py precision    # periodic 512x256x256, r ~ U[4, 10] to solid fraction 0.30, 2000 steps
     python reports.py window [--steps S --checkpoint K --fp64]   # one adjoint window of the 128^3 case, timed
-    python reports.py channels [--steps S --flow-axis A]         # batched 512 channels, S coupling cycles
+    python reports.py channels [--steps S --flow-axis A --domains D]  # batched channels (512), S coupling cycles
 
 Each prints one JSON object.  Inputs are seeded synthetic workloads
 (workloads.py); the FP64 form is the reference of the FP32 deviation form.
@@ -185,9 +185,10 @@ def window(steps: int = 6, K: int = 3, fp64: bool = False, seed: int = 2027) -> 
             "forward_ms": fwd, "backward_ms": bwd}
 
 
-def channels(steps: int = 6, flow_axis: int = 2) -> dict:
-    """The batched channels of workloads.channels stepped for a few coupling cycles."""
-    ch = W.channels(flow_axis=flow_axis)
+def channels(steps: int = 6, flow_axis: int = 2, domains: int = 512) -> dict:
+    """The batched channels of workloads.channels stepped for a few coupling cycles
+    (the first `domains` of the seeded sequence: profiling runs take fewer)."""
+    ch = W.channels(n_domains=domains, flow_axis=flow_axis)
     doms = [d for d, _ in ch]
     g = [W.with_ghosts(p, d["shape"], d["periodic"]) for d, p in ch]
     counts = np.array([x.n for x in g], dtype=np.int32)
@@ -209,6 +210,7 @@ def main():
     ap.add_argument("--checkpoint", type=int, default=3)
     ap.add_argument("--fp64", action="store_true")
     ap.add_argument("--flow-axis", type=int, default=2, choices=[0, 2])
+    ap.add_argument("--domains", type=int, default=512)
     a = ap.parse_args()
     if a.which == "adjoint":
         r = adjoint(steps=a.steps or 200)
@@ -217,7 +219,7 @@ def main():
     elif a.which == "window":
         r = window(steps=a.steps or 6, K=a.checkpoint, fp64=a.fp64)
     else:
-        r = channels(steps=a.steps or 6, flow_axis=a.flow_axis)
+        r = channels(steps=a.steps or 6, flow_axis=a.flow_axis, domains=a.domains)
     print(json.dumps(r))
 
 
