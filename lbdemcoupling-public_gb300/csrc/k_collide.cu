@@ -811,6 +811,14 @@ __device__ __forceinline__ int pick(int c, int m, int v, int p) { return c < 0 ?
 // over SEGW-cell z-segments (no block-wide barriers, so a warp with solid
 // cells does not hold up the others).
 constexpr int WARPS = COLLIDE_BLOCK / 32;    // warps per CTA
+// FP32 form, single lattice: each CTA keeps a copy of the tag -> slot map in shared
+// memory when it has at most TAGMAP_SMEM entries (a solid cell's owner lookup is then a
+// shared load, not a global load behind the cell's voxel word).
+constexpr int TAGMAP_SMEM = 2048;
+template <typename T, bool BATCH>
+__host__ __device__ constexpr bool smem_tagmap() { return sizeof(T) == 4 && !BATCH; }
+template <typename T, bool BATCH>
+__host__ __device__ constexpr size_t tagmap_bytes() { return smem_tagmap<T, BATCH>() ? sizeof(int) * TAGMAP_SMEM : 0; }
 constexpr int SEGW = COLLIDE_SEGW;          // cells per warp segment (2 per lane)
 constexpr int WAIT_LIMIT = 1 << 22;         // bounded mbarrier wait (iterations of try_wait)
 constexpr int PROBE_WAIT = 64;              // the timeout test hook's wait (iterations)
@@ -1186,7 +1194,7 @@ __device__ __noinline__ void whole_row_forces(const CollideArgs<float>& a, uint3
 template <bool ODD, bool FORCE, bool PER, bool MIS, bool STAGE_UP>
 __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& a, WarpStage<float, STAGE_UP>& st,
                                                       int b, int sx, int sy, int z0, int len, uint32_t srcrow,
-                                                      unsigned long long lead) {
+                                                      unsigned long long lead, bool smap_ok) {
     constexpr int V = WarpStage<float>::V;
     constexpr bool ADJ = !MIS;
     const int lane = threadIdx.x & 31;
@@ -1227,8 +1235,16 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     // owner particle's row of the float table (one row when both cells belong to
     // the same particle), read after the BGK arithmetic.  (Looking the owners up
     // before the moment sums, or prefetching the rows, measured slower.)
-    const int s0 = n0 > 0 ? owner_slot(w0, a.tag2slot, a.max_tag, a.nslot) : -1;
-    const int s1 = n1 > 0 ? owner_slot(w1, a.tag2slot, a.max_tag, a.nslot) : -1;
+    // owner slots (from the CTA's shared copy of the map when it has one)
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const int* smap = reinterpret_cast<const int*>(smem_raw + WARPS * sizeof(WarpStage<float, STAGE_UP>));
+    auto owner = [&](uint32_t w) -> int {
+        const int tag = (int)(w >> VOX_NBITS);
+        const int slot = tag > a.max_tag ? -1 : (smap_ok ? smap[tag] : __ldg(a.tag2slot + tag));
+        return (slot >= 0 && slot < a.nslot) ? slot : -1;
+    };
+    const int s0 = n0 > 0 ? owner(w0) : -1;
+    const int s1 = n1 > 0 ? owner(w1) : -1;
     F2 up[3] = {bc(0.f), bc(0.f), bc(0.f)};
     auto solid_velocity = [&]() {
         float ua[3] = {0.f, 0.f, 0.f}, ub[3] = {0.f, 0.f, 0.f};
@@ -1409,6 +1425,15 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
     __syncwarp();
+    bool smap_ok = false;   // the CTA holds a copy of the tag -> slot map (FP32, single lattice)
+    if constexpr (smem_tagmap<T, BATCH>()) {
+        int* m = reinterpret_cast<int*>(smem_raw + WARPS * sizeof(WarpStage<T, STAGE_UP>));
+        const int nmap = a1.max_tag + 1;
+        smap_ok = nmap <= TAGMAP_SMEM;
+        if (smap_ok)
+            for (int k = threadIdx.x; k < nmap; k += blockDim.x) m[k] = __ldg(a1.tag2slot + k);
+        __syncthreads();   // every warp of the CTA reaches it (before any leaves)
+    }
     const long long stride = (long long)gridDim.x * WARPS;
     long long seg = (long long)blockIdx.x * WARPS + warp;
     if (seg >= nseg) return;
@@ -1496,7 +1521,8 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
         }
         if constexpr (sizeof(T) == 4) {
             // FP32 form: packed pairs of cells
-            collide_segment_pairs<ODD, FORCE, PER, MIS, STAGE_UP>(a, st, b, sx, sy, z0, len, srcrow, lead);
+            collide_segment_pairs<ODD, FORCE, PER, MIS, STAGE_UP>(a, st, b, sx, sy, z0, len, srcrow, lead,
+                                                                  smap_ok);
         } else {
             // FP64 form: one cell per lane at a time; force and torque per cell with
             // double atomics.  The segment's solid cells are taken first (pass 0
@@ -1583,7 +1609,7 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
 template <typename T, bool ODD, bool FORCE, bool PER, bool MIS, bool BATCH>
 cudaError_t launch_staged(const CollideArgs<T>& a, long long nseg, const CollideArgs<T>* dargs,
                           const int* seg0, int ndom, int blocks_per_sm, cudaStream_t s) {
-    constexpr size_t smem = WARPS * sizeof(WarpStage<T, stage_up<T, BATCH>()>);
+    constexpr size_t smem = WARPS * sizeof(WarpStage<T, stage_up<T, BATCH>()>) + tagmap_bytes<T, BATCH>();
     if (nseg >= (1LL << 31)) return cudaErrorInvalidValue;   // segment indices are split in 32 bits
     // per device: (resident blocks per SM << 16) | SM count, 0 until first use there
     static std::atomic<int> shape[LBDEM_MAX_DEVICES];
