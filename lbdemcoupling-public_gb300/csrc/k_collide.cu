@@ -812,8 +812,10 @@ __device__ __forceinline__ int pick(int c, int m, int v, int p) { return c < 0 ?
 // cells does not hold up the others).
 constexpr int WARPS = COLLIDE_BLOCK / 32;    // warps per CTA
 // FP32 form, single lattice: each CTA keeps a copy of the tag -> slot map in shared
-// memory when it has at most TAGMAP_SMEM entries (a solid cell's owner lookup is then a
-// shared load, not a global load behind the cell's voxel word).
+// memory when the tags fit below TAGMAP_SMEM - 1.  The copy holds -1 for a tag with no
+// particle in the list and for every entry past max_tag (the last one included), so a
+// lookup is one shared load at min(tag, TAGMAP_SMEM - 1) with no tests between the
+// cell's voxel word and the owner's table row.
 constexpr int TAGMAP_SMEM = 2048;
 template <typename T, bool BATCH>
 __host__ __device__ constexpr bool smem_tagmap() { return sizeof(T) == 4 && !BATCH; }
@@ -1240,7 +1242,8 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     const int* smap = reinterpret_cast<const int*>(smem_raw + WARPS * sizeof(WarpStage<float, STAGE_UP>));
     auto owner = [&](uint32_t w) -> int {
         const int tag = (int)(w >> VOX_NBITS);
-        const int slot = tag > a.max_tag ? -1 : (smap_ok ? smap[tag] : __ldg(a.tag2slot + tag));
+        if (smap_ok) return smap[min(tag, TAGMAP_SMEM - 1)];
+        const int slot = tag > a.max_tag ? -1 : __ldg(a.tag2slot + tag);
         return (slot >= 0 && slot < a.nslot) ? slot : -1;
     };
     const int s0 = n0 > 0 ? owner(w0) : -1;
@@ -1428,10 +1431,12 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
     bool smap_ok = false;   // the CTA holds a copy of the tag -> slot map (FP32, single lattice)
     if constexpr (smem_tagmap<T, BATCH>()) {
         int* m = reinterpret_cast<int*>(smem_raw + WARPS * sizeof(WarpStage<T, STAGE_UP>));
-        const int nmap = a1.max_tag + 1;
-        smap_ok = nmap <= TAGMAP_SMEM;
+        smap_ok = a1.max_tag < TAGMAP_SMEM - 1;
         if (smap_ok)
-            for (int k = threadIdx.x; k < nmap; k += blockDim.x) m[k] = __ldg(a1.tag2slot + k);
+            for (int k = threadIdx.x; k < TAGMAP_SMEM; k += blockDim.x) {
+                const int v = k <= a1.max_tag ? __ldg(a1.tag2slot + k) : -1;
+                m[k] = (v >= 0 && v < a1.nslot) ? v : -1;
+            }
         __syncthreads();   // every warp of the CTA reaches it (before any leaves)
     }
     const long long stride = (long long)gridDim.x * WARPS;
