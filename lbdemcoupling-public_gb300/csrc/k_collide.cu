@@ -1252,11 +1252,13 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     auto solid_velocity = [&]() {
         float ua[3] = {0.f, 0.f, 0.f}, ub[3] = {0.f, 0.f, 0.f};
         const int sl = s0 >= 0 ? s0 : s1;
-        if (sl >= 0) {
-            const TableRow r = load_row(a.xpf, sl);
+        {
+            // every lane of the warp loads a row (slot 0 for a lane without a solid
+            // cell, whose velocities stay zero): no branch ahead of the load
+            const TableRow r = load_row(a.xpf, max(sl, 0));
             const RowPart rp = row_part(r, sx, sy, g);
             if (s0 >= 0) cell_part(r, rp, za, g, ua[0], ua[1], ua[2]);
-            if (s1 == sl) cell_part(r, rp, zb, g, ub[0], ub[1], ub[2]);
+            if (sl >= 0 && s1 == sl) cell_part(r, rp, zb, g, ub[0], ub[1], ub[2]);
         }
         if (s1 >= 0 && s1 != sl) row_velocity(load_row(a.xpf, s1), sx, sy, zb, g, ub[0], ub[1], ub[2]);
 #pragma unroll
@@ -1270,7 +1272,7 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     if constexpr (!FORCE) {
         // one pass; the solid terms only in warps that hold a solid cell
         if (__any_sync(FULL, n0 > 0 || n1 > 0)) {
-            if (n0 > 0 || n1 > 0) solid_velocity();
+            solid_velocity();
             collide_g2<true>(f, m, a.omega, up[0], up[1], up[2], B, Fx, Fy, Fz);
         } else {
             collide_g2<false>(f, m, a.omega, up[0], up[1], up[2], B, Fx, Fy, Fz);
