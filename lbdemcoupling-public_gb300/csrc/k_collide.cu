@@ -820,7 +820,9 @@ constexpr int TAGMAP_SMEM = 2048;
 template <typename T, bool BATCH>
 __host__ __device__ constexpr bool smem_tagmap() { return sizeof(T) == 4 && !BATCH; }
 template <typename T, bool BATCH>
-__host__ __device__ constexpr size_t tagmap_bytes() { return smem_tagmap<T, BATCH>() ? sizeof(int) * TAGMAP_SMEM : 0; }
+__host__ __device__ constexpr size_t tagmap_bytes() {
+    return smem_tagmap<T, BATCH>() ? sizeof(int) * TAGMAP_SMEM + sizeof(float) * 128 : 0;
+}
 constexpr int SEGW = COLLIDE_SEGW;          // cells per warp segment (2 per lane)
 constexpr int WAIT_LIMIT = 1 << 22;         // bounded mbarrier wait (iterations of try_wait)
 constexpr int PROBE_WAIT = 64;              // the timeout test hook's wait (iterations)
@@ -1196,7 +1198,7 @@ __device__ __noinline__ void whole_row_forces(const CollideArgs<float>& a, uint3
 template <bool ODD, bool FORCE, bool PER, bool MIS, bool STAGE_UP>
 __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& a, WarpStage<float, STAGE_UP>& st,
                                                       int b, int sx, int sy, int z0, int len, uint32_t srcrow,
-                                                      unsigned long long lead, bool smap_ok) {
+                                                      unsigned long long lead, bool smap_ok, bool sbtab_ok) {
     constexpr int V = WarpStage<float>::V;
     constexpr bool ADJ = !MIS;
     const int lane = threadIdx.x & 31;
@@ -1226,7 +1228,10 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     const int vlead = MIS ? (int)((lead >> 38) & 3u) : 0;
     const uint32_t w0 = v0 ? st.vox[b][vlead + j0] : 0u, w1 = v1 ? st.vox[b][vlead + j1] : 0u;
     const int n0 = min((int)(w0 & VOX_NMASK), 125), n1 = min((int)(w1 & VOX_NMASK), 125);
-    const F2 B = pk(__ldg(a.btab + n0), __ldg(a.btab + n1));
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const float* sbtab =
+        reinterpret_cast<const float*>(smem_raw + WARPS * sizeof(WarpStage<float, STAGE_UP>) + sizeof(int) * TAGMAP_SMEM);
+    const F2 B = sbtab_ok ? pk(sbtab[n0], sbtab[n1]) : pk(__ldg(a.btab + n0), __ldg(a.btab + n1));
 
     // BGK runs for every cell, the fully covered ones included (their solid
     // correction with B = 1 returns fPre + bb up to rounding), so that a cell's
@@ -1238,7 +1243,6 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     // the same particle), read after the BGK arithmetic.  (Looking the owners up
     // before the moment sums, or prefetching the rows, measured slower.)
     // owner slots (from the CTA's shared copy of the map when it has one)
-    extern __shared__ __align__(16) unsigned char smem_raw[];
     const int* smap = reinterpret_cast<const int*>(smem_raw + WARPS * sizeof(WarpStage<float, STAGE_UP>));
     auto owner = [&](uint32_t w) -> int {
         const int tag = (int)(w >> VOX_NBITS);
@@ -1439,6 +1443,8 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
                 const int v = k <= a1.max_tag ? __ldg(a1.tag2slot + k) : -1;
                 m[k] = (v >= 0 && v < a1.nslot) ? v : -1;
             }
+        float* sb = reinterpret_cast<float*>(m + TAGMAP_SMEM);
+        for (int k = threadIdx.x; k < 126; k += blockDim.x) sb[k] = __ldg(a1.btab + k);
         __syncthreads();   // every warp of the CTA reaches it (before any leaves)
     }
     const long long stride = (long long)gridDim.x * WARPS;
@@ -1529,7 +1535,7 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
         if constexpr (sizeof(T) == 4) {
             // FP32 form: packed pairs of cells
             collide_segment_pairs<ODD, FORCE, PER, MIS, STAGE_UP>(a, st, b, sx, sy, z0, len, srcrow, lead,
-                                                                  smap_ok);
+                                                                  smap_ok, smem_tagmap<T, BATCH>());
         } else {
             // FP64 form: one cell per lane at a time; force and torque per cell with
             // double atomics.  The segment's solid cells are taken first (pass 0
