@@ -1247,8 +1247,9 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     auto owner = [&](uint32_t w) -> int {
         const int tag = (int)(w >> VOX_NBITS);
         if (smap_ok) return smap[min(tag, TAGMAP_SMEM - 1)];
-        const int slot = tag > a.max_tag ? -1 : __ldg(a.tag2slot + tag);
-        return (slot >= 0 && slot < a.nslot) ? slot : -1;
+        // global map: an unconditional load at the clamped tag, tested afterwards
+        const int slot = __ldg(a.tag2slot + min(tag, a.max_tag));
+        return (tag <= a.max_tag && slot >= 0 && slot < a.nslot) ? slot : -1;
     };
     const int s0 = n0 > 0 ? owner(w0) : -1;
     const int s1 = n1 > 0 ? owner(w1) : -1;
