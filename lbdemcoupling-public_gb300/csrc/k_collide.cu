@@ -747,9 +747,14 @@ __device__ __forceinline__ void reduce_forces(const CollideArgs<T>& a, int key, 
 // warp) takes the arm of its own cell zr from the particle's row,
 // arm(zc) = arm(zr) - (zr - zc) e_z, and adds F and arm(zc) x F + (v3, v4, 0).
 __device__ __forceinline__ void finish_run(const CollideArgs<float>& a, int slot, const float (&v)[5], int sx, int sy,
-                                           int zr, int zc) {
-    const float4* p = reinterpret_cast<const float4*>(a.xpf + (size_t)slot * XPF_STRIDE);
-    const float4 h = __ldg(p), l = __ldg(p + 1);
+                                           int zr, int zc, const float4& rh, float rl0, float rl1, bool have) {
+    // the lane's own table row when it is the run's owner's (loaded for the velocity)
+    float4 h = rh, l = make_float4(rl0, rl1, 0.f, 0.f);
+    if (!have) {
+        const float4* p = reinterpret_cast<const float4*>(a.xpf + (size_t)slot * XPF_STRIDE);
+        h = __ldg(p);
+        l = __ldg(p + 1);
+    }
     float dx = ((float)sx - h.x) - h.w;
     float dy = ((float)sy - h.y) - l.x;
     float dz = ((float)zr - h.z) - l.y;
@@ -771,7 +776,7 @@ __device__ __forceinline__ void finish_run(const CollideArgs<float>& a, int slot
 // Warp reduction of v over runs of equal key (owner slot, -1: no solid cell);
 // zr is a cell of the lane's run.  Must be reached by all 32 lanes.
 __device__ __forceinline__ void reduce_runs(const CollideArgs<float>& a, int key, float (&v)[5], int zr, int sx,
-                                            int sy, int zc) {
+                                            int sy, int zc, const float4& rh, float rl0, float rl1, int rslot) {
     const unsigned solid = __ballot_sync(FULL, key >= 0);
     if (solid == 0u) return;
     const int lane = threadIdx.x & 31;
@@ -782,7 +787,7 @@ __device__ __forceinline__ void reduce_runs(const CollideArgs<float>& a, int key
         for (int d = 16; d > 0; d >>= 1)
 #pragma unroll
             for (int k = 0; k < 5; ++k) v[k] += __shfl_xor_sync(FULL, v[k], d);
-        if (lane == lead) finish_run(a, first, v, sx, sy, zr, zc);
+        if (lane == lead) finish_run(a, first, v, sx, sy, zr, zc, rh, rl0, rl1, rslot == first);
         return;
     }
     const int prevKey = __shfl_up_sync(FULL, key, 1);
@@ -799,7 +804,7 @@ __device__ __forceinline__ void reduce_runs(const CollideArgs<float>& a, int key
     }
     const int nextKey = __shfl_down_sync(FULL, key, 1);
     const bool tail = (lane == 31) || (nextKey != key);
-    if (tail && key >= 0) finish_run(a, key, v, sx, sy, zr, zc);
+    if (tail && key >= 0) finish_run(a, key, v, sx, sy, zr, zc, rh, rl0, rl1, rslot == key);
 }
 
 __device__ __forceinline__ int wrap_minus(int v, int n, int per) { return v > 0 ? v - 1 : (per ? n - 1 : -1); }
@@ -1254,6 +1259,10 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     const int s0 = n0 > 0 ? owner(w0) : -1;
     const int s1 = n1 > 0 ? owner(w1) : -1;
     F2 up[3] = {bc(0.f), bc(0.f), bc(0.f)};
+    // the centre part of the row the velocity read (slot vslot), kept for the force flush
+    float4 vrh = make_float4(0.f, 0.f, 0.f, 0.f);
+    float vrl0 = 0.f, vrl1 = 0.f;
+    int vslot = -1;
     auto solid_velocity = [&]() {
         float ua[3] = {0.f, 0.f, 0.f}, ub[3] = {0.f, 0.f, 0.f};
         const int sl = s0 >= 0 ? s0 : s1;
@@ -1261,6 +1270,7 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
             // every lane of the warp loads a row (slot 0 for a lane without a solid
             // cell, whose velocities stay zero): no branch ahead of the load
             const TableRow r = load_row(a.xpf, max(sl, 0));
+            vrh = r.a; vrl0 = r.b.x; vrl1 = r.b.y; vslot = sl;
             const RowPart rp = row_part(r, sx, sy, g);
             if (s0 >= 0) cell_part(r, rp, za, g, ua[0], ua[1], ua[2]);
             if (sl >= 0 && s1 == sl) cell_part(r, rp, zb, g, ub[0], ub[1], ub[2]);
@@ -1400,10 +1410,10 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
         const int key = ka >= 0 ? ka : kb;
 #pragma unroll
         for (int q = 0; q < 5; ++q) va[q] += vb[q];
-        reduce_runs(a, key, va, ka >= 0 ? za : zb, sx, sy, zc);
+        reduce_runs(a, key, va, ka >= 0 ? za : zb, sx, sy, zc, vrh, vrl0, vrl1, vslot);
     } else {
-        reduce_runs(a, ka, va, za, sx, sy, zc);
-        reduce_runs(a, kb, vb, zb, sx, sy, zc);
+        reduce_runs(a, ka, va, za, sx, sy, zc, vrh, vrl0, vrl1, vslot);
+        reduce_runs(a, kb, vb, zb, sx, sy, zc, vrh, vrl0, vrl1, vslot);
     }
 }
 
