@@ -828,6 +828,11 @@ template <typename T, bool BATCH>
 __host__ __device__ constexpr size_t tagmap_bytes() {
     return smem_tagmap<T, BATCH>() ? sizeof(int) * TAGMAP_SMEM + sizeof(float) * 128 : 0;
 }
+// Batch mode: each CTA keeps the first segment of every domain in shared memory when
+// there are at most SEG0_SMEM domains (the per-segment domain search reads it there).
+constexpr int SEG0_SMEM = 2048;
+template <bool BATCH>
+__host__ __device__ constexpr size_t seg0_bytes() { return BATCH ? sizeof(int) * SEG0_SMEM : 0; }
 constexpr int SEGW = COLLIDE_SEGW;          // cells per warp segment (2 per lane)
 constexpr int WAIT_LIMIT = 1 << 22;         // bounded mbarrier wait (iterations of try_wait)
 constexpr int PROBE_WAIT = 64;              // the timeout test hook's wait (iterations)
@@ -1458,6 +1463,15 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
         for (int k = threadIdx.x; k < 126; k += blockDim.x) sb[k] = __ldg(a1.btab + k);
         __syncthreads();   // every warp of the CTA reaches it (before any leaves)
     }
+    const int* sseg0 = nullptr;   // batch: the CTA's copy of seg0 (ndom <= SEG0_SMEM)
+    if constexpr (BATCH) {
+        int* m = reinterpret_cast<int*>(smem_raw + WARPS * sizeof(WarpStage<T, STAGE_UP>));
+        if (ndom <= SEG0_SMEM) {
+            for (int k = threadIdx.x; k < ndom; k += blockDim.x) m[k] = __ldg(seg0 + k);
+            sseg0 = m;
+        }
+        __syncthreads();   // every warp of the CTA reaches it (before any leaves)
+    }
     const long long stride = (long long)gridDim.x * WARPS;
     long long seg = (long long)blockIdx.x * WARPS + warp;
     if (seg >= nseg) return;
@@ -1467,9 +1481,22 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
             return T(0);
         }
         if (BATCH) {
-            const int d = find_domain(seg0, ndom, (int)sg);
+            int d, first;
+            if (sseg0) {
+                int lo = 0, hi = ndom - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (sseg0[mid] <= (int)sg) lo = mid;
+                    else hi = mid - 1;
+                }
+                d = lo;
+                first = sseg0[d];
+            } else {
+                d = find_domain(seg0, ndom, (int)sg);
+                first = __ldg(seg0 + d);
+            }
             const CollideArgs<T>& A = dargs[d];
-            return issue_segment<T, ODD, MIS, STAGE_UP>(A, st, buf, sg - __ldg(seg0 + d), d);
+            return issue_segment<T, ODD, MIS, STAGE_UP>(A, st, buf, sg - first, d);
         }
         return issue_segment<T, ODD, MIS, STAGE_UP>(a1, st, buf, sg, 0);
     };
@@ -1633,7 +1660,8 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
 template <typename T, bool ODD, bool FORCE, bool PER, bool MIS, bool BATCH>
 cudaError_t launch_staged(const CollideArgs<T>& a, long long nseg, const CollideArgs<T>* dargs,
                           const int* seg0, int ndom, int blocks_per_sm, cudaStream_t s) {
-    constexpr size_t smem = WARPS * sizeof(WarpStage<T, stage_up<T, BATCH>()>) + tagmap_bytes<T, BATCH>();
+    constexpr size_t smem =
+        WARPS * sizeof(WarpStage<T, stage_up<T, BATCH>()>) + tagmap_bytes<T, BATCH>() + seg0_bytes<BATCH>();
     if (nseg >= (1LL << 31)) return cudaErrorInvalidValue;   // segment indices are split in 32 bits
     // per device: (resident blocks per SM << 16) | SM count, 0 until first use there
     static std::atomic<int> shape[LBDEM_MAX_DEVICES];
