@@ -329,6 +329,7 @@ __device__ __noinline__ int slice_count_resolve(float dxf, float dyf, float dzf,
 constexpr int VOX_WARPS = 8;                        // warps per block
 constexpr int VOX_THREADS = 32 * VOX_WARPS;
 constexpr int VOX_STAGE = 32;                       // sphere records staged at a time
+constexpr int TOFF_SMEM = 512;                      // batch: domains whose first tiles a CTA keeps
 constexpr uint32_t SETTER_ZERO = 0xffffffffu;       // the cell was set to zero (setToZero)
 constexpr uint32_t SETTER_KEEP = 0xfffffffeu;       // the cell keeps its state (and velocity)
 
@@ -670,6 +671,17 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
     extern __shared__ __align__(16) unsigned char smem_raw[];
     WarpVox<INIT_VEL>& S = reinterpret_cast<WarpVox<INIT_VEL>*>(smem_raw)[threadIdx.x >> 5];
     const int lane = threadIdx.x & 31;
+    // batch: the CTA's copy of the domains' first tiles (ndom <= TOFF_SMEM), for the
+    // per-tile domain search
+    const int* stoff = nullptr;
+    if constexpr (BATCH) {
+        int* m = reinterpret_cast<int*>(smem_raw + sizeof(WarpVox<INIT_VEL>) * VOX_WARPS);
+        if (ndom <= TOFF_SMEM) {
+            for (int k = threadIdx.x; k < ndom; k += blockDim.x) m[k] = __ldg(toff + k);
+            stoff = m;
+        }
+        __syncthreads();   // every thread of the CTA reaches it (before any leaves)
+    }
     const int nwork = *(volatile int*)work_n;
     // the next tile is claimed and its index read while the current one is worked on
     auto claim = [&]() -> int {
@@ -683,7 +695,18 @@ k_voxelize(const SphereDev* __restrict__ sph, const SphereFast* __restrict__ fas
         const int tg = next;
         next = claim();
         if (BATCH) {
-            const int d = find_domain(toff, ndom, tg);
+            int d;
+            if (stoff) {
+                int lo = 0, hi = ndom - 1;
+                while (lo < hi) {
+                    const int mid = (lo + hi + 1) >> 1;
+                    if (stoff[mid] <= tg) lo = mid;
+                    else hi = mid - 1;
+                }
+                d = lo;
+            } else {
+                d = find_domain(toff, ndom, tg);
+            }
             const DomView& D = doms[d];
             const OwnerTable od{ot.xpf + (size_t)XPF_STRIDE * D.s0, ot.tag2slot + D.tag0, ot.max_tag};
             voxelize_tile<T, INIT_VEL>(S, tg - D.t0, sph + D.s0, fast + D.s0, __ldg(ncur + d), tile_cnt + D.t0,
@@ -736,7 +759,7 @@ cudaError_t launch_vox(const SphereDev* sph, const SphereFast* fast, int n, int*
                        const int* work, int* work_n, int ntiles, uint32_t* vox, T* up, T* f, int phase, Geom g,
                        const DomView* doms, const int* toff, int ndom, const int* ncur, const OwnerTable& ot,
                        cudaStream_t s) {
-    constexpr size_t smem = sizeof(WarpVox<INIT_VEL>) * VOX_WARPS;
+    constexpr size_t smem = sizeof(WarpVox<INIT_VEL>) * VOX_WARPS + (BATCH ? sizeof(int) * TOFF_SMEM : 0);
     static std::atomic<int> cached[LBDEM_MAX_DEVICES];   // per device: persistent grid size
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
