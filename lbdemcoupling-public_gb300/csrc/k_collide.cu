@@ -816,11 +816,12 @@ __device__ __forceinline__ int pick(int c, int m, int v, int p) { return c < 0 ?
 // over SEGW-cell z-segments (no block-wide barriers, so a warp with solid
 // cells does not hold up the others).
 constexpr int WARPS = COLLIDE_BLOCK / 32;    // warps per CTA
-// FP32 form, single lattice: each CTA keeps a copy of the tag -> slot map in shared
-// memory when the tags fit below TAGMAP_SMEM - 1.  The copy holds -1 for a tag with no
-// particle in the list and for every entry past max_tag (the last one included), so a
-// lookup is one shared load at min(tag, TAGMAP_SMEM - 1) with no tests between the
-// cell's voxel word and the owner's table row.
+// Per-CTA tables in dynamic shared memory behind the warps' stages.
+// FP32 form, single lattice: a copy of the tag -> slot map when the tags fit below
+// TAGMAP_SMEM - 1, holding -1 for a tag with no particle in the list and for every entry
+// past max_tag (the last one included), so that a lookup is one shared load at
+// min(tag, TAGMAP_SMEM - 1) with no tests between the cell's voxel word and the owner's
+// table row; then B(n) (128 floats).
 constexpr int TAGMAP_SMEM = 2048;
 template <typename T, bool BATCH>
 __host__ __device__ constexpr bool smem_tagmap() { return sizeof(T) == 4 && !BATCH; }
@@ -864,6 +865,13 @@ static_assert(sizeof(WarpStage<float, true>) % 16 == 0 && sizeof(WarpStage<float
 static_assert(offsetof(WarpStage<float>, vox) % 16 == 0 && offsetof(WarpStage<float>, up) % 16 == 0 &&
                   offsetof(WarpStage<double>, vox) % 16 == 0 && offsetof(WarpStage<double>, up) % 16 == 0,
               "bulk-copy destinations on 16-byte boundaries");
+
+// The per-CTA tables behind the warps' stages.
+template <typename T, bool STAGE_UP>
+__device__ __forceinline__ unsigned char* cta_tables() {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    return smem_raw + WARPS * sizeof(WarpStage<T, STAGE_UP>);
+}
 
 __device__ __forceinline__ constexpr int row_slot(int dx, int dy) { return 3 * (dx + 1) + dy + 1; }
 
@@ -1238,9 +1246,8 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     const int vlead = MIS ? (int)((lead >> 38) & 3u) : 0;
     const uint32_t w0 = v0 ? st.vox[b][vlead + j0] : 0u, w1 = v1 ? st.vox[b][vlead + j1] : 0u;
     const int n0 = min((int)(w0 & VOX_NMASK), 125), n1 = min((int)(w1 & VOX_NMASK), 125);
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    const float* sbtab =
-        reinterpret_cast<const float*>(smem_raw + WARPS * sizeof(WarpStage<float, STAGE_UP>) + sizeof(int) * TAGMAP_SMEM);
+    const int* smap = reinterpret_cast<const int*>(cta_tables<float, STAGE_UP>());
+    const float* sbtab = reinterpret_cast<const float*>(smap + TAGMAP_SMEM);
     const F2 B = sbtab_ok ? pk(sbtab[n0], sbtab[n1]) : pk(__ldg(a.btab + n0), __ldg(a.btab + n1));
 
     // BGK runs for every cell, the fully covered ones included (their solid
@@ -1253,7 +1260,6 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     // the same particle), read after the BGK arithmetic.  (Looking the owners up
     // before the moment sums, or prefetching the rows, measured slower.)
     // owner slots (from the CTA's shared copy of the map when it has one)
-    const int* smap = reinterpret_cast<const int*>(smem_raw + WARPS * sizeof(WarpStage<float, STAGE_UP>));
     auto owner = [&](uint32_t w) -> int {
         const int tag = (int)(w >> VOX_NBITS);
         if (smap_ok) return smap[min(tag, TAGMAP_SMEM - 1)];
@@ -1452,7 +1458,7 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
     __syncwarp();
     bool smap_ok = false;   // the CTA holds a copy of the tag -> slot map (FP32, single lattice)
     if constexpr (smem_tagmap<T, BATCH>()) {
-        int* m = reinterpret_cast<int*>(smem_raw + WARPS * sizeof(WarpStage<T, STAGE_UP>));
+        int* m = reinterpret_cast<int*>(cta_tables<T, STAGE_UP>());
         smap_ok = a1.max_tag < TAGMAP_SMEM - 1;
         if (smap_ok)
             for (int k = threadIdx.x; k < TAGMAP_SMEM; k += blockDim.x) {
@@ -1465,7 +1471,7 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
     }
     const int* sseg0 = nullptr;   // batch: the CTA's copy of seg0 (ndom <= SEG0_SMEM)
     if constexpr (BATCH) {
-        int* m = reinterpret_cast<int*>(smem_raw + WARPS * sizeof(WarpStage<T, STAGE_UP>));
+        int* m = reinterpret_cast<int*>(cta_tables<T, STAGE_UP>());
         if (ndom <= SEG0_SMEM) {
             for (int k = threadIdx.x; k < ndom; k += blockDim.x) m[k] = __ldg(seg0 + k);
             sseg0 = m;

@@ -16,6 +16,9 @@
   up to 170 spheres reach one 8^3 tile (mean about 16, eight tiles past the
   64-entry bin), so the tile-bin ordering and the bin-overflow path run at
   scale.  Same bars.
+* ``test_dense_polydisperse_large_tags``: the same spheres with tags spread up to
+  about 6000: the collide-stream kernel then looks owners up in the global
+  tag -> slot map instead of its shared-memory copy (which holds tags below 2047).
 
 Reference: src/ibProcessors3D.hh:53-184 (voxelization), :203-263 (force sum),
 src/ibCompositeDynamics3D.hh:130-203 (collision).
@@ -120,7 +123,7 @@ def test_headline_workload(gpu, oracle):
     _compare(gpu, oracle, shape, 0.55, tables, check_pops_every=False)
 
 
-def test_dense_polydisperse(gpu, oracle):
+def _dense_polydisperse(tag_of):
     rng = np.random.default_rng(11)
     shape = (96, 96, 96)
     n_big, n_small = 700, 150
@@ -128,11 +131,22 @@ def test_dense_polydisperse(gpu, oracle):
     r = np.concatenate([rng.uniform(4.0, 10.0, n_big), rng.uniform(0.6, 1.5, n_small)])
     n = n_big + n_small
     p = W.Particles(x, rng.normal(0, 0.01, (n, 3)), rng.normal(0, 1e-3, (n, 3)), r,
-                    np.arange(1, n + 1, dtype=np.int32))
+                    tag_of(np.arange(n)).astype(np.int32))
     tables = []
     for _ in range(3):
         tables.append(W.with_ghosts(p, shape))
         p = W.advance(p, shape)
     load = _tile_load(tables[0], shape)
     assert load.max() > 64 and (load >= 20).sum() >= 100 and r.max() > 9.5
+    return shape, tables
+
+
+def test_dense_polydisperse(gpu, oracle):
+    shape, tables = _dense_polydisperse(lambda i: i + 1)
+    _compare(gpu, oracle, shape, 0.6, tables)
+
+
+def test_dense_polydisperse_large_tags(gpu, oracle):
+    shape, tables = _dense_polydisperse(lambda i: 7 * i + 13)
+    assert max(int(g.tag.max()) for g in tables) > 4000
     _compare(gpu, oracle, shape, 0.6, tables)
