@@ -402,6 +402,33 @@ __device__ __noinline__ void apply_sphere(WarpVox<INIT_VEL>& S, const SphereFast
         inh[h] = zin && y >= by0 && y <= by1;
         meet[h] = !(4 * h > by1 || 4 * h + 3 < by0);   // warp-uniform
     }
+    // A sphere whose shell stays clear of the box's cells in this tile (about half
+    // of the (tile, sphere) pairs at r = 8) only clears the cells that hold its tag
+    // (decFlag 2, setToZero): the box's squared distance from the centre, formed
+    // like a cell's, is more than 2 M beyond (r + sqrt(3.1)/2)^2, so every cell of the
+    // box is outside in the reference's double arithmetic too.
+    {
+        auto gap = [](float lo, float hi) { return fmaxf(0.f, fmaxf(lo, -hi)); };
+        const float ex = gap(((float)(X0 + bx0) - q.xh[0]) - q.xl[0], ((float)(X0 + bx1) - q.xh[0]) - q.xl[0]);
+        const float ey = gap(((float)(Y0 + by0) - q.xh[1]) - q.xl[1], ((float)(Y0 + by1) - q.xh[1]) - q.xl[1]);
+        const float ez = gap(((float)(Z0 + bz0) - q.xh[2]) - q.xl[2], ((float)(Z0 + bz1) - q.xh[2]) - q.xl[2]);
+        const float d2 = __fmaf_rn(ex, ex, __fmaf_rn(ey, ey, __fmul_rn(ez, ez)));
+        if (d2 > rp2 + 2.f * M) {   // warp-uniform
+            for (int x = bx0; x <= bx1; ++x) {
+#pragma unroll
+                for (int h = 0; h < 2; ++h) {
+                    if (!meet[h] || !inh[h]) continue;
+                    const int l = lane + 64 * x + 32 * h;
+                    const uint32_t w = S.w[l];
+                    if ((w & VOX_NMASK) != 0u && (w >> VOX_NBITS) == tag) {
+                        S.w[l] = 0u;
+                        S.setter[l] = SETTER_ZERO;
+                    }
+                }
+            }
+            return;
+        }
+    }
     for (int x = bx0; x <= bx1; ++x) {
         const float dxf = ((float)(X0 + x) - q.xh[0]) - q.xl[0];
 #pragma unroll
