@@ -138,3 +138,32 @@ def test_subcell_band_decides_like_double(fused):
         assert np.array_equal(d32[near].astype(np.float64), t32[near].astype(np.float64) - float(rsq_f))
         checked += int(inside.sum() + outside.sum())
     assert checked > 10 ** 6
+
+
+def test_box_distance_bounds_every_cell():
+    """k_voxel.cu skips the per-cell classification of a (tile, sphere) pair when the
+    float squared distance from the centre to the box of the sphere's cells in the
+    tile exceeds (r + sqrt(3.1)/2)^2 + 2 M: the box distance is formed from the box
+    corners' float offsets with the cells' operation order, so it is at most every
+    cell's float distance (each rounding is monotone in non-negative terms), and
+    every cell is then outside without the double-precision test."""
+    x, r = _spheres(5, 40)
+    rng = np.random.default_rng(6)
+    checked = 0
+    for c, rad in zip(x, r):
+        xh, xl = _split(c)
+        lo = np.trunc(c - rad - 2.0).astype(np.int64)
+        for _ in range(40):
+            a = lo + rng.integers(0, int(2 * rad + 4), 3)
+            b = a + rng.integers(0, 8, 3)
+            X, Y, Z = np.meshgrid(*[np.arange(a[d], b[d] + 1) for d in range(3)], indexing="ij")
+            P = np.stack([X.ravel(), Y.ravel(), Z.ravel()], 1)
+            df = (P.astype(np.float32) - xh) - xl
+            cell = _dist_f(df[:, 0], df[:, 1], df[:, 2], "kernel")
+            lo_f = (a.astype(np.float32) - xh) - xl
+            hi_f = (b.astype(np.float32) - xh) - xl
+            e = np.maximum(f32(0), np.maximum(lo_f, -hi_f)).astype(np.float32)
+            box = _dist_f(e[None, 0], e[None, 1], e[None, 2], "kernel")[0]
+            assert box <= cell.min()
+            checked += len(P)
+    assert checked > 10 ** 5
