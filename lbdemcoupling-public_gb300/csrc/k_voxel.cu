@@ -272,7 +272,10 @@ __device__ __forceinline__ int slice_count_fast(float dxf, float dyf, float dzf,
 
 // The same slice with the samples inside the band decided by the reference's
 // double sequence ((xs_i + ys_j) + zs_k < r^2, src/ibProcessors3D.hh:141-155).
-__device__ __noinline__ int slice_count_resolve(float dxf, float dyf, float dzf, int i, float rsq, float M, int X,
+// Inlined into the count loop (a call there cost its register saves and restores on
+// every pass, 0.235 against 0.227 ms; the cell-distance routine region_exact stays out
+// of line, inlining it measured slower).
+__device__ __forceinline__ int slice_count_resolve(float dxf, float dyf, float dzf, int i, float rsq, float M, int X,
                                                 int Y, int Z, const SphereDev& s) {
     const double dx = __dsub_rn((double)X, s.x[0]);
     const double dy = __dsub_rn((double)Y, s.x[1]);
