@@ -350,7 +350,7 @@ struct alignas(16) WarpVox {
     uint32_t defv[INIT_VEL ? TILE_CELLS : 1];
     uint32_t cnt4[TILE_CELLS / 4];                  // shell sub-cell counts, one byte per cell
     uint16_t queue[TILE_CELLS];                     // shell cells of the current sphere
-    uint8_t items[5 * 32];                          // x-slices left to count: (cell in chunk) << 3 | slice
+    uint16_t items[5 * 32];                         // x-slices left to count: tile cell << 3 | slice
 };
 
 // decFlag, src/ibProcessors3D.hh:85-105 (sf > 0.001 <=> n > 0; sf > sf_old <=>
@@ -467,8 +467,9 @@ __device__ __forceinline__ void apply_sphere(WarpVox<INIT_VEL>& S, const SphereF
     // and counted sample by sample, one slice per lane.
     for (int c0 = 0; c0 < qn; c0 += 32) {
         uint32_t mixed = 0u;
+        int l = 0;
         if (c0 + lane < qn) {
-            const int l = S.queue[c0 + lane];
+            l = S.queue[c0 + lane];
             const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
             const float dxf = ((float)X - q.xh[0]) - q.xl[0];
             const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
@@ -502,11 +503,11 @@ __device__ __forceinline__ void apply_sphere(WarpVox<INIT_VEL>& S, const SphereF
             if (lane >= d) incl += o;
         }
         const int total = __shfl_sync(FULL_MASK, incl, 31);
-        for (int pos = incl - k; mixed; mixed &= mixed - 1u) S.items[pos++] = (uint8_t)((lane << 3) | (__ffs(mixed) - 1));
+        for (int pos = incl - k; mixed; mixed &= mixed - 1u) S.items[pos++] = (uint16_t)((l << 3) | (__ffs(mixed) - 1));
         __syncwarp();
         for (int u = lane; u < total; u += 32) {
             const int it = S.items[u];
-            const int l = S.queue[c0 + (it >> 3)], i = it & 7;
+            const int l = it >> 3, i = it & 7;
             const int X = X0 + (l >> 6), Y = Y0 + ((l >> 3) & 7), Z = Z0 + (l & 7);
             const float dxf = ((float)X - q.xh[0]) - q.xl[0];
             const float dyf = ((float)Y - q.xh[1]) - q.xl[1];
