@@ -653,6 +653,21 @@ __device__ __forceinline__ double widen(double x) { return x; }
 // Per-cell force and torque of a solid cell (SumForceTorque3D,
 // src/ibProcessors3D.hh:203-263): particle slot of the owner tag and the
 // terms F, r x F with the minimum-image arm of :230-243.  Returns the slot or -1.
+// The terms F and r x F of a cell with arm (dx, dy, dz) before the minimum image
+// (integer half extents of g, src/ibProcessors3D.hh:230-243).
+template <typename T>
+__device__ __forceinline__ void arm_terms(T dx, T dy, T dz, const Geom& g, T Fx, T Fy, T Fz, T (&v)[6]) {
+    const int nx = g.nx, ny = g.ny, nz = g.nz;
+    const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
+    if (dx > T(hx)) dx -= T(nx); else if (dx < T(-hx)) dx += T(nx);
+    if (dy > T(hy)) dy -= T(ny); else if (dy < T(-hy)) dy += T(ny);
+    if (dz > T(hz)) dz -= T(nz); else if (dz < T(-hz)) dz += T(nz);
+    v[0] = Fx; v[1] = Fy; v[2] = Fz;
+    v[3] = dy * Fz - dz * Fy;
+    v[4] = -dx * Fz + dz * Fx;
+    v[5] = dx * Fy - dy * Fx;
+}
+
 template <typename T>
 __device__ __forceinline__ int cell_force_terms(const CollideArgs<T>& a, uint32_t w, int x, int y, int z, T Fx,
                                                 T Fy, T Fz, T (&v)[6]) {
@@ -677,15 +692,7 @@ __device__ __forceinline__ int cell_force_terms(const CollideArgs<T>& a, uint32_
         dy = T(((float)y - h.y) - l.x);
         dz = T(((float)z - h.z) - l.y);
     }
-    const int nx = a.g.nx, ny = a.g.ny, nz = a.g.nz;
-    const int hx = nx / 2, hy = ny / 2, hz = nz / 2;
-    if (dx > T(hx)) dx -= T(nx); else if (dx < T(-hx)) dx += T(nx);
-    if (dy > T(hy)) dy -= T(ny); else if (dy < T(-hy)) dy += T(ny);
-    if (dz > T(hz)) dz -= T(nz); else if (dz < T(-hz)) dz += T(nz);
-    v[0] = Fx; v[1] = Fy; v[2] = Fz;
-    v[3] = dy * Fz - dz * Fy;
-    v[4] = -dx * Fz + dz * Fx;
-    v[5] = dx * Fy - dy * Fx;
+    arm_terms(dx, dy, dz, a.g, Fx, Fy, Fz, v);
     return slot;
 }
 
@@ -1213,10 +1220,17 @@ __device__ __noinline__ void whole_row_forces(const CollideArgs<float>& a, uint3
 // l takes j = l and l + 32 (32-bit accesses, conflict-free and coalesced).
 // Force and torque are reduced per run of equal owner (reduce_runs); the two
 // cells of a lane go through one warp reduction when their owners agree.
-template <bool ODD, bool FORCE, bool PER, bool MIS, bool STAGE_UP>
+// FLAT (even phase of the FP32 batch): the segment is 64 cells of an x-plane
+// taken in memory order across its z-rows (a.g is the plane view, see
+// CollideArgs); a solid cell's true (y, z) is recovered from its index in the
+// plane, and force and torque take per-cell arms (a run may cross rows).  The
+// even phase touches only the cell's own slots, so a cell's populations do
+// not depend on how the cells are grouped into segments.
+template <bool ODD, bool FORCE, bool PER, bool MIS, bool STAGE_UP, bool FLAT = false>
 __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& a, WarpStage<float, STAGE_UP>& st,
                                                       int b, int sx, int sy, int z0, int len, uint32_t srcrow,
                                                       unsigned long long lead, bool smap_ok, bool sbtab_ok) {
+    static_assert(!FLAT || (!ODD && MIS), "plane segments: even phase, unaligned-row staging");
     constexpr int V = WarpStage<float>::V;
     constexpr bool ADJ = !MIS;
     const int lane = threadIdx.x & 31;
@@ -1228,6 +1242,22 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     const bool v0 = j0 < len, v1 = j1 < len;
     const int za = z0 + j0, zb = z0 + j1;
     const size_t ca = own + za, cb = own + zb;
+    // the cells' true geometry and coordinates (y, z) (FLAT: from the plane index;
+    // otherwise gt is g itself, not a copy that would hold its fields in registers)
+    Geom gflat;
+    if constexpr (FLAT) {
+        gflat = g;
+        gflat.ny = a.flat_ny;
+        gflat.nz = a.flat_nz;
+    }
+    const Geom& gt = FLAT ? gflat : g;
+    int ya = sy, yb = sy, zta = za, ztb = zb;
+    if constexpr (FLAT) {
+        ya = (int)fast_div((unsigned)za, a.dnz);
+        yb = (int)fast_div((unsigned)zb, a.dnz);
+        zta = za - ya * a.flat_nz;
+        ztb = zb - yb * a.flat_nz;
+    }
 
     // staged values of direction i for the lane's two cells
     auto at2 = [&](int i) -> F2 {
@@ -1282,11 +1312,14 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
             // cell, whose velocities stay zero): no branch ahead of the load
             const TableRow r = load_row(a.xpf, max(sl, 0));
             vrh = r.a; vrl0 = r.b.x; vrl1 = r.b.y; vslot = sl;
-            const RowPart rp = row_part(r, sx, sy, g);
-            if (s0 >= 0) cell_part(r, rp, za, g, ua[0], ua[1], ua[2]);
-            if (sl >= 0 && s1 == sl) cell_part(r, rp, zb, g, ub[0], ub[1], ub[2]);
+            const RowPart rp = row_part(r, sx, ya, gt);
+            if (s0 >= 0) cell_part(r, rp, zta, gt, ua[0], ua[1], ua[2]);
+            if (sl >= 0 && s1 == sl) {
+                if (FLAT && yb != ya) cell_part(r, row_part(r, sx, yb, gt), ztb, gt, ub[0], ub[1], ub[2]);
+                else cell_part(r, rp, ztb, gt, ub[0], ub[1], ub[2]);
+            }
         }
-        if (s1 >= 0 && s1 != sl) row_velocity(load_row(a.xpf, s1), sx, sy, zb, g, ub[0], ub[1], ub[2]);
+        if (s1 >= 0 && s1 != sl) row_velocity(load_row(a.xpf, s1), sx, yb, ztb, gt, ub[0], ub[1], ub[2]);
 #pragma unroll
         for (int d = 0; d < 3; ++d) up[d] = pk(ua[d], ub[d]);
     };
@@ -1395,6 +1428,41 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
     if (a.cf) {
         if (v0) { a.cf[ca] = fx.x; a.cf[N + ca] = fy.x; a.cf[2 * N + ca] = fz.x; }
         if (v1) { a.cf[cb] = fx.y; a.cf[N + cb] = fy.y; a.cf[2 * N + cb] = fz.y; }
+    }
+    if constexpr (FLAT) {
+        // per-cell arms (a run of one owner may cross rows here), keyed by the owner
+        // slots of the velocity lookup; the arm reads the centre from the table row
+        // that lookup kept (a second owner in the lane reads its own row)
+        if ((v0 && n0 > 0 && s0 < 0) || (v1 && n1 > 0 && s1 < 0)) atomicOr(a.err, 0x8u);   // LBDEM_DEVERR_UNMAPPED_TAG
+        const int ka = v0 ? s0 : -1;
+        const int kb = v1 ? s1 : -1;
+        if (!__any_sync(FULL, ka >= 0 || kb >= 0)) return;
+        auto terms = [&](int slot, int y, int z, float cfx, float cfy, float cfz, float (&v)[6]) {
+            float4 h = vrh;
+            float lx = vrl0, lz = vrl1;
+            if (slot != vslot) {
+                const float4* p = reinterpret_cast<const float4*>(a.xpf + (size_t)slot * XPF_STRIDE);
+                h = __ldg(p);
+                const float4 l = __ldg(p + 1);
+                lx = l.x;
+                lz = l.y;
+            }
+            // centre = hi + lo in float: (x - hi) - lo is the arm to ~1 ulp
+            arm_terms(((float)sx - h.x) - h.w, ((float)y - h.y) - lx, ((float)z - h.z) - lz, gt, cfx, cfy, cfz, v);
+        };
+        float va[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, vb[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+        if (ka >= 0) terms(ka, ya, zta, fx.x, fy.x, fz.x, va);
+        if (kb >= 0) terms(kb, yb, ztb, fx.y, fy.y, fz.y, vb);
+        if (__all_sync(FULL, ka < 0 || kb < 0 || ka == kb)) {
+            const int key = ka >= 0 ? ka : kb;
+#pragma unroll
+            for (int q = 0; q < 6; ++q) va[q] += vb[q];
+            reduce_forces(a, key, va);
+        } else {
+            reduce_forces(a, ka, va);
+            reduce_forces(a, kb, vb);
+        }
+        return;
     }
     if ((PER || g.per[2]) && len == g.nz) {
         // the segment is a whole z-periodic row: a particle's chord may wrap
@@ -1577,9 +1645,10 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
                 if (cz(i) != 0 && st.row[b][row_slot(-cx(i), -cy(i))] >= 0) srcrow |= 1u << i;
         }
         if constexpr (sizeof(T) == 4) {
-            // FP32 form: packed pairs of cells
-            collide_segment_pairs<ODD, FORCE, PER, MIS, STAGE_UP>(a, st, b, sx, sy, z0, len, srcrow, lead,
-                                                                  smap_ok, smem_tagmap<T, BATCH>());
+            // FP32 form: packed pairs of cells (batch, even phase: plane segments)
+            collide_segment_pairs<ODD, FORCE, PER, MIS, STAGE_UP, BATCH && !ODD>(a, st, b, sx, sy, z0, len, srcrow,
+                                                                                lead, smap_ok,
+                                                                                smem_tagmap<T, BATCH>());
         } else {
             // FP64 form: one cell per lane at a time; force and torque per cell with
             // double atomics.  The segment's solid cells are taken first (pass 0

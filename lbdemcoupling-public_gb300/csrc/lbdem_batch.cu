@@ -33,10 +33,11 @@ struct lbdem_batch {
 
     std::vector<lbdem_domain> dom;
     std::vector<DomView> views;          // host copy of d_views
-    std::vector<int> soff, toff, seg0;   // per-domain first slot / tile / segment
+    std::vector<int> soff, toff, seg0;   // per-domain first slot / tile / segment; seg0 holds the row
+                                         // segments, then (FP32 even phase) the plane segments
     std::vector<int> cap;
     int nslots = 0, ntiles = 0;
-    long long nseg = 0;
+    long long nseg = 0, nseg_plane = 0;
     size_t ncells = 0, f_elems = 0, up_elems = 0, vox_elems = 0;
 
     void* f = nullptr;
@@ -59,8 +60,8 @@ struct lbdem_batch {
     DomView* d_views = nullptr;
     int* d_soff = nullptr;
     int* d_toff = nullptr;
-    int* d_seg0 = nullptr;
-    void* d_dargs = nullptr;             // CollideArgs<T>[ndom]
+    int* d_seg0 = nullptr;               // [2][ndom]: row segments, plane segments
+    void* d_dargs = nullptr;             // CollideArgs<T>[2][ndom]: row views, plane views
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
 
@@ -188,9 +189,12 @@ long long box_cells(const int32_t* b) {
 template <typename T>
 T* fptr(lbdem_batch* b, int d) { return (T*)b->f + b->views[d].f0; }
 
+// out[d]: domain d as rows of nz cells; out[ndom + d]: the same domain as nx rows
+// of ny nz cells (the plane view of the FP32 even phase, whose update touches
+// only each cell's own slots).
 template <typename T>
 void fill_dargs(lbdem_batch* b, std::vector<CollideArgs<T>>& out, T* f_base, double* ft_base) {
-    out.resize(b->ndom);
+    out.resize(2 * (size_t)b->ndom);
     for (int d = 0; d < b->ndom; ++d) {
         const DomView& v = b->views[d];
         CollideArgs<T>& a = out[d];
@@ -213,6 +217,16 @@ void fill_dargs(lbdem_batch* b, std::vector<CollideArgs<T>>& out, T* f_base, dou
         for (int k = 0; k < 3; ++k) a.g3[k] = (T)b->dom[d].body_force[k];
         a.dz = div_magic((unsigned)((v.g.nz + COLLIDE_SEGW - 1) / COLLIDE_SEGW));
         a.dy = div_magic((unsigned)v.g.ny);
+        CollideArgs<T>& p = out[b->ndom + d];
+        p = a;
+        const int plane = v.g.ny * v.g.nz;
+        p.g.ny = 1;
+        p.g.nz = plane;
+        p.dz = div_magic((unsigned)((plane + COLLIDE_SEGW - 1) / COLLIDE_SEGW));
+        p.dy = div_magic(1u);
+        p.flat_ny = v.g.ny;
+        p.flat_nz = v.g.nz;
+        p.dnz = div_magic((unsigned)v.g.nz);
     }
 }
 
@@ -222,12 +236,16 @@ bool any_force(const lbdem_batch* b) {
     return false;
 }
 
+// dargs: the [2][ndom] table of fill_dargs on the device.
 cudaError_t launch_k1(lbdem_batch* b, const void* dargs, bool odd, int bps) {
     const bool force = any_force(b);
     if (b->prec == LBDEM_PREC_FP64)
         return launch_collide_batch<double>((const CollideArgs<double>*)dargs, b->d_seg0, b->ndom, b->nseg, odd,
                                             force, bps, b->stream);
-    return launch_collide_batch<float>((const CollideArgs<float>*)dargs, b->d_seg0, b->ndom, b->nseg, odd, force,
+    if (!odd)   // plane segments
+        return launch_collide_batch<float>((const CollideArgs<float>*)dargs + b->ndom, b->d_seg0 + b->ndom, b->ndom,
+                                           b->nseg_plane, false, force, bps, b->stream);
+    return launch_collide_batch<float>((const CollideArgs<float>*)dargs, b->d_seg0, b->ndom, b->nseg, true, force,
                                        bps, b->stream);
 }
 
@@ -306,14 +324,15 @@ lbdem_status autotune(lbdem_batch* b) {
     };
     cudaError_t e = cudaMalloc(&fcopy, fbytes);
     if (e == cudaSuccess) e = cudaMalloc((void**)&ftcopy, ftbytes);
-    if (e == cudaSuccess) e = cudaMalloc(&dcopy, sizeof(CollideArgs<T>) * b->ndom);
+    if (e == cudaSuccess) e = cudaMalloc(&dcopy, sizeof(CollideArgs<T>) * 2 * (size_t)b->ndom);
     if (e == cudaSuccess) e = cudaEventCreate(&e0);
     if (e == cudaSuccess) e = cudaEventCreate(&e1);
     if (e == cudaSuccess) e = cudaMemcpyAsync(fcopy, b->f, fbytes, cudaMemcpyDeviceToDevice, b->stream);
     std::vector<CollideArgs<T>> args;
     if (e == cudaSuccess) {
         fill_dargs<T>(b, args, (T*)fcopy, ftcopy);
-        e = cudaMemcpyAsync(dcopy, args.data(), sizeof(CollideArgs<T>) * b->ndom, cudaMemcpyHostToDevice, b->stream);
+        e = cudaMemcpyAsync(dcopy, args.data(), sizeof(CollideArgs<T>) * args.size(), cudaMemcpyHostToDevice,
+                            b->stream);
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
     if (e != cudaSuccess) {
@@ -429,12 +448,12 @@ lbdem_status lbdem_batch_create(const lbdem_batch_config* cfg, int32_t ndomains,
     b->dom.assign(domains, domains + ndomains);
 
     // layout
-    long long slots = 0, tiles = 0, segs = 0;
+    long long slots = 0, tiles = 0, segs = 0, psegs = 0;
     size_t fo = 0, co = 0, uo = 0;
     b->views.resize(ndomains);
     b->soff.resize(ndomains);
     b->toff.resize(ndomains);
-    b->seg0.resize(ndomains);
+    b->seg0.resize(2 * (size_t)ndomains);
     b->cap.resize(ndomains);
     for (int d = 0; d < ndomains; ++d) {
         const lbdem_domain& dm = domains[d];
@@ -451,15 +470,18 @@ lbdem_status lbdem_batch_create(const lbdem_batch_config* cfg, int32_t ndomains,
         b->soff[d] = v.s0;
         b->toff[d] = v.t0;
         b->seg0[d] = (int)segs;
+        b->seg0[ndomains + d] = (int)psegs;
         b->cap[d] = dm.max_particles;
         slots += dm.max_particles;
         tiles += (long long)((dm.nx + TILE - 1) / TILE) * ((dm.ny + TILE - 1) / TILE) * ((dm.nz + TILE - 1) / TILE);
         segs += (long long)dm.nx * dm.ny * ((dm.nz + COLLIDE_SEGW - 1) / COLLIDE_SEGW);
+        psegs += (long long)dm.nx * (((long long)dm.ny * dm.nz + COLLIDE_SEGW - 1) / COLLIDE_SEGW);
         fo += round_up((size_t)Q * v.g.N, 32);
         co += round_up(v.g.N, 32);
         uo += round_up(3 * v.g.N, 32);
         b->ncells += v.g.N;
-        if (slots > 0x7fffffffLL || tiles > 0x7fffffffLL || segs > 0x7fffffffLL) {
+        if (slots > 0x7fffffffLL || tiles > 0x7fffffffLL || segs > 0x7fffffffLL || psegs > 0x7fffffffLL ||
+            (long long)dm.ny * dm.nz > 0x7fffffffLL) {
             delete b;
             return LBDEM_ERR_INVALID_ARG;
         }
@@ -467,6 +489,7 @@ lbdem_status lbdem_batch_create(const lbdem_batch_config* cfg, int32_t ndomains,
     b->nslots = (int)slots;
     b->ntiles = (int)tiles;
     b->nseg = segs;
+    b->nseg_plane = psegs;
     b->f_elems = fo;
     b->vox_elems = co;
     b->up_elems = uo;
@@ -510,9 +533,9 @@ lbdem_status lbdem_batch_create(const lbdem_batch_config* cfg, int32_t ndomains,
     TRY(dalloc(b, &b->d_views, sizeof(DomView) * ndomains));
     TRY(dalloc(b, &b->d_soff, sizeof(int) * ndomains));
     TRY(dalloc(b, &b->d_toff, sizeof(int) * ndomains));
-    TRY(dalloc(b, &b->d_seg0, sizeof(int) * ndomains));
+    TRY(dalloc(b, &b->d_seg0, sizeof(int) * 2 * (size_t)ndomains));
     TRY(dalloc(b, &b->d_dargs, (b->prec == LBDEM_PREC_FP64 ? sizeof(CollideArgs<double>) : sizeof(CollideArgs<float>)) *
-                                   ndomains));
+                                   2 * (size_t)ndomains));
     TRY(alloc_should_fail() ? cudaErrorMemoryAllocation : cudaMallocHost((void**)&b->h_stage, b->stage_bytes));
     TRY(alloc_should_fail() ? cudaErrorMemoryAllocation : cudaMallocHost((void**)&b->h_ft, sizeof(double) * 6 * capn));
     TRY(alloc_should_fail() ? cudaErrorMemoryAllocation : cudaMallocHost((void**)&b->h_err, sizeof(unsigned)));
@@ -547,15 +570,15 @@ lbdem_status lbdem_batch_create(const lbdem_batch_config* cfg, int32_t ndomains,
     TRY(cudaMemcpy(b->d_views, b->views.data(), sizeof(DomView) * ndomains, cudaMemcpyHostToDevice));
     TRY(cudaMemcpy(b->d_soff, b->soff.data(), sizeof(int) * ndomains, cudaMemcpyHostToDevice));
     TRY(cudaMemcpy(b->d_toff, b->toff.data(), sizeof(int) * ndomains, cudaMemcpyHostToDevice));
-    TRY(cudaMemcpy(b->d_seg0, b->seg0.data(), sizeof(int) * ndomains, cudaMemcpyHostToDevice));
+    TRY(cudaMemcpy(b->d_seg0, b->seg0.data(), sizeof(int) * b->seg0.size(), cudaMemcpyHostToDevice));
     if (b->prec == LBDEM_PREC_FP64) {
         std::vector<CollideArgs<double>> a;
         fill_dargs<double>(b, a, (double*)b->f, b->d_ft);
-        TRY(cudaMemcpy(b->d_dargs, a.data(), sizeof(a[0]) * ndomains, cudaMemcpyHostToDevice));
+        TRY(cudaMemcpy(b->d_dargs, a.data(), sizeof(a[0]) * a.size(), cudaMemcpyHostToDevice));
     } else {
         std::vector<CollideArgs<float>> a;
         fill_dargs<float>(b, a, (float*)b->f, b->d_ft);
-        TRY(cudaMemcpy(b->d_dargs, a.data(), sizeof(a[0]) * ndomains, cudaMemcpyHostToDevice));
+        TRY(cudaMemcpy(b->d_dargs, a.data(), sizeof(a[0]) * a.size(), cudaMemcpyHostToDevice));
     }
 
     if (b->njobs > 0) {

@@ -149,6 +149,11 @@ struct CollideArgs {
     T g3[3];                 // Guo body-force acceleration
     DivMagic dz, dy;         // division by the z-segments per row and by ny (set by the launchers)
     int probe_timeout;       // test hook: the first wait of every warp runs out (LBDEM_FLAG_PROBE_TIMEOUT)
+    // Plane view (FP32 batch, even phase): g describes the domain as nx rows of
+    // ny nz cells, so that 64-cell segments run across the z-rows of an x-plane;
+    // flat_ny, flat_nz are the true extents and dnz divides by flat_nz.  0: no view.
+    int flat_ny, flat_nz;
+    DivMagic dnz;
 };
 
 // Float table of a particle list, one row of XPF_STRIDE floats per particle:
@@ -283,6 +288,8 @@ cudaError_t launch_collide_stream(const CollideArgs<T>& a, bool odd, bool force,
 // Many domains in one persistent launch: dargs[d] describes domain d, its
 // segments (rows of nz cells cut into 64-cell pieces, x-major) are numbered
 // from seg0[d]; nseg segments in all.  blocks_per_sm <= 0: as many as fit.
+// The FP32 even phase takes plane views (CollideArgs::flat_nz != 0: rows of
+// ny nz cells, one per x-plane) with their own seg0 and nseg.
 template <typename T>
 cudaError_t launch_collide_batch(const CollideArgs<T>* dargs, const int* seg0, int ndom, long long nseg, bool odd,
                                  bool force, int blocks_per_sm, cudaStream_t s);
