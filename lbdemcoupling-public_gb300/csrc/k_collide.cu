@@ -1453,14 +1453,19 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
         float va[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f}, vb[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
         if (ka >= 0) terms(ka, ya, zta, fx.x, fy.x, fz.x, va);
         if (kb >= 0) terms(kb, yb, ztb, fx.y, fy.y, fz.y, vb);
-        if (__all_sync(FULL, ka < 0 || kb < 0 || ka == kb)) {
-            const int key = ka >= 0 ? ka : kb;
+        const bool one = __all_sync(FULL, ka < 0 || kb < 0 || ka == kb);   // one reduction for both cells
+        if (one) {
 #pragma unroll
             for (int q = 0; q < 6; ++q) va[q] += vb[q];
-            reduce_forces(a, key, va);
-        } else {
-            reduce_forces(a, ka, va);
-            reduce_forces(a, kb, vb);
+        }
+        // a single reduction site: this kernel's loop body is large enough for
+        // instruction-cache misses to cost more than the loop
+#pragma unroll 1
+        for (int pass = 0; pass < (one ? 1 : 2); ++pass) {
+            float v[6];
+#pragma unroll
+            for (int q = 0; q < 6; ++q) v[q] = pass == 0 ? va[q] : vb[q];
+            reduce_forces(a, pass == 0 ? (one && ka < 0 ? kb : ka) : kb, v);
         }
         return;
     }
