@@ -1225,8 +1225,10 @@ __device__ __noinline__ void whole_row_forces(const CollideArgs<float>& a, uint3
 // CollideArgs); a solid cell's true (y, z) is recovered from its index in the
 // plane, and force and torque take per-cell arms (a run may cross rows).  The
 // even phase touches only the cell's own slots, so a cell's populations do
-// not depend on how the cells are grouped into segments.
-template <bool ODD, bool FORCE, bool PER, bool MIS, bool STAGE_UP, bool FLAT = false>
+// not depend on how the cells are grouped into segments.  FOLD (batch): one
+// force-reduction site instead of three (the batch kernels' loop bodies miss the
+// instruction cache).
+template <bool ODD, bool FORCE, bool PER, bool MIS, bool STAGE_UP, bool FLAT = false, bool FOLD = false>
 __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& a, WarpStage<float, STAGE_UP>& st,
                                                       int b, int sx, int sy, int z0, int len, uint32_t srcrow,
                                                       unsigned long long lead, bool smap_ok, bool sbtab_ok) {
@@ -1490,7 +1492,21 @@ __device__ __forceinline__ void collide_segment_pairs(const CollideArgs<float>& 
         if (ka < 0) va[q] = 0.f;
         if (kb < 0) vb[q] = 0.f;
     }
-    if (__all_sync(FULL, ka < 0 || kb < 0 || ka == kb)) {
+    if constexpr (FOLD) {
+        const bool one = __all_sync(FULL, ka < 0 || kb < 0 || ka == kb);   // one reduction for both cells
+        if (one) {
+#pragma unroll
+            for (int q = 0; q < 5; ++q) va[q] += vb[q];
+        }
+#pragma unroll 1
+        for (int pass = 0; pass < (one ? 1 : 2); ++pass) {
+            float v[5];
+#pragma unroll
+            for (int q = 0; q < 5; ++q) v[q] = pass == 0 ? va[q] : vb[q];
+            const bool second = pass == 1 || (one && ka < 0);   // the run's cells are the b cells
+            reduce_runs(a, second ? kb : ka, v, second ? zb : za, sx, sy, zc, vrh, vrl0, vrl1, vslot);
+        }
+    } else if (__all_sync(FULL, ka < 0 || kb < 0 || ka == kb)) {
         const int key = ka >= 0 ? ka : kb;
 #pragma unroll
         for (int q = 0; q < 5; ++q) va[q] += vb[q];
@@ -1651,9 +1667,8 @@ k_collide_staged(const CollideArgs<T> a1, long long nseg, const CollideArgs<T>* 
         }
         if constexpr (sizeof(T) == 4) {
             // FP32 form: packed pairs of cells (batch, even phase: plane segments)
-            collide_segment_pairs<ODD, FORCE, PER, MIS, STAGE_UP, BATCH && !ODD>(a, st, b, sx, sy, z0, len, srcrow,
-                                                                                lead, smap_ok,
-                                                                                smem_tagmap<T, BATCH>());
+            collide_segment_pairs<ODD, FORCE, PER, MIS, STAGE_UP, BATCH && !ODD, BATCH>(
+                a, st, b, sx, sy, z0, len, srcrow, lead, smap_ok, smem_tagmap<T, BATCH>());
         } else {
             // FP64 form: one cell per lane at a time; force and torque per cell with
             // double atomics.  The segment's solid cells are taken first (pass 0
